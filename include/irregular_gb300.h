@@ -1,0 +1,199 @@
+/*
+ * irregular_gb300.h -- C ABI of the GB300 irregular-reduction library.
+ *
+ * The irregular-reduction pattern: a node array, an edge list, and a per-edge
+ * user function whose contributions are scatter-added into a per-node
+ * reduction array.  This header is the drop-in boundary for the reference's
+ * IrregularRuntime (moldyn/irregular/irregular_runtime.h:12-112) and its
+ * user-function plugin (moldyn/irregular.h, miniMD/irregular.h).  Every entry
+ * point takes plain pointers and sizes, returns an int status (IRR_OK == 0)
+ * and never calls exit(); the reference exit()s on any CUDA or MPI error
+ * (lib/macro.h:9-16).
+ *
+ * Threading: a handle is used by one host thread at a time.  Work is issued
+ * on the handle's CUDA stream (irr_set_stream); calls that return data to the
+ * host synchronise that stream.
+ */
+#ifndef IRREGULAR_GB300_H_
+#define IRREGULAR_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define IRR_API __attribute__((visibility("default")))
+#else
+#define IRR_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+enum irr_status {
+    IRR_OK = 0,
+    IRR_ERR_ARG = 1,      /* null pointer, negative size, unknown id or format     */
+    IRR_ERR_INDEX = 2,    /* an edge endpoint outside [0, num_nodes)                */
+    IRR_ERR_STATE = 3,    /* call out of order (e.g. step before nodes and edges)   */
+    IRR_ERR_CUDA = 4,     /* a CUDA runtime call failed (text in irr_last_error)    */
+    IRR_ERR_NOMEM = 5,    /* device or host allocation failed                       */
+    IRR_ERR_CAPACITY = 6, /* a size above a documented limit                        */
+    IRR_ERR_DEVICE = 7,   /* a kernel reported a fault through its status word      */
+    IRR_ERR_BUDGET = 8    /* a job does not fit the admission budget                */
+};
+
+/* --------------------------------------------------- built-in user functions
+ * Per-edge functions compiled into the library, selected by index the way the
+ * reference selects map_function_table[map_idx] (moldyn/irregular.h:116-118,
+ * irregular_runtime.cu:493-501).  All three are the Lennard-Jones law in the
+ * reference's form d * (r^-14 - r^-8 / 2) (LJ force / 48 at eps = sigma = 1),
+ * +f to idx0 and -f to idx1, applied when r^2 < cutoff^2.
+ */
+enum irr_map {
+    /* moldyn `map` (moldyn/irregular.h:26-107): minimum image in a cubic box.
+     * Parameter block: struct { double side; double cutoffRadius; }
+     * (struct para, moldyn/moldyn.h:39-43). */
+    IRR_MAP_LJ_MOLDYN = 0,
+    /* miniMD `map1` (miniMD/irregular.h:109-163): open boundaries.
+     * Parameter block: double cutforcesq (miniMD/ljs.cu:123). */
+    IRR_MAP_LJ_MINIMD = 1,
+    /* map1 with moldyn's minimum image (no reference counterpart: miniMD
+     * builds no ghosts).  Parameter block: struct { double cutforcesq;
+     * double side; }. */
+    IRR_MAP_LJ_MINIMD_PBC = 2
+};
+
+/* `reduce` (moldyn/irregular.h:109-114): float3 +=. */
+enum irr_reduce { IRR_REDUCE_SUM = 0 };
+
+/* Execution strategy. */
+enum irr_exec {
+    /* Caller's node order and edge list as given; one thread per edge,
+     * contributions added with global float4 atomics.  The straightforward
+     * GPU form of compute_gpu (moldyn/irregular/gpu_kernel.cu:21-103). */
+    IRR_EXEC_PLAIN = 0,
+    /* GPU partitioner (Morton order, shared-memory-sized node blocks, edges
+     * binned by owning block) and the tiled owner-computes kernel.  Each node
+     * sums its own contributions in registers with compensated (two-sum)
+     * partials; no atomics; results are bitwise reproducible. */
+    IRR_EXEC_PARTITIONED = 1
+};
+
+/* Node-data formats: the node_data_elm_size the reference passes. */
+enum irr_node_format {
+    IRR_NODES_F32X3 = 12, /* float xyz                                              */
+    IRR_NODES_F32X4 = 16, /* float xyzw (w ignored)                                 */
+    IRR_NODES_F64X3 = 24  /* double xyz: moldyn point_data, miniMD nodes            */
+};
+
+/* Result formats: the reduction_elm_size of get_reduction_result. */
+enum irr_result_format {
+    IRR_RESULT_F32X3 = 12, /* VALUE = float3 (moldyn/irregular/parameters.h:21-28) */
+    IRR_RESULT_F32X4 = 16, /* float xyz + 0                                        */
+    IRR_RESULT_F64X3 = 24  /* double xyz (moldyn's f[][3] buffer)                  */
+};
+
+typedef struct irr_config {
+    int device;        /* CUDA device ordinal                                        */
+    int exec;          /* enum irr_exec                                              */
+    int map_idx;       /* enum irr_map                                               */
+    int reduce_idx;    /* enum irr_reduce                                            */
+    int block_nodes;   /* partitioned: nodes per block (power of two, 64..4096);
+                          0 = tuned default                                          */
+    int lanes_per_row; /* partitioned: lanes summing one node's row (4, 8, 16, 32);
+                          0 = tuned default                                          */
+    int reorder;       /* partitioned: 1 = Morton order (default), 0 = keep the
+                          caller's order (blocks are then cut from it)              */
+    int stage_smem;    /* partitioned: 1 = copy each block's positions into shared
+                          memory with a bulk (TMA) copy, 0 = read them through L1;
+                          -1 = tuned default                                         */
+    int reserved[8];
+} irr_config;
+
+typedef struct irr_handle irr_handle;
+
+/* Counts and sizes of a prepared handle. */
+typedef struct irr_info {
+    int64_t num_nodes;
+    int64_t num_edges;
+    int64_t num_entries;     /* directed entries held (2 * edges when partitioned) */
+    int64_t num_blocks;      /* node blocks (partitioned)                          */
+    int64_t device_bytes;    /* device memory held by the handle                   */
+    int32_t block_nodes;
+    int32_t lanes_per_row;
+    int32_t stage_smem;
+    int32_t exec;
+} irr_info;
+
+IRR_API void irr_config_default(irr_config *cfg);
+IRR_API const char *irr_status_string(int status);
+
+/* IrregularRuntime::IrregularRuntime (irregular_runtime.cu:17-48).  Creates
+ * the handle and its stream on cfg->device; holds no node or edge data yet. */
+IRR_API int irr_create(const irr_config *cfg, irr_handle **out);
+/* IrregularRuntime::~IrregularRuntime (irregular_runtime.cu:446-458). */
+IRR_API int irr_destroy(irr_handle *h);
+/* Text of the last failure on this handle ("" when none). */
+IRR_API const char *irr_last_error(const irr_handle *h);
+
+/* Issue work on `stream` (a cudaStream_t) instead of the handle's own. */
+IRR_API int irr_set_stream(irr_handle *h, void *stream);
+/* set_map_idx / set_reduce_idx (irregular_runtime.cu:493-501). */
+IRR_API int irr_set_map(irr_handle *h, int map_idx);
+IRR_API int irr_set_reduce(irr_handle *h, int reduce_idx);
+/* The `parameter` block of the constructor, interpreted per map (above). */
+IRR_API int irr_set_params(irr_handle *h, const void *param, int param_size);
+
+/* The constructor's edges (EDGE = {int idx0, idx1}, moldyn/irregular/
+ * data_type.h:5-9), host memory, 2*num_edges int32.  Copied; the caller's
+ * array is never modified (the reference renumbers it in place,
+ * reorder.cpp:160-172).  Endpoints are validated (IRR_ERR_INDEX) once the
+ * node count is known. */
+IRR_API int irr_set_edges(irr_handle *h, const int32_t *edges, int64_t num_edges);
+/* Same, from device memory. */
+IRR_API int irr_set_edges_device(irr_handle *h, const int32_t *d_edges, int64_t num_edges);
+
+/* The constructor's node data, and reset_node_data (irregular_runtime.cu:
+ * 436-439) on later calls: num_nodes records of elm_size bytes (enum
+ * irr_node_format), host memory, in the caller's node order.  Positions are
+ * used in float; the first three components are the coordinates.  Changing
+ * num_nodes after irr_init is IRR_ERR_STATE. */
+IRR_API int irr_set_nodes(irr_handle *h, const void *node_data, int elm_size, int64_t num_nodes);
+/* Same, from device memory. */
+IRR_API int irr_set_nodes_device(irr_handle *h, const void *d_node_data, int elm_size,
+                         int64_t num_nodes);
+
+/* IrregularInit (irregular_runtime.cu:50-193) plus the first split()
+ * (:195-272): validates edges, runs the GPU partitioner (partitioned mode)
+ * and lays the data out for the kernel.  Called by irr_step when needed. */
+IRR_API int irr_init(irr_handle *h);
+
+/* IrregularStart (irregular_runtime.cu:311-391): one reduction over all
+ * edges with the current node data.  Enqueued on the handle's stream; the
+ * host does not wait. */
+IRR_API int irr_step(irr_handle *h);
+
+/* get_reduction_result (irregular_runtime.cu:393-411): the per-node result
+ * in the caller's node order, elm_size bytes per node (enum
+ * irr_result_format), into host memory.  Synchronises the stream and reports
+ * any device-side fault. */
+IRR_API int irr_get_result(irr_handle *h, void *out, int elm_size);
+/* Same, into device memory; enqueued, does not synchronise. */
+IRR_API int irr_get_result_device(irr_handle *h, void *d_out, int elm_size);
+
+/* Waits for the handle's stream and reports any device-side fault. */
+IRR_API int irr_sync(irr_handle *h);
+IRR_API int irr_get_info(const irr_handle *h, irr_info *info);
+
+/* Partition outputs (partitioned mode, after irr_init), copied to host:
+ * perm[new] = old node id, row_off[num_nodes + 1] (int64) and col[num_entries]
+ * (the neighbour's new id of every directed entry, rows in node order,
+ * entries within a row in edge-list order, idx0 side first).  Any pointer may
+ * be NULL. */
+IRR_API int irr_get_partition(irr_handle *h, int32_t *perm, int64_t *row_off, int32_t *col);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

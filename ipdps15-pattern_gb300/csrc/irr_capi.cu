@@ -1,0 +1,583 @@
+// irr_capi.cu -- the C ABI (include/irregular_gb300.h) over the kernels.
+//
+// One handle = one IrregularRuntime (moldyn/irregular/irregular_runtime.h:
+// 12-112) on one GPU.  The reference's MPI split, CPU/GPU work sharing and
+// per-iteration re-split are not reproduced: node data and the partition stay
+// resident on the device, and a step is one kernel launch.
+#include <cmath>
+#include <cstdarg>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "irr_internal.cuh"
+#include "../../include/irregular_gb300.h"
+
+using namespace irr;
+
+struct irr_handle {
+    irr_config cfg{};
+    int device = 0;
+    int sms = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    std::string err;
+
+    int map_idx = IRR_MAP_LJ_MOLDYN;
+    int reduce_idx = IRR_REDUCE_SUM;
+    std::vector<unsigned char> param;
+    bool have_law = false;
+    LawParams law{};
+
+    int64_t n = -1;
+    int64_t e = -1;
+    void* d_raw = nullptr;       // node records as the caller passed them
+    size_t raw_cap = 0;
+    int raw_elm = 0;
+    bool raw_pending = false;    // d_raw holds records not yet converted
+    int2* d_edges = nullptr;     // caller's half list
+    size_t edges_cap = 0;
+
+    bool inited = false;
+    TiledShape shape{};
+    float4* d_pos = nullptr;     // execution order
+    float4* d_force = nullptr;
+    PartitionOut part{};
+    InstDesc* d_inst = nullptr;
+    WorkItem* d_items = nullptr;
+    int num_items = 0;
+    int* d_status = nullptr;
+    void* d_out = nullptr;       // result staging for host reads
+    size_t out_cap = 0;
+    int64_t dev_bytes = 0;
+};
+
+namespace {
+
+int fail(irr_handle* h, int code, const char* fmt, ...)
+{
+    if (h) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof(buf), fmt, ap);
+        va_end(ap);
+        h->err = buf;
+    }
+    return code;
+}
+
+int cuda_fail(irr_handle* h, cudaError_t e, const char* what)
+{
+    cudaGetLastError();  // clear a non-sticky error
+    const int code = (e == cudaErrorMemoryAllocation) ? IRR_ERR_NOMEM : IRR_ERR_CUDA;
+    return fail(h, code, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define H_CUDA(h, expr, what)                                 \
+    do {                                                      \
+        cudaError_t e_ = (expr);                              \
+        if (e_ != cudaSuccess) return cuda_fail((h), e_, what); \
+    } while (0)
+
+template <class T>
+void dfree(T*& p)
+{
+    if (p) cudaFree((void*)p);
+    p = nullptr;
+}
+
+void free_layout(irr_handle* h)
+{
+    dfree(h->d_pos);
+    dfree(h->d_force);
+    dfree(h->part.perm);
+    dfree(h->part.inv);
+    dfree(h->part.row_off);
+    dfree(h->part.col);
+    dfree(h->d_inst);
+    dfree(h->d_items);
+    h->num_items = 0;
+    h->inited = false;
+}
+
+bool valid_node_elm(int elm) { return elm == 12 || elm == 16 || elm == 24; }
+
+// Law parameters from the reference's parameter block for the selected map.
+int make_law(irr_handle* h)
+{
+    const unsigned char* p = h->param.data();
+    const size_t sz = h->param.size();
+    double rc2d = 0, side = 0;
+    int periodic = 0;
+    switch (h->map_idx) {
+    case IRR_MAP_LJ_MOLDYN: {  // struct para {double side; double cutoffRadius;}
+        if (sz < 16) return fail(h, IRR_ERR_ARG, "moldyn map needs a 16-byte {side, cutoffRadius} block");
+        double rc;
+        memcpy(&side, p, 8);
+        memcpy(&rc, p + 8, 8);
+        rc2d = rc * rc;  // moldyn/irregular.h:40 cutoffSquare = cutoffRadius * cutoffRadius
+        periodic = 1;
+        break;
+    }
+    case IRR_MAP_LJ_MINIMD:  // double cutforcesq
+        if (sz < 8) return fail(h, IRR_ERR_ARG, "miniMD map needs an 8-byte cutforcesq");
+        memcpy(&rc2d, p, 8);
+        break;
+    case IRR_MAP_LJ_MINIMD_PBC:  // {double cutforcesq; double side;}
+        if (sz < 16) return fail(h, IRR_ERR_ARG, "miniMD PBC map needs a 16-byte {cutforcesq, side} block");
+        memcpy(&rc2d, p, 8);
+        memcpy(&side, p + 8, 8);
+        periodic = 1;
+        break;
+    default:
+        return fail(h, IRR_ERR_ARG, "unknown map index %d", h->map_idx);
+    }
+    if (!(rc2d >= 0.0) || !std::isfinite(rc2d)) return fail(h, IRR_ERR_ARG, "cutoff^2 must be finite and >= 0");
+    if (periodic && !(side > 0.0 && std::isfinite(side))) return fail(h, IRR_ERR_ARG, "box side must be finite and > 0");
+    LawParams L{};
+    L.rc2d = rc2d;
+    L.rc2 = (float)rc2d;
+    L.rc2_lo = (float)(rc2d * (1.0 - 1.0 / 262144.0));
+    L.rc2_hi = (float)(rc2d * (1.0 + 1.0 / 262144.0));
+    L.periodic = periodic;
+    L.side = side;
+    L.halfd = 0.5 * side;
+    L.half = (float)(0.5 * side);
+    L.side_hi = (float)side;
+    L.side_lo = (float)(side - (double)L.side_hi);
+    h->law = L;
+    h->have_law = true;
+    return IRR_OK;
+}
+
+int upload_inst(irr_handle* h)
+{
+    if (!h->inited || h->cfg.exec != IRR_EXEC_PARTITIONED) return IRR_OK;
+    InstDesc d{};
+    d.pos = h->d_pos;
+    d.row_off = h->part.row_off;
+    d.col = h->part.col;
+    d.force = h->d_force;
+    d.law = h->law;
+    d.n = h->n;
+    H_CUDA(h, cudaMemcpyAsync(h->d_inst, &d, sizeof(d), cudaMemcpyHostToDevice, h->stream),
+           "upload instance descriptor");
+    H_CUDA(h, cudaStreamSynchronize(h->stream), "upload instance descriptor");
+    return IRR_OK;
+}
+
+int check_status(irr_handle* h)
+{
+    int st = 0;
+    H_CUDA(h, cudaMemcpyAsync(&st, h->d_status, sizeof(int), cudaMemcpyDeviceToHost, h->stream),
+           "read status");
+    H_CUDA(h, cudaStreamSynchronize(h->stream), "synchronise");
+    if (st & kStatusBadIndex) {
+        cudaMemsetAsync(h->d_status, 0, sizeof(int), h->stream);
+        return fail(h, IRR_ERR_INDEX, "an edge endpoint is outside [0, %lld)", (long long)h->n);
+    }
+    if (st) {
+        cudaMemsetAsync(h->d_status, 0, sizeof(int), h->stream);
+        return fail(h, IRR_ERR_DEVICE, "device status 0x%x (a bounded wait gave up)", st);
+    }
+    return IRR_OK;
+}
+
+int ensure_raw(irr_handle* h, size_t bytes)
+{
+    if (bytes <= h->raw_cap) return IRR_OK;
+    dfree(h->d_raw);
+    h->raw_cap = 0;
+    H_CUDA(h, cudaMalloc(&h->d_raw, bytes), "allocate node staging");
+    h->raw_cap = bytes;
+    return IRR_OK;
+}
+
+int set_nodes_common(irr_handle* h, const void* src, int elm, int64_t n, cudaMemcpyKind kind)
+{
+    if (!h || (!src && n > 0) || n < 0) return fail(h, IRR_ERR_ARG, "bad node data arguments");
+    if (!valid_node_elm(elm)) return fail(h, IRR_ERR_ARG, "node elm_size %d: use 12, 16 or 24", elm);
+    if (n > 0x7fffffffLL) return fail(h, IRR_ERR_CAPACITY, "more than 2^31-1 nodes");
+    if (h->inited && n != h->n) return fail(h, IRR_ERR_STATE, "node count changed after init (%lld -> %lld)", (long long)h->n, (long long)n);
+    int rc = ensure_raw(h, (size_t)(n > 0 ? n : 1) * (size_t)elm);
+    if (rc) return rc;
+    if (n > 0)
+        H_CUDA(h, cudaMemcpyAsync(h->d_raw, src, (size_t)n * elm, kind, h->stream), "copy node data");
+    h->n = n;
+    h->raw_elm = elm;
+    h->raw_pending = true;
+    if (h->inited) {
+        // reset_node_data: convert (and gather into partition order) now
+        H_CUDA(h, launch_load_nodes(h->d_raw, elm, h->part.perm, n, h->d_pos, h->stream),
+               "load node data");
+        h->raw_pending = false;
+    }
+    return IRR_OK;
+}
+
+int set_edges_common(irr_handle* h, const int32_t* src, int64_t e, cudaMemcpyKind kind)
+{
+    if (!h || (!src && e > 0) || e < 0) return fail(h, IRR_ERR_ARG, "bad edge arguments");
+    if (e > 0x7fffffffLL) return fail(h, IRR_ERR_CAPACITY, "more than 2^31-1 edges");
+    const size_t bytes = (size_t)(e > 0 ? e : 1) * sizeof(int2);
+    if (bytes > h->edges_cap) {
+        dfree(h->d_edges);
+        h->edges_cap = 0;
+        H_CUDA(h, cudaMalloc(&h->d_edges, bytes), "allocate edges");
+        h->edges_cap = bytes;
+    }
+    if (e > 0) H_CUDA(h, cudaMemcpyAsync(h->d_edges, src, (size_t)e * sizeof(int2), kind, h->stream), "copy edges");
+    h->e = e;
+    if (h->inited) {
+        // new edge list: the layout is rebuilt at the next init
+        const int64_t n = h->n;
+        if (!h->raw_pending) {
+            // keep the current node data: write it back in the caller's order
+            int rc = ensure_raw(h, (size_t)(n > 0 ? n : 1) * 16);
+            if (rc) return rc;
+            H_CUDA(h, launch_store_result(h->d_pos, h->part.inv, n, 16, h->d_raw, h->stream), "save node data");
+            h->raw_elm = 16;
+            h->raw_pending = true;
+        }
+        free_layout(h);
+    }
+    return IRR_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void irr_config_default(irr_config* cfg)
+{
+    if (!cfg) return;
+    memset(cfg, 0, sizeof(*cfg));
+    cfg->device = 0;
+    cfg->exec = IRR_EXEC_PARTITIONED;
+    cfg->map_idx = IRR_MAP_LJ_MOLDYN;
+    cfg->reduce_idx = IRR_REDUCE_SUM;
+    cfg->block_nodes = 0;
+    cfg->lanes_per_row = 0;
+    cfg->reorder = 1;
+    cfg->stage_smem = -1;
+}
+
+const char* irr_status_string(int status)
+{
+    switch (status) {
+    case IRR_OK: return "ok";
+    case IRR_ERR_ARG: return "bad argument";
+    case IRR_ERR_INDEX: return "edge endpoint out of range";
+    case IRR_ERR_STATE: return "call out of order";
+    case IRR_ERR_CUDA: return "CUDA error";
+    case IRR_ERR_NOMEM: return "out of memory";
+    case IRR_ERR_CAPACITY: return "size above limit";
+    case IRR_ERR_DEVICE: return "device-side fault reported";
+    case IRR_ERR_BUDGET: return "over admission budget";
+    default: return "unknown status";
+    }
+}
+
+int irr_create(const irr_config* cfg, irr_handle** out)
+{
+    if (!out) return IRR_ERR_ARG;
+    *out = nullptr;
+    irr_config c;
+    if (cfg)
+        c = *cfg;
+    else
+        irr_config_default(&c);
+    if (c.exec != IRR_EXEC_PLAIN && c.exec != IRR_EXEC_PARTITIONED) return IRR_ERR_ARG;
+    if (c.reduce_idx != IRR_REDUCE_SUM) return IRR_ERR_ARG;
+    if (c.map_idx < IRR_MAP_LJ_MOLDYN || c.map_idx > IRR_MAP_LJ_MINIMD_PBC) return IRR_ERR_ARG;
+    if (c.block_nodes != 0 && (c.block_nodes < 64 || c.block_nodes > 4096 || (c.block_nodes & (c.block_nodes - 1))))
+        return IRR_ERR_ARG;
+    if (c.lanes_per_row != 0 && c.lanes_per_row != 4 && c.lanes_per_row != 8 && c.lanes_per_row != 16 &&
+        c.lanes_per_row != 32)
+        return IRR_ERR_ARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return IRR_ERR_CUDA;
+    }
+    if (c.device < 0 || c.device >= ndev) return IRR_ERR_ARG;
+    irr_handle* h = new (std::nothrow) irr_handle();
+    if (!h) return IRR_ERR_NOMEM;
+    h->cfg = c;
+    h->device = c.device;
+    h->map_idx = c.map_idx;
+    h->reduce_idx = c.reduce_idx;
+    if (cudaSetDevice(h->device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, h->device) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMalloc(&h->d_status, sizeof(int)) != cudaSuccess ||
+        cudaMemset(h->d_status, 0, sizeof(int)) != cudaSuccess) {
+        cudaGetLastError();
+        if (h->own_stream) cudaStreamDestroy(h->own_stream);
+        if (h->d_status) cudaFree(h->d_status);
+        delete h;
+        return IRR_ERR_CUDA;
+    }
+    h->stream = h->own_stream;
+    h->shape.lanes_per_row = c.lanes_per_row ? c.lanes_per_row : 8;
+    h->shape.block_nodes = c.block_nodes ? c.block_nodes : 1024;
+    h->shape.stage_smem = c.stage_smem < 0 ? 0 : (c.stage_smem ? 1 : 0);
+    if (h->shape.stage_smem && h->shape.block_nodes > kMaxStageNodes) h->shape.block_nodes = kMaxStageNodes;
+    *out = h;
+    return IRR_OK;
+}
+
+int irr_destroy(irr_handle* h)
+{
+    if (!h) return IRR_ERR_ARG;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    free_layout(h);
+    dfree(h->d_raw);
+    dfree(h->d_edges);
+    dfree(h->d_status);
+    dfree(h->d_out);
+    if (h->own_stream) cudaStreamDestroy(h->own_stream);
+    delete h;
+    return IRR_OK;
+}
+
+const char* irr_last_error(const irr_handle* h) { return h ? h->err.c_str() : "null handle"; }
+
+int irr_set_stream(irr_handle* h, void* stream)
+{
+    if (!h) return IRR_ERR_ARG;
+    h->stream = stream ? (cudaStream_t)stream : h->own_stream;
+    return IRR_OK;
+}
+
+int irr_set_map(irr_handle* h, int map_idx)
+{
+    if (!h) return IRR_ERR_ARG;
+    if (map_idx < IRR_MAP_LJ_MOLDYN || map_idx > IRR_MAP_LJ_MINIMD_PBC)
+        return fail(h, IRR_ERR_ARG, "unknown map index %d", map_idx);
+    h->map_idx = map_idx;
+    h->have_law = false;
+    if (!h->param.empty()) {
+        int rc = make_law(h);
+        if (rc) return rc;
+        return upload_inst(h);
+    }
+    return IRR_OK;
+}
+
+int irr_set_reduce(irr_handle* h, int reduce_idx)
+{
+    if (!h) return IRR_ERR_ARG;
+    if (reduce_idx != IRR_REDUCE_SUM) return fail(h, IRR_ERR_ARG, "unknown reduce index %d", reduce_idx);
+    h->reduce_idx = reduce_idx;
+    return IRR_OK;
+}
+
+int irr_set_params(irr_handle* h, const void* param, int param_size)
+{
+    if (!h) return IRR_ERR_ARG;
+    if (!param || param_size <= 0) return fail(h, IRR_ERR_ARG, "empty parameter block");
+    cudaSetDevice(h->device);
+    std::vector<unsigned char> keep = h->param;
+    h->param.assign((const unsigned char*)param, (const unsigned char*)param + param_size);
+    int rc = make_law(h);
+    if (rc) {
+        h->param = keep;
+        return rc;
+    }
+    return upload_inst(h);
+}
+
+int irr_set_edges(irr_handle* h, const int32_t* edges, int64_t num_edges)
+{
+    if (!h) return IRR_ERR_ARG;
+    cudaSetDevice(h->device);
+    return set_edges_common(h, edges, num_edges, cudaMemcpyHostToDevice);
+}
+
+int irr_set_edges_device(irr_handle* h, const int32_t* d_edges, int64_t num_edges)
+{
+    if (!h) return IRR_ERR_ARG;
+    cudaSetDevice(h->device);
+    return set_edges_common(h, d_edges, num_edges, cudaMemcpyDeviceToDevice);
+}
+
+int irr_set_nodes(irr_handle* h, const void* node_data, int elm_size, int64_t num_nodes)
+{
+    if (!h) return IRR_ERR_ARG;
+    cudaSetDevice(h->device);
+    return set_nodes_common(h, node_data, elm_size, num_nodes, cudaMemcpyHostToDevice);
+}
+
+int irr_set_nodes_device(irr_handle* h, const void* d_node_data, int elm_size, int64_t num_nodes)
+{
+    if (!h) return IRR_ERR_ARG;
+    cudaSetDevice(h->device);
+    return set_nodes_common(h, d_node_data, elm_size, num_nodes, cudaMemcpyDeviceToDevice);
+}
+
+int irr_init(irr_handle* h)
+{
+    if (!h) return IRR_ERR_ARG;
+    if (h->inited) return IRR_OK;
+    if (h->n < 0) return fail(h, IRR_ERR_STATE, "irr_init before irr_set_nodes");
+    if (h->e < 0) return fail(h, IRR_ERR_STATE, "irr_init before irr_set_edges");
+    if (!h->have_law) return fail(h, IRR_ERR_STATE, "irr_init before irr_set_params");
+    cudaSetDevice(h->device);
+    cudaStream_t s = h->stream;
+    const int64_t n = h->n, e = h->e;
+    H_CUDA(h, launch_validate_edges(h->d_edges, e, n, h->d_status, s), "validate edges");
+    int rc = check_status(h);
+    if (rc) return rc;
+    const size_t nb = (size_t)(n > 0 ? n : 1) * sizeof(float4);
+    H_CUDA(h, cudaMalloc(&h->d_pos, nb), "allocate positions");
+    H_CUDA(h, cudaMalloc(&h->d_force, nb), "allocate results");
+    H_CUDA(h, cudaMemsetAsync(h->d_force, 0, nb, s), "clear results");
+    h->dev_bytes = 2 * (int64_t)nb + (int64_t)h->raw_cap;
+    if (h->cfg.exec == IRR_EXEC_PLAIN) {
+        H_CUDA(h, launch_load_nodes(h->d_raw, h->raw_elm, nullptr, n, h->d_pos, s), "load node data");
+        h->raw_pending = false;
+        h->dev_bytes += (int64_t)h->edges_cap;
+        h->inited = true;
+        H_CUDA(h, cudaStreamSynchronize(s), "init");
+        return IRR_OK;
+    }
+    // partitioned: positions in the caller's order feed the partitioner
+    H_CUDA(h, launch_load_nodes(h->d_raw, h->raw_elm, nullptr, n, h->d_pos, s), "load node data");
+    PartitionOut p;
+    cudaError_t pe = build_partition(h->d_pos, n, h->d_edges, e, h->cfg.reorder, &p, s);
+    h->part = p;
+    if (pe != cudaSuccess) {
+        free_layout(h);
+        return cuda_fail(h, pe, "build partition");
+    }
+    H_CUDA(h, launch_load_nodes(h->d_raw, h->raw_elm, h->part.perm, n, h->d_pos, s), "gather node data");
+    h->raw_pending = false;
+    // node blocks -> work items
+    const int K = h->shape.block_nodes;
+    std::vector<WorkItem> items;
+    for (int64_t r0 = 0; r0 < n; r0 += K) {
+        WorkItem w{};
+        w.inst = 0;
+        w.row0 = (int32_t)r0;
+        w.nrows = (int32_t)(n - r0 < K ? n - r0 : K);
+        items.push_back(w);
+    }
+    h->num_items = (int)items.size();
+    H_CUDA(h, cudaMalloc(&h->d_items, sizeof(WorkItem) * (items.size() ? items.size() : 1)), "allocate work items");
+    if (!items.empty())
+        H_CUDA(h, cudaMemcpyAsync(h->d_items, items.data(), sizeof(WorkItem) * items.size(),
+                                  cudaMemcpyHostToDevice, s), "upload work items");
+    H_CUDA(h, cudaMalloc(&h->d_inst, sizeof(InstDesc)), "allocate instance descriptor");
+    h->shape.periodic = h->law.periodic;
+    h->inited = true;
+    rc = upload_inst(h);
+    if (rc) return rc;
+    h->dev_bytes += (int64_t)(2 * n + n + 1) * 4 + 2 * e * 4;
+    // the half list is not needed by the partitioned kernel
+    dfree(h->d_edges);
+    h->edges_cap = 0;
+    H_CUDA(h, cudaStreamSynchronize(s), "init");
+    return IRR_OK;
+}
+
+int irr_step(irr_handle* h)
+{
+    if (!h) return IRR_ERR_ARG;
+    if (!h->inited) {
+        int rc = irr_init(h);
+        if (rc) return rc;
+    }
+    cudaSetDevice(h->device);
+    if (h->raw_pending) {
+        H_CUDA(h, launch_load_nodes(h->d_raw, h->raw_elm, h->part.perm, h->n, h->d_pos, h->stream), "load node data");
+        h->raw_pending = false;
+    }
+    if (h->cfg.exec == IRR_EXEC_PLAIN) {
+        H_CUDA(h, cudaMemsetAsync(h->d_force, 0, (size_t)(h->n > 0 ? h->n : 1) * sizeof(float4), h->stream), "clear results");
+        H_CUDA(h, launch_plain(h->d_pos, h->d_edges, h->e, h->d_force, h->law, h->stream), "plain kernel");
+        return IRR_OK;
+    }
+    H_CUDA(h, launch_tiled(h->shape, h->d_inst, h->d_items, h->num_items, nullptr, 0, h->d_status, h->stream),
+           "tiled kernel");
+    return IRR_OK;
+}
+
+int irr_get_result_device(irr_handle* h, void* d_out, int elm_size)
+{
+    if (!h || !d_out) return fail(h, IRR_ERR_ARG, "null output");
+    if (elm_size != 12 && elm_size != 16 && elm_size != 24) return fail(h, IRR_ERR_ARG, "result elm_size %d: use 12, 16 or 24", elm_size);
+    if (!h->inited) return fail(h, IRR_ERR_STATE, "no result before irr_step");
+    cudaSetDevice(h->device);
+    H_CUDA(h, launch_store_result(h->d_force, h->part.inv, h->n, elm_size, d_out, h->stream), "store result");
+    return IRR_OK;
+}
+
+int irr_get_result(irr_handle* h, void* out, int elm_size)
+{
+    if (!h || (!out && h->n > 0)) return fail(h, IRR_ERR_ARG, "null output");
+    if (elm_size != 12 && elm_size != 16 && elm_size != 24) return fail(h, IRR_ERR_ARG, "result elm_size %d: use 12, 16 or 24", elm_size);
+    if (!h->inited) return fail(h, IRR_ERR_STATE, "no result before irr_step");
+    cudaSetDevice(h->device);
+    const size_t bytes = (size_t)(h->n > 0 ? h->n : 1) * elm_size;
+    if (bytes > h->out_cap) {
+        dfree(h->d_out);
+        h->out_cap = 0;
+        H_CUDA(h, cudaMalloc(&h->d_out, bytes), "allocate result staging");
+        h->out_cap = bytes;
+    }
+    int rc = irr_get_result_device(h, h->d_out, elm_size);
+    if (rc) return rc;
+    if (h->n > 0)
+        H_CUDA(h, cudaMemcpyAsync(out, h->d_out, (size_t)h->n * elm_size, cudaMemcpyDeviceToHost, h->stream), "copy result");
+    return check_status(h);
+}
+
+int irr_sync(irr_handle* h)
+{
+    if (!h) return IRR_ERR_ARG;
+    cudaSetDevice(h->device);
+    return check_status(h);
+}
+
+int irr_get_info(const irr_handle* h, irr_info* info)
+{
+    if (!h || !info) return IRR_ERR_ARG;
+    memset(info, 0, sizeof(*info));
+    info->num_nodes = h->n;
+    info->num_edges = h->e;
+    info->num_entries = h->cfg.exec == IRR_EXEC_PARTITIONED ? 2 * (h->e > 0 ? h->e : 0) : (h->e > 0 ? h->e : 0);
+    info->num_blocks = h->num_items;
+    info->device_bytes = h->dev_bytes;
+    info->block_nodes = h->shape.block_nodes;
+    info->lanes_per_row = h->shape.lanes_per_row;
+    info->stage_smem = h->shape.stage_smem;
+    info->exec = h->cfg.exec;
+    return IRR_OK;
+}
+
+int irr_get_partition(irr_handle* h, int32_t* perm, int64_t* row_off, int32_t* col)
+{
+    if (!h) return IRR_ERR_ARG;
+    if (h->cfg.exec != IRR_EXEC_PARTITIONED) return fail(h, IRR_ERR_STATE, "handle is not partitioned");
+    if (!h->inited) return fail(h, IRR_ERR_STATE, "no partition before irr_init");
+    cudaSetDevice(h->device);
+    const int64_t n = h->n, m = 2 * h->e;
+    if (perm && n > 0)
+        H_CUDA(h, cudaMemcpyAsync(perm, h->part.perm, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, h->stream), "copy perm");
+    std::vector<uint32_t> ro;
+    if (row_off) {
+        ro.resize((size_t)n + 1);
+        H_CUDA(h, cudaMemcpyAsync(ro.data(), h->part.row_off, sizeof(uint32_t) * (n + 1), cudaMemcpyDeviceToHost, h->stream), "copy row offsets");
+    }
+    if (col && m > 0)
+        H_CUDA(h, cudaMemcpyAsync(col, h->part.col, sizeof(int32_t) * m, cudaMemcpyDeviceToHost, h->stream), "copy entries");
+    H_CUDA(h, cudaStreamSynchronize(h->stream), "copy partition");
+    if (row_off)
+        for (int64_t i = 0; i <= n; i++) row_off[i] = ro[(size_t)i];
+    return IRR_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,107 @@
+// irr_internal.cuh -- declarations shared by the library's translation units.
+#pragma once
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <cuda_runtime.h>
+
+#include "irr_law.cuh"
+
+namespace irr {
+
+// Device status word bits (set by kernels, read by the host at sync points).
+enum : int {
+    kStatusBadIndex = 1 << 0,   // an edge endpoint outside [0, n)
+    kStatusWaitTimeout = 1 << 1, // a bounded device-side wait gave up
+    kStatusBadAlign = 1 << 2,   // a bulk copy was asked for an unaligned range
+};
+
+// One system of the (possibly batched) owner-computes reduction.
+struct InstDesc {
+    const float4* pos;        // node positions, execution (partition) order
+    const uint32_t* row_off;  // n + 1 entry offsets
+    const int32_t* col;       // neighbour of each directed entry (instance-local id)
+    float4* force;            // per-node result, execution order
+    LawParams law;
+    int64_t n;
+};
+
+// One node block: rows [row0, row0 + nrows) of instance `inst`.
+struct WorkItem {
+    int32_t inst;
+    int32_t row0;
+    int32_t nrows;
+    int32_t pad_;
+};
+
+struct TiledShape {
+    int lanes_per_row;   // 4, 8, 16 or 32
+    int stage_smem;      // 0 or 1
+    int block_nodes;     // max rows per work item (stage_smem: <= kMaxStageNodes)
+    int periodic;
+};
+
+constexpr int kTiledThreads = 256;
+constexpr int kMaxStageNodes = 2048;   // 32 KB of float4 in shared memory
+
+// -- reduction kernels (irr_reduce.cu) --
+cudaError_t launch_plain(const float4* pos, const int2* edges, int64_t e, float4* force,
+                         const LawParams& law, cudaStream_t s);
+// queue == nullptr: one CTA per work item.  Otherwise a persistent grid of
+// `grid` CTAs draws items from *queue (which must be 0 at launch).
+cudaError_t launch_tiled(const TiledShape& shape, const InstDesc* d_insts,
+                         const WorkItem* d_items, int num_items, int* d_queue, int grid,
+                         int* d_status, cudaStream_t s);
+
+// -- data movement (irr_partition.cu) --
+// Raw node records (12/16/24 bytes) -> float4, optionally gathered: dst[k] =
+// rec[perm ? perm[k] : k].
+cudaError_t launch_load_nodes(const void* raw, int elm_size, const int32_t* perm, int64_t n,
+                              float4* dst, cudaStream_t s);
+// Results: out[i] = force[inv ? inv[i] : i] in the requested format.
+cudaError_t launch_store_result(const float4* force, const int32_t* inv, int64_t n,
+                                int elm_size, void* out, cudaStream_t s);
+cudaError_t launch_validate_edges(const int2* edges, int64_t e, int64_t n, int* d_status,
+                                  cudaStream_t s);
+
+// -- partitioner (irr_partition.cu) --
+struct PartitionOut {
+    int32_t* perm = nullptr;      // [n] new -> old
+    int32_t* inv = nullptr;       // [n] old -> new
+    uint32_t* row_off = nullptr;  // [n + 1]
+    int32_t* col = nullptr;       // [2e]
+};
+// Computes the Morton frame (per-axis min and 1024 / extent) of pos.
+cudaError_t bbox_frame(const float4* pos, int64_t n, float lo[3], float scale[3],
+                       cudaStream_t s);
+// Full partition of n nodes and e half edges.  Allocates out's arrays with
+// cudaMallocAsync on s (caller frees).  reorder == 0 keeps the identity order.
+cudaError_t build_partition(const float4* pos_user, int64_t n, const int2* edges, int64_t e,
+                            int reorder, PartitionOut* out, cudaStream_t s);
+// Stable LSD radix sort of (key, value) pairs on key bits [0, key_bits).
+// Sorted data ends in (keys, vals); tmp arrays have n entries each.
+cudaError_t radix_sort_pairs(uint32_t* keys, int32_t* vals, uint32_t* keys_tmp,
+                             int32_t* vals_tmp, int64_t n, int key_bits, cudaStream_t s);
+// Exclusive prefix sum of n uint32 into out (out may alias in); *total, if
+// non-null, receives the sum (device pointer).
+cudaError_t scan_exclusive_u32(const uint32_t* in, uint32_t* out, int64_t n, uint32_t* d_total,
+                               cudaStream_t s);
+
+// Morton key of one position in a frame (shared with the oracle bit for bit).
+__host__ __device__ __forceinline__ uint32_t spread3(uint32_t v)
+{
+    v &= 0x3ffu;
+    v = (v | (v << 16)) & 0x030000ffu;
+    v = (v | (v << 8)) & 0x0300f00fu;
+    v = (v | (v << 4)) & 0x030c30c3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+
+}  // namespace irr
+
+#define IRR_CUDA_TRY(expr)                         \
+    do {                                           \
+        cudaError_t irr_e_ = (expr);               \
+        if (irr_e_ != cudaSuccess) return irr_e_;  \
+    } while (0)

@@ -1,0 +1,496 @@
+// irr_partition.cu -- the GPU partitioner and the node/result data movers.
+//
+// The reference partitions on the host: a randomized quickselect recursive
+// bisection of the coordinates into shared-memory-sized parts
+// (moldyn/irregular/partitioner.cpp:348-437), then an O(E) pass that copies
+// every edge into the part of each endpoint with std::vector push_back
+// (partitioner.cpp:142-297), then part_index (:490-499).  Here the whole pass
+// runs on the GPU and is deterministic:
+//   1. Morton key per node: each axis quantised to 10 bits in the bounding
+//      box frame (float ops, each rounded), bits interleaved;
+//   2. stable LSD radix sort of (key, node) -> perm[new] = old, inv[old] = new;
+//   3. every half edge (i, j) at list position t becomes the directed entries
+//      (inv[i] <- inv[j]) and (inv[j] <- inv[i]); a stable radix sort by row
+//      bins them, and a degree count + scan gives the row offsets.
+// Node blocks are then consecutive ranges of rows.  Every output is an
+// integer function of the inputs, reproduced bit for bit by the CPU oracle.
+#include <algorithm>
+
+#include "irr_internal.cuh"
+
+namespace irr {
+namespace {
+
+__device__ __forceinline__ uint32_t lanemask_lt()
+{
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// ------------------------------------------------------------------ scan
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 4;
+constexpr int kScanBlock = kScanThreads * kScanItems;
+
+__global__ void __launch_bounds__(kScanThreads) scan_blocks_kernel(const uint32_t* in,
+                                                                   uint32_t* out, int64_t n,
+                                                                   uint32_t* block_sums)
+{
+    __shared__ uint32_t warp_tot[kScanThreads / 32];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int64_t base = (int64_t)blockIdx.x * kScanBlock + (int64_t)tid * kScanItems;
+    uint32_t v[kScanItems];
+    uint32_t sum = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) {
+        v[k] = (base + k < n) ? in[base + k] : 0u;
+        sum += v[k];
+    }
+    uint32_t incl = sum;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, off);
+        if (lane >= off) incl += y;
+    }
+    if (lane == 31) warp_tot[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t t = lane < kScanThreads / 32 ? warp_tot[lane] : 0u;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, t, off);
+            if (lane >= off) t += y;
+        }
+        if (lane < kScanThreads / 32) warp_tot[lane] = t;  // inclusive
+    }
+    __syncthreads();
+    uint32_t run = incl - sum + (warp > 0 ? warp_tot[warp - 1] : 0u);
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) {
+        if (base + k < n) out[base + k] = run;
+        run += v[k];
+    }
+    if (tid == kScanThreads - 1) block_sums[blockIdx.x] = warp_tot[kScanThreads / 32 - 1];
+}
+
+__global__ void add_offsets_kernel(uint32_t* out, int64_t n, const uint32_t* block_off)
+{
+    const uint32_t add = block_off[blockIdx.x];
+    const int64_t base = (int64_t)blockIdx.x * kScanBlock;
+    for (int k = threadIdx.x; k < kScanBlock; k += blockDim.x)
+        if (base + k < n) out[base + k] += add;
+}
+
+__global__ void copy_u32_kernel(const uint32_t* src, uint32_t* dst) { *dst = *src; }
+
+// ------------------------------------------------------------ radix sort
+constexpr int kSortThreads = 256;
+constexpr int kSortRounds = 16;
+constexpr int kSortTile = kSortThreads * kSortRounds;  // items per tile, in order
+constexpr int kSortWarps = kSortThreads / 32;
+
+__global__ void __launch_bounds__(kSortThreads) radix_hist_kernel(const uint32_t* keys, int64_t n,
+                                                                  int shift, uint32_t* hist,
+                                                                  int64_t ntiles)
+{
+    __shared__ uint32_t cnt[256];
+    const int tid = threadIdx.x;
+    cnt[tid] = 0;
+    __syncthreads();
+    const int64_t base = (int64_t)blockIdx.x * kSortTile;
+    for (int r = 0; r < kSortRounds; r++) {
+        const int64_t i = base + r * kSortThreads + tid;
+        const bool v = i < n;
+        const uint32_t d = v ? (keys[i] >> shift) & 255u : 256u;
+        const uint32_t peers = __match_any_sync(0xffffffffu, d);
+        if (v && (peers & lanemask_lt()) == 0) atomicAdd(&cnt[d], (uint32_t)__popc(peers));
+    }
+    __syncthreads();
+    hist[(int64_t)tid * ntiles + blockIdx.x] = cnt[tid];
+}
+
+// Stable scatter: items of a tile keep their index order within each digit.
+// Round r covers tile items [r*256, r*256+256): item k goes to thread k.
+__global__ void __launch_bounds__(kSortThreads) radix_scatter_kernel(
+    const uint32_t* kin, const int32_t* vin, uint32_t* kout, int32_t* vout, int64_t n, int shift,
+    const uint32_t* offs, int64_t ntiles)
+{
+    __shared__ uint32_t base[256];
+    __shared__ uint32_t wcnt[kSortWarps][256];
+    const int tid = threadIdx.x, warp = tid >> 5;
+    base[tid] = offs[(int64_t)tid * ntiles + blockIdx.x];
+#pragma unroll
+    for (int w = 0; w < kSortWarps; w++) wcnt[w][tid] = 0;
+    __syncthreads();
+    const int64_t tile0 = (int64_t)blockIdx.x * kSortTile;
+    for (int r = 0; r < kSortRounds; r++) {
+        const int64_t i = tile0 + r * kSortThreads + tid;
+        const bool v = i < n;
+        const uint32_t key = v ? kin[i] : 0u;
+        const int32_t val = v ? vin[i] : 0;
+        const uint32_t d = v ? (key >> shift) & 255u : 256u;
+        const uint32_t peers = __match_any_sync(0xffffffffu, d);
+        const uint32_t below = peers & lanemask_lt();
+        if (v && below == 0) wcnt[warp][d] = (uint32_t)__popc(peers);
+        __syncthreads();
+        // thread t owns digit t: exclusive prefix over warps, round total
+        uint32_t run = 0;
+#pragma unroll
+        for (int w = 0; w < kSortWarps; w++) {
+            const uint32_t c = wcnt[w][tid];
+            wcnt[w][tid] = run;
+            run += c;
+        }
+        __syncthreads();
+        if (v) {
+            const uint32_t dst = base[d] + wcnt[warp][d] + (uint32_t)__popc(below);
+            kout[dst] = key;
+            vout[dst] = val;
+        }
+        __syncthreads();
+        base[tid] += run;
+#pragma unroll
+        for (int w = 0; w < kSortWarps; w++) wcnt[w][tid] = 0;
+        __syncthreads();
+    }
+}
+
+// --------------------------------------------------------------- bbox
+__global__ void bbox_partial_kernel(const float4* pos, int64_t n, float* part)
+{
+    __shared__ float red[6][256];
+    float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const float4 p = pos[i];
+        mn[0] = fminf(mn[0], p.x);
+        mn[1] = fminf(mn[1], p.y);
+        mn[2] = fminf(mn[2], p.z);
+        mx[0] = fmaxf(mx[0], p.x);
+        mx[1] = fmaxf(mx[1], p.y);
+        mx[2] = fmaxf(mx[2], p.z);
+    }
+    for (int c = 0; c < 3; c++) {
+        red[c][threadIdx.x] = mn[c];
+        red[3 + c][threadIdx.x] = mx[c];
+    }
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if ((int)threadIdx.x < s)
+            for (int c = 0; c < 3; c++) {
+                red[c][threadIdx.x] = fminf(red[c][threadIdx.x], red[c][threadIdx.x + s]);
+                red[3 + c][threadIdx.x] =
+                    fmaxf(red[3 + c][threadIdx.x], red[3 + c][threadIdx.x + s]);
+            }
+        __syncthreads();
+    }
+    if (threadIdx.x < 6) part[blockIdx.x * 6 + threadIdx.x] = red[threadIdx.x][0];
+}
+
+__global__ void bbox_final_kernel(const float* part, int nparts, float* out)
+{
+    if (threadIdx.x != 0) return;
+    float v[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+    for (int b = 0; b < nparts; b++)
+        for (int c = 0; c < 3; c++) {
+            v[c] = fminf(v[c], part[b * 6 + c]);
+            v[3 + c] = fmaxf(v[3 + c], part[b * 6 + 3 + c]);
+        }
+    for (int c = 0; c < 6; c++) out[c] = v[c];
+}
+
+// ------------------------------------------------------------- morton
+__device__ __forceinline__ uint32_t quant10(float x, float lo, float scale)
+{
+    float t = __fsub_rn(x, lo);
+    t = __fmul_rn(t, scale);
+    if (!(t > 0.0f)) return 0u;
+    if (t >= 1023.0f) return 1023u;
+    return __float2uint_rz(t);
+}
+
+__global__ void morton_kernel(const float4* pos, int64_t n, float3 lo, float3 scale,
+                              uint32_t* keys, int32_t* vals)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const float4 p = pos[i];
+        keys[i] = spread3(quant10(p.x, lo.x, scale.x)) |
+                  (spread3(quant10(p.y, lo.y, scale.y)) << 1) |
+                  (spread3(quant10(p.z, lo.z, scale.z)) << 2);
+        vals[i] = (int32_t)i;
+    }
+}
+
+__global__ void iota_kernel(int32_t* a, int64_t n)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        a[i] = (int32_t)i;
+}
+
+__global__ void invert_kernel(const int32_t* perm, int64_t n, int32_t* inv)
+{
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * blockDim.x)
+        inv[perm[k]] = (int32_t)k;
+}
+
+__global__ void entries_kernel(const int2* edges, int64_t e, const int32_t* inv, uint32_t* rows,
+                               int32_t* cols, uint32_t* deg)
+{
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < e;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int2 ed = edges[t];
+        const int32_t a = inv[ed.x], b = inv[ed.y];
+        rows[2 * t] = (uint32_t)a;
+        cols[2 * t] = b;
+        rows[2 * t + 1] = (uint32_t)b;
+        cols[2 * t + 1] = a;
+        atomicAdd(deg + a, 1u);
+        atomicAdd(deg + b, 1u);
+    }
+}
+
+// --------------------------------------------------------- data movers
+__global__ void load_nodes_kernel(const char* raw, int elm, const int32_t* perm, int64_t n,
+                                  float4* dst)
+{
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t src = perm ? perm[k] : k;
+        float4 p;
+        if (elm == 24) {
+            const double* d = reinterpret_cast<const double*>(raw + src * 24);
+            p = make_float4((float)d[0], (float)d[1], (float)d[2], 0.f);
+        } else if (elm == 16) {
+            p = reinterpret_cast<const float4*>(raw)[src];
+            p.w = 0.f;
+        } else {
+            const float* f = reinterpret_cast<const float*>(raw + src * 12);
+            p = make_float4(f[0], f[1], f[2], 0.f);
+        }
+        dst[k] = p;
+    }
+}
+
+__global__ void store_result_kernel(const float4* force, const int32_t* inv, int64_t n, int elm,
+                                    char* out)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const float4 f = force[inv ? inv[i] : i];
+        if (elm == 24) {
+            double* d = reinterpret_cast<double*>(out + i * 24);
+            d[0] = f.x;
+            d[1] = f.y;
+            d[2] = f.z;
+        } else if (elm == 16) {
+            reinterpret_cast<float4*>(out)[i] = make_float4(f.x, f.y, f.z, 0.f);
+        } else {
+            float* o = reinterpret_cast<float*>(out + i * 12);
+            o[0] = f.x;
+            o[1] = f.y;
+            o[2] = f.z;
+        }
+    }
+}
+
+__global__ void validate_edges_kernel(const int2* edges, int64_t e, int64_t n, int* status)
+{
+    bool bad = false;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < e;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int2 ed = edges[t];
+        bad |= ed.x < 0 || ed.y < 0 || ed.x >= n || ed.y >= n;
+    }
+    if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(status, kStatusBadIndex);
+}
+
+int grid_for(int64_t n, int threads = 256)
+{
+    int64_t g = (n + threads - 1) / threads;
+    if (g < 1) g = 1;
+    if (g > 8192) g = 8192;
+    return (int)g;
+}
+
+template <class T>
+cudaError_t alloc_async(T** p, int64_t count, cudaStream_t s)
+{
+    return cudaMallocAsync(reinterpret_cast<void**>(p), sizeof(T) * (size_t)(count > 0 ? count : 1),
+                           s);
+}
+
+}  // namespace
+
+cudaError_t scan_exclusive_u32(const uint32_t* in, uint32_t* out, int64_t n, uint32_t* d_total,
+                               cudaStream_t s)
+{
+    if (n <= 0) {
+        if (d_total) IRR_CUDA_TRY(cudaMemsetAsync(d_total, 0, sizeof(uint32_t), s));
+        return cudaSuccess;
+    }
+    const int64_t nb = (n + kScanBlock - 1) / kScanBlock;
+    uint32_t* sums = nullptr;
+    IRR_CUDA_TRY(alloc_async(&sums, nb, s));
+    scan_blocks_kernel<<<(unsigned)nb, kScanThreads, 0, s>>>(in, out, n, sums);
+    cudaError_t err = cudaGetLastError();
+    if (err == cudaSuccess) {
+        if (nb == 1) {
+            if (d_total) copy_u32_kernel<<<1, 1, 0, s>>>(sums, d_total);
+        } else {
+            err = scan_exclusive_u32(sums, sums, nb, d_total, s);
+            if (err == cudaSuccess)
+                add_offsets_kernel<<<(unsigned)nb, kScanThreads, 0, s>>>(out, n, sums);
+        }
+        if (err == cudaSuccess) err = cudaGetLastError();
+    }
+    cudaError_t ferr = cudaFreeAsync(sums, s);
+    return err != cudaSuccess ? err : ferr;
+}
+
+cudaError_t radix_sort_pairs(uint32_t* keys, int32_t* vals, uint32_t* keys_tmp,
+                             int32_t* vals_tmp, int64_t n, int key_bits, cudaStream_t s)
+{
+    if (n <= 1 || key_bits <= 0) return cudaSuccess;
+    if (n > 0xffffffffLL) return cudaErrorInvalidValue;
+    const int64_t ntiles = (n + kSortTile - 1) / kSortTile;
+    uint32_t* hist = nullptr;
+    IRR_CUDA_TRY(alloc_async(&hist, 256 * ntiles, s));
+    uint32_t *ka = keys, *kb = keys_tmp;
+    int32_t *va = vals, *vb = vals_tmp;
+    cudaError_t err = cudaSuccess;
+    int passes = 0;
+    for (int shift = 0; shift < key_bits && err == cudaSuccess; shift += 8, passes++) {
+        radix_hist_kernel<<<(unsigned)ntiles, kSortThreads, 0, s>>>(ka, n, shift, hist, ntiles);
+        err = cudaGetLastError();
+        if (err == cudaSuccess) err = scan_exclusive_u32(hist, hist, 256 * ntiles, nullptr, s);
+        if (err == cudaSuccess) {
+            radix_scatter_kernel<<<(unsigned)ntiles, kSortThreads, 0, s>>>(ka, va, kb, vb, n, shift,
+                                                                          hist, ntiles);
+            err = cudaGetLastError();
+        }
+        std::swap(ka, kb);
+        std::swap(va, vb);
+    }
+    if (err == cudaSuccess && (passes & 1)) {
+        err = cudaMemcpyAsync(keys, ka, sizeof(uint32_t) * (size_t)n, cudaMemcpyDeviceToDevice, s);
+        if (err == cudaSuccess)
+            err = cudaMemcpyAsync(vals, va, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToDevice, s);
+    }
+    cudaError_t ferr = cudaFreeAsync(hist, s);
+    return err != cudaSuccess ? err : ferr;
+}
+
+cudaError_t bbox_frame(const float4* pos, int64_t n, float lo[3], float scale[3], cudaStream_t s)
+{
+    for (int c = 0; c < 3; c++) {
+        lo[c] = 0.f;
+        scale[c] = 0.f;
+    }
+    if (n <= 0) return cudaSuccess;
+    const int nparts = (int)std::min<int64_t>((n + 255) / 256, 1024);
+    float* part = nullptr;
+    IRR_CUDA_TRY(alloc_async(&part, 6 * (int64_t)nparts + 6, s));
+    bbox_partial_kernel<<<nparts, 256, 0, s>>>(pos, n, part);
+    bbox_final_kernel<<<1, 32, 0, s>>>(part, nparts, part + 6 * nparts);
+    float h[6];
+    cudaError_t err = cudaGetLastError();
+    if (err == cudaSuccess)
+        err = cudaMemcpyAsync(h, part + 6 * nparts, sizeof(h), cudaMemcpyDeviceToHost, s);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(s);
+    cudaError_t ferr = cudaFreeAsync(part, s);
+    if (err != cudaSuccess) return err;
+    for (int c = 0; c < 3; c++) {
+        lo[c] = h[c];
+        const float ext = h[3 + c] - h[c];
+        scale[c] = ext > 0.0f ? 1024.0f / ext : 0.0f;
+    }
+    return ferr;
+}
+
+cudaError_t build_partition(const float4* pos_user, int64_t n, const int2* edges, int64_t e,
+                            int reorder, PartitionOut* out, cudaStream_t s)
+{
+    if (n < 0 || e < 0 || n > 0x7fffffffLL || 2 * e > 0xffffffffLL) return cudaErrorInvalidValue;
+    *out = PartitionOut{};
+    IRR_CUDA_TRY(alloc_async(&out->perm, n, s));
+    IRR_CUDA_TRY(alloc_async(&out->inv, n, s));
+    IRR_CUDA_TRY(alloc_async(&out->row_off, n + 1, s));
+    IRR_CUDA_TRY(alloc_async(&out->col, 2 * e, s));
+    const int g = grid_for(n);
+    if (reorder && n > 1) {
+        float lo[3], scale[3];
+        IRR_CUDA_TRY(bbox_frame(pos_user, n, lo, scale, s));
+        uint32_t *keys = nullptr, *keys_tmp = nullptr;
+        int32_t* vals_tmp = nullptr;
+        IRR_CUDA_TRY(alloc_async(&keys, n, s));
+        IRR_CUDA_TRY(alloc_async(&keys_tmp, n, s));
+        IRR_CUDA_TRY(alloc_async(&vals_tmp, n, s));
+        morton_kernel<<<g, 256, 0, s>>>(pos_user, n, make_float3(lo[0], lo[1], lo[2]),
+                                        make_float3(scale[0], scale[1], scale[2]), keys, out->perm);
+        IRR_CUDA_TRY(cudaGetLastError());
+        IRR_CUDA_TRY(radix_sort_pairs(keys, out->perm, keys_tmp, vals_tmp, n, 30, s));
+        IRR_CUDA_TRY(cudaFreeAsync(keys, s));
+        IRR_CUDA_TRY(cudaFreeAsync(keys_tmp, s));
+        IRR_CUDA_TRY(cudaFreeAsync(vals_tmp, s));
+    } else if (n > 0) {
+        iota_kernel<<<g, 256, 0, s>>>(out->perm, n);
+        IRR_CUDA_TRY(cudaGetLastError());
+    }
+    if (n > 0) {
+        invert_kernel<<<g, 256, 0, s>>>(out->perm, n, out->inv);
+        IRR_CUDA_TRY(cudaGetLastError());
+    }
+    // directed entries, binned by row
+    uint32_t* deg = out->row_off;  // counted in place, then scanned
+    IRR_CUDA_TRY(cudaMemsetAsync(deg, 0, sizeof(uint32_t) * (size_t)(n + 1), s));
+    if (e > 0) {
+        const int64_t m = 2 * e;
+        uint32_t *rows = nullptr, *rows_tmp = nullptr;
+        int32_t* cols_tmp = nullptr;
+        IRR_CUDA_TRY(alloc_async(&rows, m, s));
+        IRR_CUDA_TRY(alloc_async(&rows_tmp, m, s));
+        IRR_CUDA_TRY(alloc_async(&cols_tmp, m, s));
+        entries_kernel<<<grid_for(e), 256, 0, s>>>(edges, e, out->inv, rows, out->col, deg);
+        IRR_CUDA_TRY(cudaGetLastError());
+        int bits = 1;
+        while (bits < 31 && ((int64_t)1 << bits) < n) bits++;
+        IRR_CUDA_TRY(radix_sort_pairs(rows, out->col, rows_tmp, cols_tmp, m, bits, s));
+        IRR_CUDA_TRY(cudaFreeAsync(rows, s));
+        IRR_CUDA_TRY(cudaFreeAsync(rows_tmp, s));
+        IRR_CUDA_TRY(cudaFreeAsync(cols_tmp, s));
+    }
+    IRR_CUDA_TRY(scan_exclusive_u32(deg, out->row_off, n + 1, nullptr, s));
+    return cudaSuccess;
+}
+
+cudaError_t launch_load_nodes(const void* raw, int elm_size, const int32_t* perm, int64_t n,
+                              float4* dst, cudaStream_t s)
+{
+    if (n <= 0) return cudaSuccess;
+    load_nodes_kernel<<<grid_for(n), 256, 0, s>>>(static_cast<const char*>(raw), elm_size, perm, n,
+                                                  dst);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_store_result(const float4* force, const int32_t* inv, int64_t n,
+                                int elm_size, void* out, cudaStream_t s)
+{
+    if (n <= 0) return cudaSuccess;
+    store_result_kernel<<<grid_for(n), 256, 0, s>>>(force, inv, n, elm_size,
+                                                    static_cast<char*>(out));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_validate_edges(const int2* edges, int64_t e, int64_t n, int* d_status,
+                                  cudaStream_t s)
+{
+    if (e <= 0) return cudaSuccess;
+    validate_edges_kernel<<<grid_for(e), 256, 0, s>>>(edges, e, n, d_status);
+    return cudaGetLastError();
+}
+
+}  // namespace irr

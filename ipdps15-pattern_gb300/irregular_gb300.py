@@ -1,0 +1,283 @@
+"""Python host binding of libirregular_gb300.so (ctypes over the C ABI).
+
+`IrregularRuntime` mirrors the reference's C++ class of the same name
+(moldyn/irregular/irregular_runtime.h:12-112): construct it with the edge
+list, node data and parameter block, call IrregularInit(), then per iteration
+reset_node_data() / IrregularStart() / get_reduction_result().  Errors raise
+IrregularError carrying the C status code; nothing falls back to the CPU.  If
+the shared library has not been built the import of this module still works,
+but the first call raises with the build instruction.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libirregular_gb300.so")
+
+IRR_OK = 0
+IRR_ERR_ARG = 1
+IRR_ERR_INDEX = 2
+IRR_ERR_STATE = 3
+IRR_ERR_CUDA = 4
+IRR_ERR_NOMEM = 5
+IRR_ERR_CAPACITY = 6
+IRR_ERR_DEVICE = 7
+IRR_ERR_BUDGET = 8
+
+IRR_MAP_LJ_MOLDYN = 0
+IRR_MAP_LJ_MINIMD = 1
+IRR_MAP_LJ_MINIMD_PBC = 2
+IRR_REDUCE_SUM = 0
+IRR_EXEC_PLAIN = 0
+IRR_EXEC_PARTITIONED = 1
+
+
+class IrregularError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"[status {status}] {msg}")
+        self.status = status
+
+
+class Config(C.Structure):
+    _fields_ = [("device", C.c_int), ("exec", C.c_int), ("map_idx", C.c_int),
+                ("reduce_idx", C.c_int), ("block_nodes", C.c_int), ("lanes_per_row", C.c_int),
+                ("reorder", C.c_int), ("stage_smem", C.c_int), ("reserved", C.c_int * 8)]
+
+
+class Info(C.Structure):
+    _fields_ = [("num_nodes", C.c_int64), ("num_edges", C.c_int64), ("num_entries", C.c_int64),
+                ("num_blocks", C.c_int64), ("device_bytes", C.c_int64),
+                ("block_nodes", C.c_int32), ("lanes_per_row", C.c_int32),
+                ("stage_smem", C.c_int32), ("exec", C.c_int32)]
+
+
+# name -> (restype, argtypes); every symbol include/irregular_gb300.h declares
+P = C.c_void_p
+I64 = C.c_int64
+_SIGS = {
+    "irr_config_default": (None, [C.POINTER(Config)]),
+    "irr_status_string": (C.c_char_p, [C.c_int]),
+    "irr_create": (C.c_int, [C.POINTER(Config), C.POINTER(P)]),
+    "irr_destroy": (C.c_int, [P]),
+    "irr_last_error": (C.c_char_p, [P]),
+    "irr_set_stream": (C.c_int, [P, P]),
+    "irr_set_map": (C.c_int, [P, C.c_int]),
+    "irr_set_reduce": (C.c_int, [P, C.c_int]),
+    "irr_set_params": (C.c_int, [P, P, C.c_int]),
+    "irr_set_edges": (C.c_int, [P, P, I64]),
+    "irr_set_edges_device": (C.c_int, [P, P, I64]),
+    "irr_set_nodes": (C.c_int, [P, P, C.c_int, I64]),
+    "irr_set_nodes_device": (C.c_int, [P, P, C.c_int, I64]),
+    "irr_init": (C.c_int, [P]),
+    "irr_step": (C.c_int, [P]),
+    "irr_get_result": (C.c_int, [P, P, C.c_int]),
+    "irr_get_result_device": (C.c_int, [P, P, C.c_int]),
+    "irr_sync": (C.c_int, [P]),
+    "irr_get_info": (C.c_int, [P, C.POINTER(Info)]),
+    "irr_get_partition": (C.c_int, [P, P, P, P]),
+}
+
+_lib = None
+
+
+def lib_path() -> str:
+    return LIB_PATH
+
+
+def load():
+    """Loads the CUDA library; raises if it was never built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(
+                f"{LIB_PATH} is missing: build it with "
+                "`python -c 'import __graft_entry__ as g; g.build()'`")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _ptr(a) -> C.c_void_p:
+    if a is None:
+        return None
+    if isinstance(a, int):
+        return C.c_void_p(a)
+    if hasattr(a, "data_ptr"):  # torch tensor
+        return C.c_void_p(a.data_ptr())
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def default_config(**kw) -> Config:
+    cfg = Config()
+    load().irr_config_default(C.byref(cfg))
+    for k, v in kw.items():
+        setattr(cfg, k, v)
+    return cfg
+
+
+def moldyn_params(side: float, cutoff: float) -> np.ndarray:
+    """struct para {double side; double cutoffRadius;} (moldyn/moldyn.h:39-43)."""
+    return np.array([side, cutoff], np.float64)
+
+
+def minimd_params(cutforcesq: float, side: Optional[float] = None) -> np.ndarray:
+    """double cutforcesq (miniMD/ljs.cu:123), plus the box side for the PBC map."""
+    if side is None:
+        return np.array([cutforcesq], np.float64)
+    return np.array([cutforcesq, side], np.float64)
+
+
+class Handle:
+    """Owning wrapper of one irr_handle."""
+
+    def __init__(self, cfg: Optional[Config] = None, **kw):
+        L = load()
+        if cfg is None:
+            cfg = default_config(**kw)
+        h = C.c_void_p()
+        rc = L.irr_create(C.byref(cfg), C.byref(h))
+        if rc != IRR_OK:
+            raise IrregularError(rc, f"irr_create: {L.irr_status_string(rc).decode()}")
+        self._h = h
+        self.cfg = cfg
+
+    def _check(self, rc: int, what: str):
+        if rc != IRR_OK:
+            msg = load().irr_last_error(self._h)
+            raise IrregularError(rc, f"{what}: {msg.decode() if msg else ''}")
+
+    @property
+    def raw(self):
+        return self._h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().irr_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_ptr: int):
+        self._check(load().irr_set_stream(self._h, C.c_void_p(stream_ptr)), "irr_set_stream")
+
+    def set_map(self, idx: int):
+        self._check(load().irr_set_map(self._h, int(idx)), "irr_set_map")
+
+    def set_params(self, blob: np.ndarray):
+        blob = np.ascontiguousarray(blob)
+        self._check(load().irr_set_params(self._h, _ptr(blob), blob.nbytes), "irr_set_params")
+
+    def set_edges(self, edges):
+        if hasattr(edges, "data_ptr"):
+            self._check(load().irr_set_edges_device(self._h, _ptr(edges), edges.numel() // 2),
+                        "irr_set_edges_device")
+            return
+        e = np.ascontiguousarray(edges, np.int32).reshape(-1, 2)
+        self._check(load().irr_set_edges(self._h, _ptr(e), e.shape[0]), "irr_set_edges")
+
+    def set_nodes(self, nodes, elm_size: Optional[int] = None, n: Optional[int] = None):
+        if hasattr(nodes, "data_ptr"):
+            elm = elm_size or nodes.element_size() * nodes.shape[-1]
+            cnt = n if n is not None else nodes.numel() * nodes.element_size() // elm
+            self._check(load().irr_set_nodes_device(self._h, _ptr(nodes), elm, cnt),
+                        "irr_set_nodes_device")
+            return
+        a = np.ascontiguousarray(nodes)
+        elm = elm_size or a.dtype.itemsize * (a.shape[-1] if a.ndim > 1 else 1)
+        cnt = n if n is not None else a.nbytes // elm
+        self._check(load().irr_set_nodes(self._h, _ptr(a), elm, cnt), "irr_set_nodes")
+
+    def init(self):
+        self._check(load().irr_init(self._h), "irr_init")
+
+    def step(self):
+        self._check(load().irr_step(self._h), "irr_step")
+
+    def sync(self):
+        self._check(load().irr_sync(self._h), "irr_sync")
+
+    def get_result(self, out: Optional[np.ndarray] = None, elm_size: int = 12) -> np.ndarray:
+        info = self.info()
+        n = info.num_nodes
+        if out is None:
+            dt = np.float64 if elm_size == 24 else np.float32
+            out = np.empty((n, elm_size // np.dtype(dt).itemsize), dt)
+        self._check(load().irr_get_result(self._h, _ptr(out), elm_size), "irr_get_result")
+        return out
+
+    def get_result_device(self, d_out, elm_size: int = 16):
+        self._check(load().irr_get_result_device(self._h, _ptr(d_out), elm_size),
+                    "irr_get_result_device")
+
+    def info(self) -> Info:
+        inf = Info()
+        self._check(load().irr_get_info(self._h, C.byref(inf)), "irr_get_info")
+        return inf
+
+    def partition(self):
+        inf = self.info()
+        n, m = inf.num_nodes, inf.num_entries
+        perm = np.zeros(n, np.int32)
+        row_off = np.zeros(n + 1, np.int64)
+        col = np.zeros(max(m, 1), np.int32)
+        self._check(load().irr_get_partition(self._h, _ptr(perm), _ptr(row_off), _ptr(col)),
+                    "irr_get_partition")
+        return perm, row_off, col[:m]
+
+
+class IrregularRuntime:
+    """The reference's IrregularRuntime interface over the C ABI.
+
+    Constructor arguments follow irregular_runtime.h:71-86; `num_procs`,
+    `num_iters` and the edge/coordinate extras are accepted for source
+    compatibility (one GPU, no MPI split).  `map_idx` picks the built-in user
+    function (IRR_MAP_*)."""
+
+    def __init__(self, num_edges, num_nodes, edges, edge_data, node_data, edge_data_elm_size,
+                 node_data_elm_size, reduction_elm_size, node_num_dims=3,
+                 node_coordinates=None, coordinate_size=8, parameter=None, parameter_size=None,
+                 num_procs=1, num_iters=1, map_idx=IRR_MAP_LJ_MOLDYN,
+                 exec_mode=IRR_EXEC_PARTITIONED, **cfg_kw):
+        self.num_edges = int(num_edges)
+        self.num_nodes = int(num_nodes)
+        self.node_elm = int(node_data_elm_size)
+        self.red_elm = int(reduction_elm_size)
+        self.h = Handle(default_config(map_idx=map_idx, exec=exec_mode, **cfg_kw))
+        self.h.set_params(np.ascontiguousarray(parameter))
+        self.h.set_edges(np.asarray(edges, np.int32).reshape(-1, 2)[: self.num_edges])
+        self.h.set_nodes(node_data, self.node_elm, self.num_nodes)
+
+    def set_map_idx(self, idx: int):
+        self.h.set_map(idx)
+
+    def set_reduce_idx(self, idx: int):
+        if idx != IRR_REDUCE_SUM:
+            raise IrregularError(IRR_ERR_ARG, f"unknown reduce index {idx}")
+
+    def IrregularInit(self):
+        self.h.init()
+
+    def IrregularStart(self):
+        self.h.step()
+
+    def IrregularBarrier(self):
+        self.h.sync()
+
+    def reset_node_data(self, node_data):
+        self.h.set_nodes(node_data, self.node_elm, self.num_nodes)
+
+    def get_reduction_result(self, buffer: Optional[np.ndarray] = None) -> np.ndarray:
+        return self.h.get_result(buffer, self.red_elm)

@@ -1,0 +1,117 @@
+/*
+ * irr_oracle.h -- CPU oracle for the irregular-reduction hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  Nothing in the product library links, loads or
+ * calls this code; only tests/, __graft_entry__.smoke() and bench.py's
+ * cpu_baseline / --impl reference legs use it, and only as the checker or as
+ * the timed CPU baseline.
+ *
+ * It restates, in plain C, the arithmetic of the reference's CPU path:
+ *   - the per-edge user function `map` (moldyn/irregular.h:26-107) and
+ *     `map1` (miniMD/irregular.h:109-163), with the `reduce` float3 `+=`
+ *     (moldyn/irregular.h:109-114);
+ *   - the pthread executor `compute_cpu` (moldyn/irregular/cpu_kernel.cu:13-70)
+ *     with its per-thread open-addressing table `Cobject::insert`
+ *     (moldyn/irregular/roc.cu:11-65), used as the timed CPU baseline;
+ *   - the binned half neighbour list of miniMD (miniMD/neighbor.cpp:76-205)
+ *     and the all-pairs list rule of moldyn (moldyn/moldyn.cu:552-594);
+ *   - the GPU partitioner's Morton ordering and edge binning, which has no
+ *     reference counterpart beyond the part bookkeeping of
+ *     moldyn/irregular/partitioner.cpp:142-297; the oracle fixes the exact
+ *     integer results the GPU pass must reproduce bit for bit.
+ *
+ * Parity pinning: the restated `map`/`map1` numerics are checked against the
+ * reference's own FCPU::map compiled from its sources (oracle/ref_harness.cpp,
+ * built into oracle/_ref/), and the neighbour builders against the two known
+ * list sizes the reference logs (miniMD/2:13 and moldyn/irresult/2:5).
+ */
+#ifndef IRR_ORACLE_H_
+#define IRR_ORACLE_H_
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Lennard-Jones law in the reference's form r*(r^-14 - r^-8/2) (the LJ force
+ * divided by 48 at eps = sigma = 1).  periodic != 0 selects moldyn's minimum
+ * image (moldyn/irregular.h:51-60) with box side `side`; cutoff2 is the
+ * squared force cutoff compared with `<` (moldyn/irregular.h:64,
+ * miniMD/irregular.h:133). */
+typedef struct {
+    double side;
+    double cutoff2;
+    int periodic;
+} orc_lj_param;
+
+/* FP64 reduction over all edges (the oracle).  pos: 3n doubles.  f: 3n out.
+ * sabs (optional): per node and component, the sum over incident in-cutoff
+ * edges of |d_c| * (r^-14 + r^-8/2) -- the magnitude of the terms before
+ * cancellation, used as the per-node error scale. */
+void orc_lj_reduce_f64(int64_t n, const double *pos, int64_t e, const int32_t *edges,
+                       const orc_lj_param *p, double *f, double *sabs);
+
+/* The reference's CPU numerics, single-threaded and deterministic: per edge
+ * the FP64 `map` result is rounded to float (VALUE is float3,
+ * moldyn/irregular/parameters.h:21-28) and added with float `+=` in edge
+ * order, +f to idx0 and -f to idx1. */
+void orc_lj_reduce_refnum_f32(int64_t n, const double *pos, int64_t e, const int32_t *edges,
+                              const orc_lj_param *p, float *f);
+
+/* Port of the reference's CPU executor (moldyn/irregular/cpu_kernel.cu:13-70):
+ * `threads` workers take `chunk` consecutive edges at a time from a
+ * mutex-guarded cursor, run the FP64 per-edge law and insert both endpoint
+ * contributions into a private open-addressing table with a per-bucket CAS
+ * lock and linear probing (moldyn/irregular/roc.cu:11-65).  Table set-up is
+ * excluded from the timing, as re_init is in the reference.  The tables are
+ * then merged in thread order into f (the reference's merge is a no-op,
+ * roc.cu:67-77, so the harness merges).  Returns 0 on success; *seconds gets
+ * the fork-to-join wall time (irregular_runtime.cu:286-301). */
+int orc_cpu_executor(int64_t n, const double *pos, int64_t e, const int32_t *edges,
+                     const orc_lj_param *p, int threads, int64_t chunk, float *f,
+                     double *seconds);
+
+/* Same executor over float xyz positions (12 B per node) and a caller-owned
+ * set of tables, so a benchmark can time repeated passes without
+ * re-allocating.  Returns seconds of the fork-to-join region, < 0 on error. */
+typedef struct orc_exec orc_exec;
+orc_exec *orc_exec_create(int64_t n, int threads);
+double orc_exec_run(orc_exec *x, const float *pos, int64_t e, const int32_t *edges,
+                    const orc_lj_param *p, int64_t chunk, float *f_out);
+void orc_exec_destroy(orc_exec *x);
+
+/* Half neighbour list by cell binning.  pos: 3n floats.  box > 0 selects
+ * periodic minimum image with side `box`; box == 0 is open boundaries
+ * (miniMD builds no ghosts, miniMD/neighbor.cpp:76-205).  A pair i<j is
+ * listed when r2 <= list_cut2, r2 evaluated in float as
+ * ((dx*dx + dy*dy) + dz*dz) with each operation rounded (no FMA), d wrapped
+ * once by +-box when |d| > box/2.  Output pairs are (i, j), i < j, sorted by
+ * i then j.  Returns the pair count; writes at most cap pairs when out is
+ * non-NULL.  Returns -1 on bad arguments. */
+int64_t orc_neighbor_half_list(int64_t n, const float *pos, float box, float list_cut2,
+                               int32_t *out, int64_t cap);
+
+/* FCC lattice of moldyn's InitCoordinates (moldyn/moldyn.cu:596-626):
+ * 4*m^3 points, spacing side/m.  pos: 3*4*m^3 doubles. */
+void orc_fcc_moldyn(int m, double side, double *pos);
+/* FCC lattice of miniMD's create_atoms (miniMD/setup.cpp:61-122) for an
+ * nx*ny*nz cell box at density rho; returns the atom count written. */
+int64_t orc_fcc_minimd(int nx, int ny, int nz, double rho, double *pos, int64_t cap);
+
+/* Partition oracle.  Morton key of each node from float positions: per axis
+ * q = trunc((x - lo) * scale) clamped to [0, 1023] (float ops, each rounded),
+ * key = bit interleave of (qx, qy, qz), x in the lowest bit. */
+void orc_morton_keys(int64_t n, const float *pos, const float lo[3], const float scale[3],
+                     uint32_t *keys);
+/* Full partition: stable sort by key (ties by node id) gives perm[new]=old
+ * and inv[old]=new; every half edge (i, j) at list position t yields the
+ * directed entries (inv[i] <- inv[j]) then (inv[j] <- inv[i]); a stable
+ * bin of all entries by row gives row_off[n+1] and col[2e]. */
+int orc_partition(int64_t n, const float *pos, const float lo[3], const float scale[3],
+                  int64_t e, const int32_t *edges, int32_t *perm, int32_t *inv,
+                  int64_t *row_off, int32_t *col);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,76 @@
+"""The C-ABI library loads and exports every symbol include/*.h declares
+(CPU only: no compute call is made without a GPU)."""
+import glob
+import os
+import re
+import subprocess
+
+import pytest
+
+from conftest import ROOT
+
+
+def declared_symbols():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        src = open(h).read()
+        names |= set(re.findall(r"IRR_API\s+[\w\s\*]*?\b(irr_\w+)\s*\(", src))
+    return names
+
+
+def exported_symbols(path):
+    out = subprocess.run(["nm", "-D", "--defined-only", path], capture_output=True, text=True,
+                         check=True).stdout
+    return {ln.split()[-1] for ln in out.splitlines() if " T " in ln}
+
+
+def test_header_declares_entry_points():
+    names = declared_symbols()
+    for required in ("irr_create", "irr_destroy", "irr_set_edges", "irr_set_nodes",
+                     "irr_set_params", "irr_step", "irr_get_result", "irr_last_error"):
+        assert required in names
+
+
+def test_library_exports_every_declared_symbol(built_lib):
+    import irregular_gb300 as irr
+    exported = exported_symbols(irr.LIB_PATH)
+    declared = declared_symbols()
+    assert declared <= exported, f"missing: {sorted(declared - exported)}"
+    assert {s for s in exported if s.startswith("irr_")} == declared
+
+
+def test_binding_covers_header(built_lib):
+    import irregular_gb300 as irr
+    assert declared_symbols() <= set(irr._SIGS)
+
+
+def test_status_strings_and_defaults(built_lib):
+    import irregular_gb300 as irr
+    L = irr.load()
+    assert L.irr_status_string(0) == b"ok"
+    assert L.irr_status_string(2) == b"edge endpoint out of range"
+    cfg = irr.default_config()
+    assert cfg.exec == irr.IRR_EXEC_PARTITIONED and cfg.reorder == 1 and cfg.stage_smem == -1
+
+
+def test_create_rejects_bad_config_without_crashing(built_lib):
+    import irregular_gb300 as irr
+    for bad in (dict(exec=7), dict(map_idx=9), dict(block_nodes=100), dict(lanes_per_row=3)):
+        with pytest.raises(irr.IrregularError) as ei:
+            irr.Handle(irr.default_config(**bad))
+        assert ei.value.status in (irr.IRR_ERR_ARG, irr.IRR_ERR_CUDA)
+
+
+def test_no_gpu_fails_loudly(built_lib):
+    """On a host without a GPU the product path raises; it never computes on the CPU."""
+    import irregular_gb300 as irr
+    try:
+        import torch
+        has_gpu = torch.cuda.is_available()
+    except Exception:
+        has_gpu = False
+    if has_gpu:
+        pytest.skip("a GPU is present")
+    with pytest.raises(irr.IrregularError) as ei:
+        irr.Handle()
+    assert ei.value.status == irr.IRR_ERR_CUDA

@@ -1,0 +1,288 @@
+"""Parity of the CUDA reduction with the oracle, through the C ABI (GPU).
+
+Every case compares the GPU result with
+  * the reference's own CPU result (golden fixtures): per node and component
+    within 1e-5 of the FP64 absolute-term scale (FP32 reordering), and
+  * the FP64 oracle: normwise max|df|/max|f| <= 1e-6.
+Integer outputs (the partition) are compared bit for bit.
+"""
+import numpy as np
+import pytest
+
+from helpers import (TOL_NORMWISE_F64, TOL_PERNODE_F64, TOL_VS_REFERENCE, golden_names,
+                     load_golden, map_idx_of, normwise_error, oracle_param, random_box,
+                     scaled_error)
+
+pytestmark = pytest.mark.gpu
+
+SHAPES = {
+    "plain": dict(exec=0),
+    "part": dict(exec=1),
+    "part_g4": dict(exec=1, lanes_per_row=4),
+    "part_g16": dict(exec=1, lanes_per_row=16),
+    "part_g32": dict(exec=1, lanes_per_row=32),
+    "part_smem": dict(exec=1, stage_smem=1),
+    "part_smem_b2048": dict(exec=1, stage_smem=1, block_nodes=2048),
+    "part_b64": dict(exec=1, block_nodes=64),
+    "part_noreorder": dict(exec=1, reorder=0),
+}
+
+
+def run_case(irr, case, elm_out=12, **cfg):
+    h = irr.Handle(irr.default_config(map_idx=map_idx_of(case), **cfg))
+    h.set_params(case["param"])
+    h.set_edges(case["edges"])
+    h.set_nodes(case["pos"], 24)
+    h.step()
+    f = h.get_result(elm_size=elm_out)
+    return f, h
+
+
+@pytest.mark.parametrize("shape", sorted(SHAPES))
+@pytest.mark.parametrize("name", golden_names())
+def test_parity_golden(built_lib, oracle_lib, name, shape):
+    import irregular_gb300 as irr
+    O = oracle_lib
+    c = load_golden(name)
+    f, h = run_case(irr, c, **SHAPES[shape])
+    f64, sabs = O.lj_reduce_f64(c["pos"], c["edges"], oracle_param(O, c))
+    assert scaled_error(f, c["f_ref"], sabs) <= TOL_VS_REFERENCE
+    assert normwise_error(f, f64) <= TOL_NORMWISE_F64
+    assert scaled_error(f, f64, sabs) <= TOL_PERNODE_F64
+    h.close()
+
+
+@pytest.mark.parametrize("name", golden_names())
+@pytest.mark.parametrize("reorder", [1, 0])
+def test_partition_bit_exact(built_lib, oracle_lib, name, reorder):
+    import irregular_gb300 as irr
+    O = oracle_lib
+    c = load_golden(name)
+    h = irr.Handle(irr.default_config(map_idx=map_idx_of(c), exec=1, reorder=reorder))
+    h.set_params(c["param"])
+    h.set_edges(c["edges"])
+    h.set_nodes(c["pos"], 24)
+    h.init()
+    perm, row_off, col = h.partition()
+    pos32 = c["pos"].astype(np.float32)
+    if reorder:
+        lo, scale = O.morton_frame(pos32)
+    else:
+        lo, scale = np.zeros(3, np.float32), np.zeros(3, np.float32)  # all keys 0: identity
+    operm, oinv, orow, ocol = O.partition(pos32, lo, scale, c["edges"])
+    assert np.array_equal(perm, operm)
+    assert np.array_equal(row_off, orow)
+    assert np.array_equal(col, ocol)
+
+
+@pytest.mark.parametrize("shape", ["part", "part_smem", "part_g32"])
+def test_partitioned_is_bitwise_reproducible(built_lib, shape):
+    import irregular_gb300 as irr
+    c = load_golden("moldyn_random_2048")
+    f1, h1 = run_case(irr, c, **SHAPES[shape])
+    h1.step()
+    f2 = h1.get_result(elm_size=12)
+    f3, _ = run_case(irr, c, **SHAPES[shape])
+    assert np.array_equal(f1.view(np.uint32), f2.view(np.uint32))
+    assert np.array_equal(f1.view(np.uint32), f3.view(np.uint32))
+
+
+@pytest.mark.parametrize("exec_mode", [0, 1])
+def test_result_formats_agree(built_lib, exec_mode):
+    import irregular_gb300 as irr
+    c = load_golden("minimd_fcc_864")
+    f12, h = run_case(irr, c, exec=exec_mode)
+    f16 = h.get_result(elm_size=16)
+    f24 = h.get_result(elm_size=24)
+    assert np.array_equal(f12, f16[:, :3]) and np.all(f16[:, 3] == 0)
+    assert np.array_equal(f12.astype(np.float64), f24)
+
+
+@pytest.mark.parametrize("exec_mode", [0, 1])
+@pytest.mark.parametrize("fmt", [12, 16, 24])
+def test_reset_node_data(built_lib, oracle_lib, exec_mode, fmt):
+    """reset_node_data between iterations (irregular_runtime.cu:436-439), every node format."""
+    import irregular_gb300 as irr
+    O = oracle_lib
+    c = load_golden("moldyn_random_2048")
+    h = irr.Handle(irr.default_config(map_idx=0, exec=exec_mode))
+    h.set_params(c["param"])
+    h.set_edges(c["edges"])
+    h.set_nodes(c["pos"], 24)
+    h.step()
+    rng = np.random.Generator(np.random.PCG64(11))
+    L = np.float32(c["side"])
+    pos2 = ((c["pos"].astype(np.float32) + rng.normal(0, 0.05, c["pos"].shape).astype(np.float32))
+            % L).astype(np.float32)
+    if fmt == 24:
+        h.set_nodes(pos2.astype(np.float64), 24)
+    elif fmt == 16:
+        h.set_nodes(np.concatenate([pos2, np.full((pos2.shape[0], 1), 7, np.float32)], 1), 16)
+    else:
+        h.set_nodes(pos2, 12)
+    h.step()
+    f = h.get_result(elm_size=12)
+    p = oracle_param(O, c)
+    f64, sabs = O.lj_reduce_f64(pos2.astype(np.float64), c["edges"], p)
+    fr = O.lj_reduce_refnum(pos2.astype(np.float64), c["edges"], p)
+    assert scaled_error(f, fr, sabs) <= TOL_VS_REFERENCE
+    assert normwise_error(f, f64) <= TOL_NORMWISE_F64
+
+
+@pytest.mark.parametrize("exec_mode", [0, 1])
+def test_empty_edge_list(built_lib, exec_mode):
+    import irregular_gb300 as irr
+    h = irr.Handle(irr.default_config(map_idx=0, exec=exec_mode))
+    h.set_params(irr.moldyn_params(20.0, 2.5))
+    h.set_edges(np.zeros((0, 2), np.int32))
+    h.set_nodes(np.random.default_rng(0).random((100, 3)) * 20, 24)
+    h.step()
+    assert np.all(h.get_result(elm_size=12) == 0)
+
+
+@pytest.mark.parametrize("exec_mode", [0, 1])
+def test_out_of_range_endpoint_is_an_error(built_lib, exec_mode):
+    import irregular_gb300 as irr
+    h = irr.Handle(irr.default_config(map_idx=0, exec=exec_mode))
+    h.set_params(irr.moldyn_params(20.0, 2.5))
+    h.set_edges(np.array([[0, 1], [2, 100]], np.int32))
+    h.set_nodes(np.random.default_rng(0).random((100, 3)) * 20, 24)
+    with pytest.raises(irr.IrregularError) as ei:
+        h.step()
+    assert ei.value.status == irr.IRR_ERR_INDEX
+    h.set_edges(np.array([[0, 1], [-1, 3]], np.int32))
+    with pytest.raises(irr.IrregularError) as ei:
+        h.init()
+    assert ei.value.status == irr.IRR_ERR_INDEX
+
+
+@pytest.mark.parametrize("exec_mode", [0, 1])
+def test_self_loop_gives_nan_like_reference(built_lib, oracle_lib, exec_mode):
+    """An edge (i, i) has rd = 0 < cutoff^2: the reference's map computes
+    inf - inf and inserts NaN; so does the kernel.  Other nodes are unaffected."""
+    import irregular_gb300 as irr
+    O = oracle_lib
+    pos = np.array([[1, 1, 1], [2, 1, 1], [5, 5, 5], [5.5, 5, 5]], np.float64)
+    edges = np.array([[0, 1], [2, 2], [2, 3]], np.int32)
+    h = irr.Handle(irr.default_config(map_idx=0, exec=exec_mode))
+    h.set_params(irr.moldyn_params(20.0, 2.5))
+    h.set_edges(edges)
+    h.set_nodes(pos, 24)
+    h.step()
+    f = h.get_result(elm_size=12)
+    fr = O.lj_reduce_refnum(pos, edges, O.lj_param(6.25, 20.0, True))
+    assert np.array_equal(np.isnan(f), np.isnan(fr))
+    assert np.all(np.isnan(f[2])) and not np.any(np.isnan(f[[0, 1]]))
+    assert np.allclose(f[[0, 1]], fr[[0, 1]], rtol=1e-6)
+
+
+def test_cutoff_boundary_follows_reference_decision(built_lib, oracle_lib):
+    """Pairs within a few ulps of the cutoff take the reference's FP64 decision."""
+    import irregular_gb300 as irr
+    O = oracle_lib
+    rc = 2.5
+    # distances straddling rc by a few float ulps along x
+    base = np.float32(10.0)
+    xs = [np.nextafter(np.float32(base + rc), np.float32(k), dtype=np.float32) for k in (0, 100)]
+    xs += [np.float32(base + rc)]
+    pos = [[base, 5, 5]]
+    for x in xs:
+        pos.append([x, 5, 5])
+    pos = np.array(pos, np.float32).astype(np.float64)
+    edges = np.array([[0, k] for k in range(1, len(pos))], np.int32)
+    for exec_mode in (0, 1):
+        h = irr.Handle(irr.default_config(map_idx=0, exec=exec_mode))
+        h.set_params(irr.moldyn_params(40.0, rc))
+        h.set_edges(edges)
+        h.set_nodes(pos, 24)
+        h.step()
+        f = h.get_result(elm_size=12)
+        fr = O.lj_reduce_refnum(pos, edges, O.lj_param(rc * rc, 40.0, True))
+        assert np.array_equal(f != 0, fr != 0)
+
+
+def test_wrapped_pairs_with_non_float_side(built_lib, oracle_lib):
+    """moldyn's side (N/0.83134)^(1/3) is not a float: pairs across the box
+    wall must still match the reference to FP32 accuracy."""
+    import irregular_gb300 as irr
+    O = oracle_lib
+    side = (1048576 / 0.83134) ** 0.3333333  # 108.045548...
+    rng = np.random.Generator(np.random.PCG64(3))
+    n = 400
+    a = (rng.random((n, 3)) * 1.0).astype(np.float32).astype(np.float64)       # near 0
+    b = (side - rng.random((n, 3)) * 1.0).astype(np.float32).astype(np.float64)  # near side
+    pos = np.concatenate([a, b])
+    edges = np.array([[i, n + i] for i in range(n)], np.int32)
+    p = O.lj_param(3.5 ** 2, side, True)
+    f64, sabs = O.lj_reduce_f64(pos, edges, p)
+    fr = O.lj_reduce_refnum(pos, edges, p)
+    for exec_mode in (0, 1):
+        h = irr.Handle(irr.default_config(map_idx=0, exec=exec_mode))
+        h.set_params(irr.moldyn_params(side, 3.5))
+        h.set_edges(edges)
+        h.set_nodes(pos, 24)
+        h.step()
+        f = h.get_result(elm_size=12)
+        assert scaled_error(f, fr, sabs) <= TOL_VS_REFERENCE
+        assert scaled_error(f, f64, sabs) <= TOL_PERNODE_F64
+
+
+def test_minimd_pbc_map(built_lib, oracle_lib):
+    import irregular_gb300 as irr
+    O = oracle_lib
+    pos32, L = random_box(3000, 0.8442, 21)
+    edges = O.neighbor_half_list(pos32, float(L), np.float32(2.8 ** 2))
+    pos = pos32.astype(np.float64)
+    p = O.lj_param(2.5 ** 2, float(L), True)
+    f64, sabs = O.lj_reduce_f64(pos, edges, p)
+    for exec_mode in (0, 1):
+        h = irr.Handle(irr.default_config(map_idx=irr.IRR_MAP_LJ_MINIMD_PBC, exec=exec_mode))
+        h.set_params(irr.minimd_params(2.5 ** 2, float(L)))
+        h.set_edges(edges)
+        h.set_nodes(pos, 24)
+        h.step()
+        f = h.get_result(elm_size=12)
+        assert normwise_error(f, f64) <= TOL_NORMWISE_F64
+        assert scaled_error(f, f64, sabs) <= TOL_PERNODE_F64
+
+
+def test_set_params_after_init(built_lib, oracle_lib):
+    import irregular_gb300 as irr
+    O = oracle_lib
+    c = load_golden("moldyn_random_2048")
+    f, h = run_case(irr, c, exec=1)
+    h.set_params(irr.moldyn_params(float(c["side"]), 2.0))
+    h.step()
+    g = h.get_result(elm_size=12)
+    p = O.lj_param(4.0, float(c["side"]), True)
+    f64, sabs = O.lj_reduce_f64(c["pos"], c["edges"], p)
+    assert normwise_error(g, f64) <= TOL_NORMWISE_F64
+    assert not np.array_equal(f, g)
+
+
+@pytest.mark.parametrize("n", [65536])
+def test_larger_random_periodic_properties(built_lib, oracle_lib, n):
+    """Config-1 shape (65,536 nodes, ~32 neighbours at 2.5): plain and
+    partitioned agree, Newton's third law holds, FP64 error bounds hold."""
+    import irregular_gb300 as irr
+    O = oracle_lib
+    rho = 32.0 / (4.0 / 3.0 * np.pi * 2.5 ** 3)
+    pos32, L = random_box(n, rho, 20260001)
+    edges = O.neighbor_half_list(pos32, float(L), np.float32(2.5 * 2.5))
+    pos = pos32.astype(np.float64)
+    p = O.lj_param(6.25, float(L), True)
+    f64, sabs = O.lj_reduce_f64(pos, edges, p)
+    fr = O.lj_reduce_refnum(pos, edges, p)
+    out = {}
+    for exec_mode in (0, 1):
+        h = irr.Handle(irr.default_config(map_idx=0, exec=exec_mode))
+        h.set_params(irr.moldyn_params(float(L), 2.5))
+        h.set_edges(edges)
+        h.set_nodes(pos, 24)
+        h.step()
+        out[exec_mode] = h.get_result(elm_size=12)
+        assert scaled_error(out[exec_mode], fr, sabs) <= TOL_VS_REFERENCE
+        assert normwise_error(out[exec_mode], f64) <= TOL_NORMWISE_F64
+        tot = np.abs(out[exec_mode].astype(np.float64).sum(axis=0))
+        assert np.all(tot <= 1e-6 * sabs.sum(axis=0))
+    assert scaled_error(out[0], out[1], sabs) <= 2 * TOL_PERNODE_F64
