@@ -101,8 +101,8 @@ typedef struct irr_config {
     int reduce_idx;    /* enum irr_reduce                                            */
     int block_nodes;   /* partitioned: nodes per block (power of two, 64..4096);
                           0 = tuned default                                          */
-    int lanes_per_row; /* partitioned: lanes summing one node's row (4, 8, 16, 32);
-                          0 = tuned default                                          */
+    int lanes_per_row; /* partitioned: lanes summing one node's row (1, 2, 4, 8, 16,
+                          32); 0 = tuned default                                     */
     int reorder;       /* partitioned: 1 = Morton order (default), 0 = keep the
                           caller's order (blocks are then cut from it)              */
     int stage_smem;    /* partitioned: 1 = copy each block's positions into shared
@@ -137,7 +137,8 @@ IRR_API int irr_destroy(irr_handle *h);
 /* Text of the last failure on this handle ("" when none). */
 IRR_API const char *irr_last_error(const irr_handle *h);
 
-/* Issue work on `stream` (a cudaStream_t) instead of the handle's own. */
+/* Issue work on `stream` (a cudaStream_t, used as given: NULL is the CUDA
+ * default stream) instead of the handle's own non-blocking stream. */
 IRR_API int irr_set_stream(irr_handle *h, void *stream);
 /* set_map_idx / set_reduce_idx (irregular_runtime.cu:493-501). */
 IRR_API int irr_set_map(irr_handle *h, int map_idx);
@@ -192,6 +193,23 @@ IRR_API int irr_get_info(const irr_handle *h, irr_info *info);
  * entries within a row in edge-list order, idx0 side first).  Any pointer may
  * be NULL. */
 IRR_API int irr_get_partition(irr_handle *h, int32_t *perm, int64_t *row_off, int32_t *col);
+
+/* ------------------------------------------------------ neighbour lists
+ * The half neighbour list the drivers build before the reduction, on the GPU
+ * as a counting-sort cell list: miniMD's binned build (miniMD/neighbor.cpp:
+ * 76-397) and moldyn's all-pairs RebuildNeighbor (moldyn/moldyn.cu:552-594).
+ * pos: n records of pos_elm bytes (12, 16 or 24; xyz first), in host memory
+ * or, with pos_on_device != 0, device memory.  box > 0: periodic cube of side
+ * box (minimum image); box == 0: open boundaries.  A pair i < j is listed when
+ * r2 <= list_cut2 with r2 = ((dx*dx + dy*dy) + dz*dz) in float, each operation
+ * rounded, d wrapped once by +-box when |d| > box/2.  On success *d_edges is a
+ * device array of 2 * *num_edges int32, pairs (i, j) sorted by i then j (free
+ * it with irr_device_free). */
+IRR_API int irr_neighbor_build(int device, void *stream, const void *pos, int pos_elm,
+                               int pos_on_device, int64_t n, float box, float list_cut2,
+                               int32_t **d_edges, int64_t *num_edges);
+/* Frees device memory this library allocated for the caller. */
+IRR_API int irr_device_free(int device, void *d_ptr);
 
 #ifdef __cplusplus
 }

@@ -47,6 +47,7 @@ struct irr_handle {
     WorkItem* d_items = nullptr;
     int num_items = 0;
     int* d_status = nullptr;
+    int* d_queue = nullptr;      // work-queue cursor, cleared before each launch
     void* d_out = nullptr;       // result staging for host reads
     size_t out_cap = 0;
     int64_t dev_bytes = 0;
@@ -146,6 +147,11 @@ int make_law(irr_handle* h)
     L.half = (float)(0.5 * side);
     L.side_hi = (float)side;
     L.side_lo = (float)(side - (double)L.side_hi);
+    // rd from the unwrapped d exceeds (side/2)^2 whenever a component needs a
+    // wrap; the margin covers rd's rounding.  Non-periodic: never wrap.
+    L.half2 = periodic ? (float)(0.25 * side * side * (1.0 - 1.0 / 65536.0)) : INFINITY;
+    // the FP64 decision band: rc2_lo < rd < rc2_hi, widened for the rounding of rd - rc2
+    L.band = (float)(rc2d * (2.0 / 262144.0));
     h->law = L;
     h->have_law = true;
     return IRR_OK;
@@ -293,8 +299,8 @@ int irr_create(const irr_config* cfg, irr_handle** out)
     if (c.map_idx < IRR_MAP_LJ_MOLDYN || c.map_idx > IRR_MAP_LJ_MINIMD_PBC) return IRR_ERR_ARG;
     if (c.block_nodes != 0 && (c.block_nodes < 64 || c.block_nodes > 4096 || (c.block_nodes & (c.block_nodes - 1))))
         return IRR_ERR_ARG;
-    if (c.lanes_per_row != 0 && c.lanes_per_row != 4 && c.lanes_per_row != 8 && c.lanes_per_row != 16 &&
-        c.lanes_per_row != 32)
+    if (c.lanes_per_row != 0 && c.lanes_per_row != 1 && c.lanes_per_row != 2 && c.lanes_per_row != 4 &&
+        c.lanes_per_row != 8 && c.lanes_per_row != 16 && c.lanes_per_row != 32)
         return IRR_ERR_ARG;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
@@ -320,10 +326,16 @@ int irr_create(const irr_config* cfg, irr_handle** out)
         return IRR_ERR_CUDA;
     }
     h->stream = h->own_stream;
-    h->shape.lanes_per_row = c.lanes_per_row ? c.lanes_per_row : 8;
+    h->shape.lanes_per_row = c.lanes_per_row ? c.lanes_per_row : 4;
     h->shape.block_nodes = c.block_nodes ? c.block_nodes : 1024;
-    h->shape.stage_smem = c.stage_smem < 0 ? 0 : (c.stage_smem ? 1 : 0);
-    if (h->shape.stage_smem && h->shape.block_nodes > kMaxStageNodes) h->shape.block_nodes = kMaxStageNodes;
+    h->shape.stage_smem = c.stage_smem < 0 ? 1 : (c.stage_smem ? 1 : 0);
+    if (cudaMalloc(&h->d_queue, sizeof(int)) != cudaSuccess) {
+        cudaGetLastError();
+        cudaStreamDestroy(h->own_stream);
+        cudaFree(h->d_status);
+        delete h;
+        return IRR_ERR_CUDA;
+    }
     *out = h;
     return IRR_OK;
 }
@@ -337,6 +349,7 @@ int irr_destroy(irr_handle* h)
     dfree(h->d_raw);
     dfree(h->d_edges);
     dfree(h->d_status);
+    dfree(h->d_queue);
     dfree(h->d_out);
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
     delete h;
@@ -348,7 +361,7 @@ const char* irr_last_error(const irr_handle* h) { return h ? h->err.c_str() : "n
 int irr_set_stream(irr_handle* h, void* stream)
 {
     if (!h) return IRR_ERR_ARG;
-    h->stream = stream ? (cudaStream_t)stream : h->own_stream;
+    h->stream = (cudaStream_t)stream;  // used as given: NULL is the default stream
     return IRR_OK;
 }
 
@@ -455,16 +468,13 @@ int irr_init(irr_handle* h)
     }
     H_CUDA(h, launch_load_nodes(h->d_raw, h->raw_elm, h->part.perm, n, h->d_pos, s), "gather node data");
     h->raw_pending = false;
-    // node blocks -> work items
-    const int K = h->shape.block_nodes;
+    // node blocks -> work items (cut on the row offsets)
+    std::vector<uint32_t> ro((size_t)n + 1);
+    H_CUDA(h, cudaMemcpyAsync(ro.data(), h->part.row_off, sizeof(uint32_t) * (n + 1), cudaMemcpyDeviceToHost, s),
+           "copy row offsets");
+    H_CUDA(h, cudaStreamSynchronize(s), "copy row offsets");
     std::vector<WorkItem> items;
-    for (int64_t r0 = 0; r0 < n; r0 += K) {
-        WorkItem w{};
-        w.inst = 0;
-        w.row0 = (int32_t)r0;
-        w.nrows = (int32_t)(n - r0 < K ? n - r0 : K);
-        items.push_back(w);
-    }
+    make_work_items(ro.data(), n, 0, h->shape.block_nodes, h->shape.stage_smem, items);
     h->num_items = (int)items.size();
     H_CUDA(h, cudaMalloc(&h->d_items, sizeof(WorkItem) * (items.size() ? items.size() : 1)), "allocate work items");
     if (!items.empty())
@@ -500,7 +510,9 @@ int irr_step(irr_handle* h)
         H_CUDA(h, launch_plain(h->d_pos, h->d_edges, h->e, h->d_force, h->law, h->stream), "plain kernel");
         return IRR_OK;
     }
-    H_CUDA(h, launch_tiled(h->shape, h->d_inst, h->d_items, h->num_items, nullptr, 0, h->d_status, h->stream),
+    H_CUDA(h, cudaMemsetAsync(h->d_queue, 0, sizeof(int), h->stream), "clear work queue");
+    H_CUDA(h, launch_tiled(h->shape, h->d_inst, h->d_items, h->num_items, h->d_queue,
+                           h->sms * kCtasPerSm, h->d_status, h->stream),
            "tiled kernel");
     return IRR_OK;
 }

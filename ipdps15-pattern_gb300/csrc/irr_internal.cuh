@@ -3,6 +3,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <string>
+#include <vector>
 #include <cuda_runtime.h>
 
 #include "irr_law.cuh"
@@ -26,23 +27,36 @@ struct InstDesc {
     int64_t n;
 };
 
-// One node block: rows [row0, row0 + nrows) of instance `inst`.
+// One node block: rows [row0, row0 + nrows) of instance `inst`, whose
+// directed entries are [ent0, ent0 + nent) of the instance's col array.
 struct WorkItem {
     int32_t inst;
     int32_t row0;
     int32_t nrows;
-    int32_t pad_;
+    int32_t flags;       // kItemDirect: read entries from global memory
+    uint32_t ent0;
+    uint32_t nent;
 };
+
+enum : int { kItemDirect = 1 };
 
 struct TiledShape {
     int lanes_per_row;   // 4, 8, 16 or 32
-    int stage_smem;      // 0 or 1
-    int block_nodes;     // max rows per work item (stage_smem: <= kMaxStageNodes)
+    int stage_smem;      // 1: entry segments bulk-copied into a shared-memory ring
+    int block_nodes;     // max rows per work item
     int periodic;
 };
 
 constexpr int kTiledThreads = 256;
-constexpr int kMaxStageNodes = 2048;   // 32 KB of float4 in shared memory
+constexpr int kStages = 4;             // shared-memory ring depth
+constexpr int kStageEntries = 4096;    // entries per stage (16 KB)
+constexpr int kColPad = 4;             // entries allocated past the end of col
+constexpr int kCtasPerSm = 3;        // resident CTAs per SM (registers and the ring)
+
+// Cuts rows [0, n) into work items of at most max_rows rows and (unless a
+// single row is longer) at most kStageEntries entries.  row_off: host copy.
+void make_work_items(const uint32_t* row_off, int64_t n, int inst, int max_rows, int staged,
+                     std::vector<WorkItem>& out);
 
 // -- reduction kernels (irr_reduce.cu) --
 cudaError_t launch_plain(const float4* pos, const int2* edges, int64_t e, float4* force,
@@ -71,6 +85,8 @@ struct PartitionOut {
     uint32_t* row_off = nullptr;  // [n + 1]
     int32_t* col = nullptr;       // [2e]
 };
+// Per-axis min and max of pos (synchronises s).
+cudaError_t bbox_minmax(const float4* pos, int64_t n, float lo[3], float hi[3], cudaStream_t s);
 // Computes the Morton frame (per-axis min and 1024 / extent) of pos.
 cudaError_t bbox_frame(const float4* pos, int64_t n, float lo[3], float scale[3],
                        cudaStream_t s);
@@ -78,6 +94,9 @@ cudaError_t bbox_frame(const float4* pos, int64_t n, float lo[3], float scale[3]
 // cudaMallocAsync on s (caller frees).  reorder == 0 keeps the identity order.
 cudaError_t build_partition(const float4* pos_user, int64_t n, const int2* edges, int64_t e,
                             int reorder, PartitionOut* out, cudaStream_t s);
+// Half neighbour list (irr_neighbor.cu); *d_edges is cudaMalloc'd.
+cudaError_t build_neighbor_list(const float4* pos, int64_t n, float box, float cut2,
+                                int2** d_edges, int64_t* num_edges, cudaStream_t s);
 // Stable LSD radix sort of (key, value) pairs on key bits [0, key_bits).
 // Sorted data ends in (keys, vals); tmp arrays have n entries each.
 cudaError_t radix_sort_pairs(uint32_t* keys, int32_t* vals, uint32_t* keys_tmp,

@@ -36,6 +36,8 @@ struct LawParams {
     float side_hi;  // side = side_hi + side_lo
     float side_lo;
     int periodic;
+    float half2;    // (side/2)^2 less a margin: rd <= half2 needs no wrap
+    float band;     // |rd - rc2| < band: FP64 decision (rc2_lo/rc2_hi in one test)
     int pad_;
     double rc2d;    // the reference's cutoff^2 (moldyn: cutoffRadius*cutoffRadius)
     double side;

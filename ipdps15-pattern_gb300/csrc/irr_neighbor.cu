@@ -1,0 +1,306 @@
+// irr_neighbor.cu -- half neighbour list on the GPU by a counting-sort cell list.
+//
+// Replaces miniMD's serial binned build (miniMD/neighbor.cpp:76-205: linked-list
+// bins filled by binatoms :209-239, a half stencil from setup :289-397) and
+// moldyn's O(N^2) all-pairs RebuildNeighbor (moldyn/moldyn.cu:552-594):
+//   1. each node gets a cell key (cells at least as wide as the list cutoff);
+//   2. a stable radix sort by key orders nodes by cell; a count + scan gives
+//      each cell's start;
+//   3. one thread per node (in cell order, so a warp shares cells) scans the
+//      27 surrounding cells for partners j > i with r2 <= cut2, first counting,
+//      then -- after a scan of the counts -- writing them, sorted by j.
+// The pair rule is shared bit for bit with the CPU oracle: d = x_i - x_j in
+// float, wrapped once by +-box when |d| > box/2 (periodic), r2 = ((dx*dx +
+// dy*dy) + dz*dz) with every operation rounded.  Output: pairs (i, j), i < j,
+// sorted by i then j -- moldyn's loop order; miniMD lists the same pairs.
+#include <cmath>
+
+#include "irr_internal.cuh"
+#include "../../include/irregular_gb300.h"
+
+namespace irr {
+namespace {
+
+struct Grid {
+    int nc[3];
+    int offs[3][3];   // neighbour cell offsets per axis (deduplicated)
+    int noff[3];
+    double org[3];
+    double inv[3];    // 1 / cell size
+    float box, hb, cut2;
+    int periodic;
+};
+
+__device__ __forceinline__ bool list_pair(float4 a, float4 b, const Grid& g)
+{
+    float d[3] = {__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y), __fsub_rn(a.z, b.z)};
+    if (g.periodic) {
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            if (d[c] > g.hb)
+                d[c] = __fsub_rn(d[c], g.box);
+            else if (d[c] < -g.hb)
+                d[c] = __fadd_rn(d[c], g.box);
+        }
+    }
+    const float r2 = __fadd_rn(__fadd_rn(__fmul_rn(d[0], d[0]), __fmul_rn(d[1], d[1])),
+                               __fmul_rn(d[2], d[2]));
+    return r2 <= g.cut2;
+}
+
+__device__ __forceinline__ int cell_coord(float x, int axis, const Grid& g)
+{
+    long long k = (long long)floor(((double)x - g.org[axis]) * g.inv[axis]);
+    if (g.periodic) k = ((k % g.nc[axis]) + g.nc[axis]) % g.nc[axis];
+    if (k < 0) k = 0;
+    if (k >= g.nc[axis]) k = g.nc[axis] - 1;
+    return (int)k;
+}
+
+__global__ void cell_keys_kernel(const float4* pos, int64_t n, Grid g, uint32_t* keys,
+                                 int32_t* vals, uint32_t* cell_count)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const float4 p = pos[i];
+        const uint32_t c = ((uint32_t)cell_coord(p.z, 2, g) * g.nc[1] + cell_coord(p.y, 1, g)) *
+                               g.nc[0] +
+                           cell_coord(p.x, 0, g);
+        keys[i] = c;
+        vals[i] = (int32_t)i;
+        atomicAdd(cell_count + c, 1u);
+    }
+}
+
+// WRITE == false: counts partners; WRITE == true: writes them at row_off[i]
+// and sorts the row by j.
+template <bool WRITE>
+__global__ void pairs_kernel(const float4* __restrict__ pos, const int32_t* __restrict__ sorted,
+                             const uint32_t* __restrict__ cell_start, int64_t n, Grid g,
+                             uint32_t* count, const uint32_t* __restrict__ row_off, int32_t* nbr)
+{
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t i = sorted[t];
+        const float4 a = pos[i];
+        const int cx = cell_coord(a.x, 0, g), cy = cell_coord(a.y, 1, g), cz = cell_coord(a.z, 2, g);
+        uint32_t m = 0;
+        const uint32_t base = WRITE ? row_off[i] : 0;
+        for (int oz = 0; oz < g.noff[2]; oz++) {
+            int z = cz + g.offs[2][oz];
+            if (g.periodic) z = (z + g.nc[2]) % g.nc[2];
+            else if (z < 0 || z >= g.nc[2]) continue;
+            for (int oy = 0; oy < g.noff[1]; oy++) {
+                int y = cy + g.offs[1][oy];
+                if (g.periodic) y = (y + g.nc[1]) % g.nc[1];
+                else if (y < 0 || y >= g.nc[1]) continue;
+                for (int ox = 0; ox < g.noff[0]; ox++) {
+                    int x = cx + g.offs[0][ox];
+                    if (g.periodic) x = (x + g.nc[0]) % g.nc[0];
+                    else if (x < 0 || x >= g.nc[0]) continue;
+                    const uint32_t c = ((uint32_t)z * g.nc[1] + y) * g.nc[0] + x;
+                    for (uint32_t q = cell_start[c]; q < cell_start[c + 1]; q++) {
+                        const int32_t j = sorted[q];
+                        if (j <= i) continue;
+                        if (list_pair(a, pos[j], g)) {
+                            if (WRITE) nbr[base + m] = j;
+                            m++;
+                        }
+                    }
+                }
+            }
+        }
+        if (!WRITE) {
+            count[i] = m;
+        } else {
+            // insertion sort of the row (rows are short: tens of entries)
+            for (uint32_t u = 1; u < m; u++) {
+                const int32_t v = nbr[base + u];
+                uint32_t w = u;
+                while (w > 0 && nbr[base + w - 1] > v) {
+                    nbr[base + w] = nbr[base + w - 1];
+                    w--;
+                }
+                nbr[base + w] = v;
+            }
+        }
+    }
+}
+
+__global__ void expand_pairs_kernel(const uint32_t* row_off, const int32_t* nbr, int64_t n,
+                                    int2* edges)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        for (uint32_t k = row_off[i]; k < row_off[i + 1]; k++) edges[k] = make_int2((int)i, nbr[k]);
+}
+
+int grid_of(int64_t n)
+{
+    int64_t g = (n + 255) / 256;
+    return (int)(g < 1 ? 1 : (g > 8192 ? 8192 : g));
+}
+
+}  // namespace
+
+// Builds the list; *d_edges is cudaMalloc'd (2 * *num_edges int32).
+cudaError_t build_neighbor_list(const float4* pos, int64_t n, float box, float cut2,
+                                int2** d_edges, int64_t* num_edges, cudaStream_t s)
+{
+    *d_edges = nullptr;
+    *num_edges = 0;
+    if (n <= 1) return cudaSuccess;
+    Grid g{};
+    g.periodic = box > 0.0f;
+    g.box = box;
+    g.hb = 0.5f * box;
+    g.cut2 = cut2;
+    const double cut = std::sqrt((double)cut2) * 1.0001 + 1e-12;
+    double lo[3] = {0, 0, 0}, ext[3] = {box, box, box};
+    if (!g.periodic) {
+        float flo[3], fhi[3];
+        IRR_CUDA_TRY(bbox_minmax(pos, n, flo, fhi, s));
+        for (int c = 0; c < 3; c++) {
+            lo[c] = flo[c];
+            ext[c] = (double)fhi[c] - (double)flo[c];
+        }
+    }
+    for (int c = 0; c < 3; c++) {
+        int k = (int)std::floor(ext[c] / cut);
+        if (g.periodic && k < 3) k = 1;
+        if (k < 1) k = 1;
+        if (k > 1024) k = 1024;
+        g.nc[c] = k;
+    }
+    // keep the cell count within a few cells per node (coarser cells stay valid)
+    while ((double)g.nc[0] * g.nc[1] * g.nc[2] > 8.0 * (double)n + 64.0) {
+        int a = (g.nc[0] >= g.nc[1] && g.nc[0] >= g.nc[2]) ? 0 : (g.nc[1] >= g.nc[2] ? 1 : 2);
+        g.nc[a] = g.nc[a] / 2;
+        if (g.periodic && g.nc[a] < 3) g.nc[a] = 1;
+        if (g.nc[a] < 1) g.nc[a] = 1;
+    }
+    for (int c = 0; c < 3; c++) {
+        g.org[c] = g.periodic ? 0.0 : lo[c];
+        // slightly wider cells than ext/nc so the max coordinate maps inside
+        // (clamped anyway); the layout never decides a pair, the rule does
+        const double csz = ext[c] > 0 ? ext[c] / g.nc[c] : 1.0;
+        g.inv[c] = 1.0 / csz;
+        if (g.nc[c] >= 3) {
+            g.offs[c][0] = -1; g.offs[c][1] = 0; g.offs[c][2] = 1; g.noff[c] = 3;
+        } else if (g.nc[c] == 2) {
+            g.offs[c][0] = 0; g.offs[c][1] = 1; g.noff[c] = 2;
+            if (!g.periodic) { g.offs[c][0] = -1; g.offs[c][1] = 0; g.offs[c][2] = 1; g.noff[c] = 3; }
+        } else {
+            g.offs[c][0] = 0; g.noff[c] = 1;
+        }
+    }
+    const int64_t ncell = (int64_t)g.nc[0] * g.nc[1] * g.nc[2];
+    uint32_t *keys = nullptr, *keys_tmp = nullptr, *cell_start = nullptr, *cnt = nullptr;
+    int32_t *sorted = nullptr, *vals_tmp = nullptr, *nbr = nullptr;
+    IRR_CUDA_TRY(cudaMallocAsync((void**)&keys, sizeof(uint32_t) * n, s));
+    IRR_CUDA_TRY(cudaMallocAsync((void**)&keys_tmp, sizeof(uint32_t) * n, s));
+    IRR_CUDA_TRY(cudaMallocAsync((void**)&sorted, sizeof(int32_t) * n, s));
+    IRR_CUDA_TRY(cudaMallocAsync((void**)&vals_tmp, sizeof(int32_t) * n, s));
+    IRR_CUDA_TRY(cudaMallocAsync((void**)&cell_start, sizeof(uint32_t) * (ncell + 1), s));
+    IRR_CUDA_TRY(cudaMallocAsync((void**)&cnt, sizeof(uint32_t) * (n + 1), s));
+    IRR_CUDA_TRY(cudaMemsetAsync(cell_start, 0, sizeof(uint32_t) * (ncell + 1), s));
+    cell_keys_kernel<<<grid_of(n), 256, 0, s>>>(pos, n, g, keys, sorted, cell_start);
+    IRR_CUDA_TRY(cudaGetLastError());
+    int bits = 1;
+    while (bits < 32 && ((int64_t)1 << bits) < ncell) bits++;
+    IRR_CUDA_TRY(radix_sort_pairs(keys, sorted, keys_tmp, vals_tmp, n, bits, s));
+    IRR_CUDA_TRY(scan_exclusive_u32(cell_start, cell_start, ncell + 1, nullptr, s));
+    pairs_kernel<false><<<grid_of(n), 256, 0, s>>>(pos, sorted, cell_start, n, g, cnt, nullptr,
+                                                   nullptr);
+    IRR_CUDA_TRY(cudaGetLastError());
+    IRR_CUDA_TRY(cudaMemsetAsync(cnt + n, 0, sizeof(uint32_t), s));
+    uint32_t* d_total = keys_tmp;  // reuse as the total's slot
+    IRR_CUDA_TRY(scan_exclusive_u32(cnt, cnt, n + 1, d_total, s));
+    uint32_t total = 0;
+    IRR_CUDA_TRY(cudaMemcpyAsync(&total, d_total, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    IRR_CUDA_TRY(cudaStreamSynchronize(s));
+    if ((int64_t)total > 0x7fffffffLL) return cudaErrorInvalidValue;
+    int2* edges = nullptr;
+    if (total > 0) {
+        IRR_CUDA_TRY(cudaMallocAsync((void**)&nbr, sizeof(int32_t) * total, s));
+        pairs_kernel<true><<<grid_of(n), 256, 0, s>>>(pos, sorted, cell_start, n, g, nullptr, cnt,
+                                                      nbr);
+        IRR_CUDA_TRY(cudaGetLastError());
+        IRR_CUDA_TRY(cudaMalloc((void**)&edges, sizeof(int2) * total));
+        expand_pairs_kernel<<<grid_of(n), 256, 0, s>>>(cnt, nbr, n, edges);
+        IRR_CUDA_TRY(cudaGetLastError());
+        IRR_CUDA_TRY(cudaFreeAsync(nbr, s));
+    }
+    IRR_CUDA_TRY(cudaFreeAsync(keys, s));
+    IRR_CUDA_TRY(cudaFreeAsync(keys_tmp, s));
+    IRR_CUDA_TRY(cudaFreeAsync(sorted, s));
+    IRR_CUDA_TRY(cudaFreeAsync(vals_tmp, s));
+    IRR_CUDA_TRY(cudaFreeAsync(cell_start, s));
+    IRR_CUDA_TRY(cudaFreeAsync(cnt, s));
+    IRR_CUDA_TRY(cudaStreamSynchronize(s));
+    *d_edges = edges;
+    *num_edges = total;
+    return cudaSuccess;
+}
+
+}  // namespace irr
+
+extern "C" {
+
+int irr_neighbor_build(int device, void* stream, const void* pos, int pos_elm, int pos_on_device,
+                       int64_t n, float box, float list_cut2, int32_t** d_edges,
+                       int64_t* num_edges)
+{
+    if (!d_edges || !num_edges || n < 0 || (n > 0 && !pos)) return IRR_ERR_ARG;
+    if (pos_elm != 12 && pos_elm != 16 && pos_elm != 24) return IRR_ERR_ARG;
+    if (!(box >= 0.0f) || !(list_cut2 >= 0.0f) || !std::isfinite(box) || !std::isfinite(list_cut2))
+        return IRR_ERR_ARG;
+    if (n > 0x7fffffffLL) return IRR_ERR_CAPACITY;
+    *d_edges = nullptr;
+    *num_edges = 0;
+    if (cudaSetDevice(device) != cudaSuccess) {
+        cudaGetLastError();
+        return IRR_ERR_CUDA;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    void* raw = nullptr;
+    float4* p4 = nullptr;
+    int rc = IRR_OK;
+    cudaError_t e = cudaSuccess;
+    const void* src = pos;
+    if (n > 0 && !pos_on_device) {
+        e = cudaMalloc(&raw, (size_t)n * pos_elm);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(raw, pos, (size_t)n * pos_elm, cudaMemcpyHostToDevice, s);
+        src = raw;
+    }
+    if (e == cudaSuccess && n > 0) e = cudaMalloc((void**)&p4, sizeof(float4) * (size_t)n);
+    if (e == cudaSuccess && n > 0) e = irr::launch_load_nodes(src, pos_elm, nullptr, n, p4, s);
+    int2* edges = nullptr;
+    int64_t cnt = 0;
+    if (e == cudaSuccess) e = irr::build_neighbor_list(p4, n, box, list_cut2, &edges, &cnt, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        rc = (e == cudaErrorMemoryAllocation) ? IRR_ERR_NOMEM : (e == cudaErrorInvalidValue ? IRR_ERR_CAPACITY : IRR_ERR_CUDA);
+        if (edges) cudaFree(edges);
+        edges = nullptr;
+        cnt = 0;
+    }
+    if (raw) cudaFree(raw);
+    if (p4) cudaFree(p4);
+    *d_edges = (int32_t*)edges;
+    *num_edges = cnt;
+    return rc;
+}
+
+int irr_device_free(int device, void* d_ptr)
+{
+    if (!d_ptr) return IRR_OK;
+    if (cudaSetDevice(device) != cudaSuccess || cudaFree(d_ptr) != cudaSuccess) {
+        cudaGetLastError();
+        return IRR_ERR_CUDA;
+    }
+    return IRR_OK;
+}
+
+}  // extern "C"

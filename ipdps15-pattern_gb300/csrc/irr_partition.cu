@@ -384,11 +384,11 @@ cudaError_t radix_sort_pairs(uint32_t* keys, int32_t* vals, uint32_t* keys_tmp,
     return err != cudaSuccess ? err : ferr;
 }
 
-cudaError_t bbox_frame(const float4* pos, int64_t n, float lo[3], float scale[3], cudaStream_t s)
+cudaError_t bbox_minmax(const float4* pos, int64_t n, float lo[3], float hi[3], cudaStream_t s)
 {
     for (int c = 0; c < 3; c++) {
         lo[c] = 0.f;
-        scale[c] = 0.f;
+        hi[c] = 0.f;
     }
     if (n <= 0) return cudaSuccess;
     const int nparts = (int)std::min<int64_t>((n + 255) / 256, 1024);
@@ -405,10 +405,20 @@ cudaError_t bbox_frame(const float4* pos, int64_t n, float lo[3], float scale[3]
     if (err != cudaSuccess) return err;
     for (int c = 0; c < 3; c++) {
         lo[c] = h[c];
-        const float ext = h[3 + c] - h[c];
-        scale[c] = ext > 0.0f ? 1024.0f / ext : 0.0f;
+        hi[c] = h[3 + c];
     }
     return ferr;
+}
+
+cudaError_t bbox_frame(const float4* pos, int64_t n, float lo[3], float scale[3], cudaStream_t s)
+{
+    float hi[3];
+    IRR_CUDA_TRY(bbox_minmax(pos, n, lo, hi, s));
+    for (int c = 0; c < 3; c++) {
+        const float ext = hi[c] - lo[c];
+        scale[c] = ext > 0.0f ? 1024.0f / ext : 0.0f;
+    }
+    return cudaSuccess;
 }
 
 cudaError_t build_partition(const float4* pos_user, int64_t n, const int2* edges, int64_t e,
@@ -419,7 +429,10 @@ cudaError_t build_partition(const float4* pos_user, int64_t n, const int2* edges
     IRR_CUDA_TRY(alloc_async(&out->perm, n, s));
     IRR_CUDA_TRY(alloc_async(&out->inv, n, s));
     IRR_CUDA_TRY(alloc_async(&out->row_off, n + 1, s));
-    IRR_CUDA_TRY(alloc_async(&out->col, 2 * e, s));
+    // + kColPad: bulk copies of an entry segment are widened to 16-byte
+    // boundaries and may read up to 3 entries past the last one
+    IRR_CUDA_TRY(alloc_async(&out->col, 2 * e + kColPad, s));
+    IRR_CUDA_TRY(cudaMemsetAsync(out->col + 2 * e, 0, sizeof(int32_t) * kColPad, s));
     const int g = grid_for(n);
     if (reorder && n > 1) {
         float lo[3], scale[3];

@@ -10,15 +10,19 @@
 // tiled_kernel: owner computes.  The partitioner hands each node a row of
 //   directed entries (one per incident edge); a group of G lanes walks the
 //   row, evaluates the law for every entry, keeps FP32 partial sums in
-//   registers and combines the G partials with error-free TwoSum steps.  A
-//   CTA takes a node block (a work item); optionally the block's positions
-//   are first copied into shared memory with one bulk (TMA) copy.  Each edge
-//   is evaluated from both ends -- the reference duplicates cross-part edges
-//   the same way (moldyn/irregular/partitioner.cpp:142-297, paper Sec. II-A)
-//   -- so no atomics are needed and every result is bitwise reproducible.
-//   With a queue it is the persistent (instance, block) work-queue kernel of
-//   the batched form, generalising the reference's per-part atomicAdd queue
-//   (gpu_kernel.cu:60-77).
+//   registers and combines the G partials with error-free TwoSum steps.  Each
+//   edge is evaluated from both ends -- the reference duplicates cross-part
+//   edges the same way (moldyn/irregular/partitioner.cpp:142-297, paper
+//   Sec. II-A) -- so no atomics are needed and every result is bitwise
+//   reproducible.  The grid is persistent: CTAs claim node blocks (work
+//   items) from a queue, the reference's per-part atomicAdd queue
+//   (gpu_kernel.cu:60-77) generalised to (instance, block) items for the
+//   batched form.  A block's entries are contiguous, so one bulk (TMA) copy
+//   per item moves them into a ring of shared-memory stages a few items
+//   ahead of the consumers: the entry stream, which is most of the traffic,
+//   is kept in flight while positions are gathered through L1.
+#include <vector>
+
 #include "irr_internal.cuh"
 
 namespace irr {
@@ -88,148 +92,275 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
 
 constexpr int kWaitPolls = 1 << 20;
 
-template <bool PERIODIC, int G, bool STAGE, int UNROLL>
-__global__ void __launch_bounds__(kTiledThreads) tiled_kernel(const InstDesc* __restrict__ insts,
-                                                              const WorkItem* __restrict__ items,
-                                                              int num_items, int* queue,
-                                                              int* status)
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar)
 {
-    extern __shared__ float4 spos[];
-    __shared__ uint64_t bar;
-    __shared__ int s_item;
-    constexpr int kGroups = kTiledThreads / G;
-    const int tid = threadIdx.x;
-    const int lane = tid % G;
-    const int gid = tid / G;
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
 
-    bool staged = STAGE;
-    if (STAGE) {
-        if (tid == 0) mbar_init(&bar, 1);
-        __syncthreads();
+// Law parameters the inner loop keeps in registers; the rest (box side as a
+// float pair, FP64 cutoff) is read from the instance descriptor on the rare
+// paths that need it.
+struct HotLaw {
+    float half2;   // just under (side/2)^2: rd at or below it never needs a wrap
+    float rc2;
+    float band;    // |rd - rc2| < band: take the reference's FP64 decision
+};
+
+// A pair wrapped across the box wall, recomputed exactly (irr_law.cuh).
+__device__ __noinline__ float3 wrap_exact(float4 a, float4 b, const LawParams* __restrict__ P)
+{
+    const LawParams L = *P;
+    return make_float3(wrap_component(a.x, b.x, __fsub_rn(a.x, b.x), L),
+                       wrap_component(a.y, b.y, __fsub_rn(a.y, b.y), L),
+                       wrap_component(a.z, b.z, __fsub_rn(a.z, b.z), L));
+}
+
+template <bool PERIODIC>
+__device__ __noinline__ bool exact_inside_g(float4 a, float4 b, const LawParams* __restrict__ P)
+{
+    return exact_inside<PERIODIC>(a, b, *P);
+}
+
+__device__ __forceinline__ float rcp_approx(float x)
+{
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+__device__ __forceinline__ float rd_of(float dx, float dy, float dz)
+{
+    return fmaf(dx, dx, fmaf(dy, dy, __fmul_rn(dz, dz)));
+}
+
+// Two entries (b0, b1) of the row of node a, evaluated with packed FP32x2
+// arithmetic (each half rounds exactly as the scalar law in irr_law.cuh), and
+// accumulated into the lane's packed partials.  An unused slot passes b == a
+// and v1 == false: d = 0 and its scalar is replaced by 0.
+//
+// A component |d| > side/2 implies rd > (side/2)^2, so the wrap test is one
+// compare on rd; a pair that fails it is re-examined exactly (rare: only a
+// pair across the box wall or beyond half the box).
+template <bool PERIODIC>
+__device__ __forceinline__ void lj_pair(float4 a, float4 b0, float4 b1, bool v1, const HotLaw& H,
+                                        const LawParams* __restrict__ cold, float2& ax, float2& ay,
+                                        float2& az)
+{
+    float2 dx = __fadd2_rn(make_float2(a.x, a.x), make_float2(-b0.x, -b1.x));
+    float2 dy = __fadd2_rn(make_float2(a.y, a.y), make_float2(-b0.y, -b1.y));
+    float2 dz = __fadd2_rn(make_float2(a.z, a.z), make_float2(-b0.z, -b1.z));
+    float2 rd = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
+    if (PERIODIC && fmaxf(rd.x, rd.y) > H.half2) {
+        const LawParams* P = cold;
+        const float half = P->half;
+        if (fabsf(dx.x) > half || fabsf(dy.x) > half || fabsf(dz.x) > half) {
+            const float3 w = wrap_exact(a, b0, P);
+            dx.x = w.x;
+            dy.x = w.y;
+            dz.x = w.z;
+            rd.x = rd_of(w.x, w.y, w.z);
+        }
+        if (fabsf(dx.y) > half || fabsf(dy.y) > half || fabsf(dz.y) > half) {
+            const float3 w = wrap_exact(a, b1, P);
+            dx.y = w.x;
+            dy.y = w.y;
+            dz.y = w.z;
+            rd.y = rd_of(w.x, w.y, w.z);
+        }
     }
-    uint32_t parity = 0;
-    int it = blockIdx.x;
-    for (;;) {
-        if (queue) {
-            if (tid == 0) s_item = atomicAdd(queue, 1);
-            __syncthreads();
-            it = s_item;
-            __syncthreads();
-        }
-        if (it >= num_items) break;
-        const WorkItem w = items[it];
-        const float4* __restrict__ pos = insts[w.inst].pos;
-        const uint32_t* __restrict__ row_off = insts[w.inst].row_off;
-        const int32_t* __restrict__ col = insts[w.inst].col;
-        float4* __restrict__ force = insts[w.inst].force;
-        const LawParams law = insts[w.inst].law;
-        const int nr = w.nrows;
+    bool in0 = rd.x < H.rc2, in1 = rd.y < H.rc2;
+    const float2 t = __fadd2_rn(rd, make_float2(-H.rc2, -H.rc2));
+    if (fminf(fabsf(t.x), fabsf(t.y)) < H.band) {
+        if (fabsf(t.x) < H.band) in0 = exact_inside_g<PERIODIC>(a, b0, cold);
+        if (fabsf(t.y) < H.band) in1 = exact_inside_g<PERIODIC>(a, b1, cold);
+    }
+    float2 r = make_float2(rcp_approx(rd.x), rcp_approx(rd.y));
+    const float2 e = __ffma2_rn(make_float2(-rd.x, -rd.y), r, make_float2(1.0f, 1.0f));
+    r = __ffma2_rn(r, e, r);                                     // rd^-1 (one Newton step)
+    const float2 r2 = __fmul2_rn(r, r);                          // rd^-2
+    float2 s = __fmul2_rn(__fmul2_rn(r2, r2), __ffma2_rn(r2, r, make_float2(-0.5f, -0.5f)));
+    s.x = in0 ? s.x : 0.0f;
+    s.y = (in1 && v1) ? s.y : 0.0f;
+    ax = __ffma2_rn(dx, s, ax);
+    ay = __ffma2_rn(dy, s, ay);
+    az = __ffma2_rn(dz, s, az);
+}
 
-        bool use_smem = false;
-        if (STAGE && staged) {
-            if (tid == 0) bulk_load(spos, pos + w.row0, (uint32_t)nr * 16u, &bar);
-            const bool ok = mbar_wait_bounded(&bar, parity, kWaitPolls);
-            parity ^= 1u;
-            // Uniform decision: if any thread gave up, the CTA stops staging
-            // for good (a copy may still be in flight into spos).
-            if (__syncthreads_or(!ok)) {
-                if (tid == 0) atomicOr(status, kStatusWaitTimeout);
-                staged = false;
-            } else {
-                use_smem = true;
-            }
-        }
+// One row: G lanes; each lane takes entry pairs (k, k + G) with stride 2G.
+// Partials: two per lane (the packed halves), joined by TwoSum, then the G
+// lanes by a TwoSum butterfly.  Entry k of the row is cols[k - shift].
+template <bool PERIODIC, int G>
+__device__ __forceinline__ float3 row_sum(const float4* __restrict__ pos, const int32_t* cols,
+                                          uint32_t shift, float4 a, uint32_t beg, uint32_t end,
+                                          int lane, const HotLaw& H,
+                                          const LawParams* __restrict__ cold)
+{
+    float2 ax = make_float2(0.f, 0.f), ay = ax, az = ax;
+    for (uint32_t k = beg + lane; k < end; k += 2 * G) {
+        const bool v1 = k + G < end;
+        const float4 b0 = __ldg(pos + cols[k - shift]);
+        const float4 b1 = v1 ? __ldg(pos + cols[k + G - shift]) : a;
+        lj_pair<PERIODIC>(a, b0, b1, v1, H, cold, ax, ay, az);
+    }
+    float hx, hy, hz, cx, cy, cz;
+    two_sum(ax.x, ax.y, hx, cx);
+    two_sum(ay.x, ay.y, hy, cy);
+    two_sum(az.x, az.y, hz, cz);
+#pragma unroll
+    for (int off = G / 2; off > 0; off >>= 1) {
+        const float ox = __shfl_xor_sync(0xffffffffu, hx, off, G);
+        const float oy = __shfl_xor_sync(0xffffffffu, hy, off, G);
+        const float oz = __shfl_xor_sync(0xffffffffu, hz, off, G);
+        const float ocx = __shfl_xor_sync(0xffffffffu, cx, off, G);
+        const float ocy = __shfl_xor_sync(0xffffffffu, cy, off, G);
+        const float ocz = __shfl_xor_sync(0xffffffffu, cz, off, G);
+        float e;
+        two_sum(hx, ox, hx, e);
+        cx = __fadd_rn(__fadd_rn(cx, ocx), e);
+        two_sum(hy, oy, hy, e);
+        cy = __fadd_rn(__fadd_rn(cy, ocy), e);
+        two_sum(hz, oz, hz, e);
+        cz = __fadd_rn(__fadd_rn(cz, ocz), e);
+    }
+    return make_float3(__fadd_rn(hx, cx), __fadd_rn(hy, cy), __fadd_rn(hz, cz));
+}
 
-        const int rounds = (nr + kGroups - 1) / kGroups;
-        for (int q = 0; q < rounds; q++) {
-            const int rl = q * kGroups + gid;
-            const bool valid = rl < nr;
-            const int64_t r = (int64_t)w.row0 + rl;
-            float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
-            uint32_t beg = 0, end = 0;
-            if (valid) {
-                a = use_smem ? spos[rl] : __ldg(pos + r);
-                beg = __ldg(row_off + r);
-                end = __ldg(row_off + r + 1);
-            }
-            float ax = 0.f, ay = 0.f, az = 0.f;
-            for (uint32_t k = beg + lane; k < end; k += G * UNROLL) {
-                int32_t j[UNROLL];
-#pragma unroll
-                for (int u = 0; u < UNROLL; u++) {
-                    const uint32_t kk = k + u * G;
-                    j[u] = kk < end ? __ldcs(col + kk) : -1;
-                }
-                float4 b[UNROLL];
-#pragma unroll
-                for (int u = 0; u < UNROLL; u++) {
-                    if (j[u] >= 0) {
-                        const uint32_t jl = (uint32_t)(j[u] - w.row0);
-                        b[u] = (use_smem && jl < (uint32_t)nr) ? spos[jl] : __ldg(pos + j[u]);
-                    }
-                }
-#pragma unroll
-                for (int u = 0; u < UNROLL; u++) {
-                    if (j[u] >= 0) {
-                        float dx, dy, dz;
-                        const float s = lj_scalar<PERIODIC>(a, b[u], law, dx, dy, dz);
-                        ax = fmaf(dx, s, ax);
-                        ay = fmaf(dy, s, ay);
-                        az = fmaf(dz, s, az);
-                    }
-                }
-            }
-            // Combine the G lane partials: TwoSum keeps each rounding error,
-            // which is carried in (cx, cy, cz) and added back at the end.
-            float cx = 0.f, cy = 0.f, cz = 0.f;
-#pragma unroll
-            for (int off = G / 2; off > 0; off >>= 1) {
-                const float ox = __shfl_xor_sync(0xffffffffu, ax, off, G);
-                const float oy = __shfl_xor_sync(0xffffffffu, ay, off, G);
-                const float oz = __shfl_xor_sync(0xffffffffu, az, off, G);
-                const float ocx = __shfl_xor_sync(0xffffffffu, cx, off, G);
-                const float ocy = __shfl_xor_sync(0xffffffffu, cy, off, G);
-                const float ocz = __shfl_xor_sync(0xffffffffu, cz, off, G);
-                float e;
-                two_sum(ax, ox, ax, e);
-                cx = __fadd_rn(__fadd_rn(cx, ocx), e);
-                two_sum(ay, oy, ay, e);
-                cy = __fadd_rn(__fadd_rn(cy, ocy), e);
-                two_sum(az, oz, az, e);
-                cz = __fadd_rn(__fadd_rn(cz, ocz), e);
-            }
-            if (valid && lane == 0)
-                force[r] = make_float4(__fadd_rn(ax, cx), __fadd_rn(ay, cy), __fadd_rn(az, cz),
-                                       0.f);
+constexpr int kConsumerWarps = 8;
+constexpr int kPipeThreads = (kConsumerWarps + 1) * 32;
+
+// The rows of one work item that belong to consumer warp `cw`.
+template <bool PERIODIC, int G>
+__device__ __forceinline__ void consume_item(const WorkItem& w, const InstDesc* __restrict__ insts,
+                                             const int32_t* cols, uint32_t shift, int cw, int lane32)
+{
+    constexpr int kGroupsPerWarp = 32 / G;
+    constexpr int kGroups = kConsumerWarps * kGroupsPerWarp;
+    const int lane = lane32 % G;
+    const int gid = cw * kGroupsPerWarp + lane32 / G;
+    const InstDesc* __restrict__ I = insts + w.inst;
+    const float4* __restrict__ pos = I->pos;
+    const uint32_t* __restrict__ row_off = I->row_off;
+    float4* __restrict__ force = I->force;
+    const LawParams* __restrict__ cold = &I->law;
+    HotLaw H;
+    H.half2 = I->law.half2;
+    H.rc2 = I->law.rc2;
+    H.band = I->law.band;
+    const int rounds = (w.nrows + kGroups - 1) / kGroups;
+    for (int q = 0; q < rounds; q++) {
+        const int rl = q * kGroups + gid;
+        const bool valid = rl < w.nrows;
+        const int64_t r = (int64_t)w.row0 + rl;
+        float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
+        uint32_t beg = 0, end = 0;
+        if (valid) {
+            a = __ldg(pos + r);
+            beg = __ldg(row_off + r);
+            end = __ldg(row_off + r + 1);
         }
-        if (!queue) break;
-        __syncthreads();  // every thread is done with spos before it is refilled
+        const float3 f = row_sum<PERIODIC, G>(pos, cols, shift, a, beg, end, lane, H, cold);
+        if (valid && lane == 0) force[r] = make_float4(f.x, f.y, f.z, 0.f);
     }
 }
 
-template <bool PERIODIC, int G, bool STAGE>
-cudaError_t launch_tiled_t(const TiledShape& shape, const InstDesc* d_insts,
-                           const WorkItem* d_items, int num_items, int* d_queue, int grid,
-                           int* d_status, cudaStream_t s)
+// Persistent owner-computes kernel, warp-specialised.  Warp kConsumerWarps is
+// the producer: its lane 0 claims work items from *queue in order, and for
+// each one waits until its ring stage is empty, publishes the item id and
+// either bulk-copies the item's entry segment (widened to 16-byte bounds)
+// into the stage -- the stage's `full` mbarrier completes on the byte count --
+// or, for items read from global memory, just arrives.  The consumer warps
+// walk the ring independently: wait `full`, sum their share of the item's
+// rows, arrive on `empty` (kConsumerWarps arrivals free the stage).  Every
+// wait is bounded; a wait that gives up sets kStatusWaitTimeout, waits once
+// more (bounded) for a copy that may be in flight, and leaves.
+template <bool PERIODIC, int G>
+__global__ void __launch_bounds__(kPipeThreads, kCtasPerSm) tiled_kernel(
+    const InstDesc* __restrict__ insts, const WorkItem* __restrict__ items, int num_items,
+    int* queue, int* status, int use_stages)
 {
-    constexpr int kUnroll = 2;
-    auto kern = tiled_kernel<PERIODIC, G, STAGE, kUnroll>;
-    const size_t smem = STAGE ? (size_t)shape.block_nodes * sizeof(float4) : 0;
-    if (STAGE && smem > 48 * 1024)
-        IRR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)smem));
-    const int blocks = d_queue ? grid : num_items;
-    if (blocks <= 0) return cudaSuccess;
-    kern<<<blocks, kTiledThreads, smem, s>>>(d_insts, d_items, num_items, d_queue, d_status);
-    return cudaGetLastError();
+    extern __shared__ int4 smem_raw[];
+    int32_t* stage_base = reinterpret_cast<int32_t*>(smem_raw);
+    constexpr int kStageInts = kStageEntries + kColPad;
+    __shared__ uint64_t full[kStages];
+    __shared__ uint64_t empty[kStages];
+    __shared__ int s_item[kStages];
+    __shared__ int s_smem[kStages];
+    const int warp = threadIdx.x / 32;
+    const int lane = threadIdx.x % 32;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kStages; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], kConsumerWarps);
+        }
+    }
+    __syncthreads();
+
+    if (warp == kConsumerWarps) {
+        if (lane != 0) return;
+        for (int k = 0;; k++) {
+            const int s = k % kStages;
+            const int use = k / kStages;
+            if (use > 0 && !mbar_wait_bounded(&empty[s], (uint32_t)(use - 1) & 1u, kWaitPolls)) {
+                atomicOr(status, kStatusWaitTimeout);
+                return;  // nothing of this stage is in flight: its last copy was consumed
+            }
+            const int it = atomicAdd(queue, 1);
+            s_item[s] = it;
+            bool issue = false;
+            if (it < num_items && use_stages) {
+                const WorkItem w = items[it];
+                issue = !(w.flags & kItemDirect);
+                if (issue) {
+                    s_smem[s] = 1;
+                    const uint32_t a0 = w.ent0 & ~3u;
+                    const uint32_t words = ((w.ent0 + w.nent - a0) + 3u) & ~3u;
+                    bulk_load(stage_base + s * kStageInts, insts[w.inst].col + a0, words * 4u,
+                              &full[s]);
+                }
+            }
+            if (!issue) {
+                s_smem[s] = 0;
+                mbar_arrive(&full[s]);
+            }
+            if (it >= num_items) return;
+        }
+    }
+
+    for (int k = 0;; k++) {
+        const int s = k % kStages;
+        if (!mbar_wait_bounded(&full[s], (uint32_t)(k / kStages) & 1u, kWaitPolls)) {
+            if (lane == 0) atomicOr(status, kStatusWaitTimeout);
+            mbar_wait_bounded(&full[s], (uint32_t)(k / kStages) & 1u, kWaitPolls);
+            return;
+        }
+        const int it = s_item[s];
+        if (it >= num_items) return;
+        const WorkItem w = items[it];
+        if (s_smem[s])
+            consume_item<PERIODIC, G>(w, insts, stage_base + s * kStageInts, w.ent0 & ~3u, warp, lane);
+        else
+            consume_item<PERIODIC, G>(w, insts, insts[w.inst].col, 0u, warp, lane);
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[s]);
+    }
 }
 
 template <bool PERIODIC, int G>
-cudaError_t launch_tiled_g(const TiledShape& sh, const InstDesc* a, const WorkItem* b, int n,
-                           int* q, int grid, int* st, cudaStream_t s)
+cudaError_t launch_tiled_g(const TiledShape& shape, const InstDesc* d_insts,
+                           const WorkItem* d_items, int num_items, int* d_queue, int grid,
+                           int* d_status, cudaStream_t s)
 {
-    return sh.stage_smem ? launch_tiled_t<PERIODIC, G, true>(sh, a, b, n, q, grid, st, s)
-                         : launch_tiled_t<PERIODIC, G, false>(sh, a, b, n, q, grid, st, s);
+    auto kern = tiled_kernel<PERIODIC, G>;
+    const size_t smem =
+        shape.stage_smem ? (size_t)kStages * (kStageEntries + kColPad) * sizeof(int32_t) : 0;
+    if (smem > 48 * 1024)
+        IRR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)smem));
+    if (grid <= 0 || num_items <= 0) return cudaSuccess;
+    kern<<<grid, kPipeThreads, smem, s>>>(d_insts, d_items, num_items, d_queue, d_status,
+                                          shape.stage_smem);
+    return cudaGetLastError();
 }
 
 template <bool PERIODIC>
@@ -237,6 +368,8 @@ cudaError_t launch_tiled_p(const TiledShape& sh, const InstDesc* a, const WorkIt
                            int* q, int grid, int* st, cudaStream_t s)
 {
     switch (sh.lanes_per_row) {
+    case 1: return launch_tiled_g<PERIODIC, 1>(sh, a, b, n, q, grid, st, s);
+    case 2: return launch_tiled_g<PERIODIC, 2>(sh, a, b, n, q, grid, st, s);
     case 4: return launch_tiled_g<PERIODIC, 4>(sh, a, b, n, q, grid, st, s);
     case 8: return launch_tiled_g<PERIODIC, 8>(sh, a, b, n, q, grid, st, s);
     case 16: return launch_tiled_g<PERIODIC, 16>(sh, a, b, n, q, grid, st, s);
@@ -267,11 +400,34 @@ cudaError_t launch_tiled(const TiledShape& shape, const InstDesc* d_insts,
                          const WorkItem* d_items, int num_items, int* d_queue, int grid,
                          int* d_status, cudaStream_t s)
 {
-    if (shape.stage_smem && (shape.block_nodes > kMaxStageNodes || shape.block_nodes < 1))
-        return cudaErrorInvalidValue;
+    if (!d_queue) return cudaErrorInvalidValue;
     return shape.periodic
                ? launch_tiled_p<true>(shape, d_insts, d_items, num_items, d_queue, grid, d_status, s)
                : launch_tiled_p<false>(shape, d_insts, d_items, num_items, d_queue, grid, d_status, s);
+}
+
+void make_work_items(const uint32_t* row_off, int64_t n, int inst, int max_rows, int staged,
+                     std::vector<WorkItem>& out)
+{
+    int64_t r = 0;
+    while (r < n) {
+        WorkItem w{};
+        w.inst = inst;
+        w.row0 = (int32_t)r;
+        w.ent0 = row_off[r];
+        int64_t q = r + 1;
+        if ((int64_t)(row_off[q] - row_off[r]) > kStageEntries) {
+            w.flags = kItemDirect;  // one long row: read from global memory
+        } else {
+            while (q < n && q - r < max_rows && (int64_t)(row_off[q + 1] - row_off[r]) <= kStageEntries)
+                q++;
+        }
+        w.nrows = (int32_t)(q - r);
+        w.nent = row_off[q] - row_off[r];
+        if (!staged || w.nent == 0) w.flags |= kItemDirect;
+        out.push_back(w);
+        r = q;
+    }
 }
 
 }  // namespace irr

@@ -80,6 +80,9 @@ _SIGS = {
     "irr_sync": (C.c_int, [P]),
     "irr_get_info": (C.c_int, [P, C.POINTER(Info)]),
     "irr_get_partition": (C.c_int, [P, P, P, P]),
+    "irr_neighbor_build": (C.c_int, [C.c_int, P, P, C.c_int, C.c_int, I64, C.c_float, C.c_float,
+                                     C.POINTER(P), C.POINTER(I64)]),
+    "irr_device_free": (C.c_int, [C.c_int, P]),
 }
 
 _lib = None
@@ -136,6 +139,82 @@ def minimd_params(cutforcesq: float, side: Optional[float] = None) -> np.ndarray
     return np.array([cutforcesq, side], np.float64)
 
 
+class DeviceEdges:
+    """A device edge array owned by the library (freed on close)."""
+
+    def __init__(self, device: int, ptr: int, count: int):
+        self.device = device
+        self.ptr = ptr
+        self.count = count
+
+    def to_host(self, count: Optional[int] = None) -> np.ndarray:
+        """Copies the first `count` pairs (all by default) to a host array."""
+        import ctypes
+        cnt = self.count if count is None else max(0, min(int(count), self.count))
+        out = np.empty((cnt, 2), np.int32)
+        if cnt:
+            cudart = _cudart()
+            rc = cudart.cudaMemcpy(out.ctypes.data_as(ctypes.c_void_p), ctypes.c_void_p(self.ptr),
+                                   ctypes.c_size_t(out.nbytes), 2)
+            if rc != 0:
+                raise IrregularError(IRR_ERR_CUDA, f"cudaMemcpy failed ({rc})")
+        return out
+
+    def close(self):
+        if self.ptr:
+            load().irr_device_free(self.device, C.c_void_p(self.ptr))
+            self.ptr = 0
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_cudart_lib = None
+
+
+def _cudart():
+    global _cudart_lib
+    if _cudart_lib is None:
+        import ctypes.util
+        for name in ("libcudart.so", "libcudart.so.13", ctypes.util.find_library("cudart")):
+            if not name:
+                continue
+            try:
+                _cudart_lib = C.CDLL(name)
+                break
+            except OSError:
+                continue
+        if _cudart_lib is None:
+            raise ImportError("libcudart not found")
+    return _cudart_lib
+
+
+def neighbor_build(pos, box: float, list_cut2: float, device: int = 0, stream: int = 0,
+                   elm_size: Optional[int] = None) -> DeviceEdges:
+    """GPU half neighbour list (irr_neighbor_build); pos is a host array or a
+    torch CUDA tensor of xyz records."""
+    L = load()
+    d_edges = C.c_void_p()
+    cnt = C.c_int64()
+    if hasattr(pos, "data_ptr"):
+        elm = elm_size or pos.element_size() * pos.shape[-1]
+        n = pos.numel() * pos.element_size() // elm
+        rc = L.irr_neighbor_build(device, C.c_void_p(stream), _ptr(pos), elm, 1, n,
+                                  float(box), float(list_cut2), C.byref(d_edges), C.byref(cnt))
+    else:
+        a = np.ascontiguousarray(pos)
+        elm = elm_size or a.dtype.itemsize * a.shape[-1]
+        n = a.nbytes // elm
+        rc = L.irr_neighbor_build(device, C.c_void_p(stream), _ptr(a), elm, 0, n, float(box),
+                                  float(list_cut2), C.byref(d_edges), C.byref(cnt))
+    if rc != IRR_OK:
+        raise IrregularError(rc, f"irr_neighbor_build: {L.irr_status_string(rc).decode()}")
+    return DeviceEdges(device, d_edges.value or 0, cnt.value)
+
+
 class Handle:
     """Owning wrapper of one irr_handle."""
 
@@ -180,7 +259,15 @@ class Handle:
         blob = np.ascontiguousarray(blob)
         self._check(load().irr_set_params(self._h, _ptr(blob), blob.nbytes), "irr_set_params")
 
+    def set_edges_device(self, d_ptr: int, num_edges: int):
+        """Edges already in device memory (2 * num_edges int32 at d_ptr)."""
+        self._check(load().irr_set_edges_device(self._h, C.c_void_p(d_ptr), int(num_edges)),
+                    "irr_set_edges_device")
+
     def set_edges(self, edges):
+        if isinstance(edges, DeviceEdges):
+            self.set_edges_device(edges.ptr, edges.count)
+            return
         if hasattr(edges, "data_ptr"):
             self._check(load().irr_set_edges_device(self._h, _ptr(edges), edges.numel() // 2),
                         "irr_set_edges_device")

@@ -253,11 +253,43 @@ static double now_seconds(void)
     return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
 }
 
+typedef struct {
+    orc_table *t;
+    int64_t nb;
+} clear_arg;
+
+static void *clear_worker(void *argp)
+{
+    clear_arg *a = (clear_arg *)argp;
+    table_clear(a->t, a->nb);
+    return NULL;
+}
+
+/* Re-initialises every worker's table in parallel, one thread per table, as
+ * re_init does (moldyn/irregular/irregular_runtime.cu:474-490). */
+static void clear_tables(orc_exec *x)
+{
+    pthread_t *tids = (pthread_t *)malloc(sizeof(pthread_t) * (size_t)x->threads);
+    clear_arg *args = (clear_arg *)malloc(sizeof(clear_arg) * (size_t)x->threads);
+    if (!tids || !args) {
+        for (int t = 0; t < x->threads; t++) table_clear(&x->tab[t], x->nb);
+    } else {
+        for (int t = 0; t < x->threads; t++) {
+            args[t].t = &x->tab[t];
+            args[t].nb = x->nb;
+            pthread_create(&tids[t], NULL, clear_worker, &args[t]);
+        }
+        for (int t = 0; t < x->threads; t++) pthread_join(tids[t], NULL);
+    }
+    free(tids);
+    free(args);
+}
+
 static double exec_run_dpos(orc_exec *x, const double *pos, int64_t e, const int32_t *edges,
                             const orc_lj_param *p, int64_t chunk, float *f_out)
 {
     if (!x || chunk < 1) return -1.0;
-    for (int t = 0; t < x->threads; t++) table_clear(&x->tab[t], x->nb);
+    clear_tables(x);
     pthread_t *tids = (pthread_t *)malloc(sizeof(pthread_t) * (size_t)x->threads);
     worker_arg *args = (worker_arg *)malloc(sizeof(worker_arg) * (size_t)x->threads);
     if (!tids || !args) {
@@ -357,7 +389,15 @@ static int cmp_i32(const void *a, const void *b)
 int64_t orc_neighbor_half_list(int64_t n, const float *pos, float box, float list_cut2,
                                int32_t *out, int64_t cap)
 {
+    return orc_neighbor_half_list_rows(n, pos, box, list_cut2, 0, n, out, cap);
+}
+
+int64_t orc_neighbor_half_list_rows(int64_t n, const float *pos, float box, float list_cut2,
+                                    int64_t row_begin, int64_t row_end, int32_t *out, int64_t cap)
+{
     if (n < 0 || list_cut2 < 0.0f || box < 0.0f) return -1;
+    if (row_begin < 0) row_begin = 0;
+    if (row_end > n) row_end = n;
     if (n == 0) return 0;
     float hb = 0.5f * box;
     float lo[3], hi[3];
@@ -419,7 +459,7 @@ int64_t orc_neighbor_half_list(int64_t n, const float *pos, float box, float lis
         free(fill);
     }
     int64_t count = 0;
-    for (int64_t i = 0; i < n; i++) {
+    for (int64_t i = row_begin; i < row_end; i++) {
         int64_t c0 = cell_of[i];
         int64_t cx = c0 % nc[0], cy = (c0 / nc[0]) % nc[1], cz = c0 / ((int64_t)nc[0] * nc[1]);
         int64_t m = 0;

@@ -91,6 +91,11 @@ void orc_exec_destroy(orc_exec *x);
 int64_t orc_neighbor_half_list(int64_t n, const float *pos, float box, float list_cut2,
                                int32_t *out, int64_t cap);
 
+/* The same list restricted to rows i in [row_begin, row_end) (pairs i < j,
+ * j anywhere): a bounded sample of a large list for the timed CPU baseline. */
+int64_t orc_neighbor_half_list_rows(int64_t n, const float *pos, float box, float list_cut2,
+                                    int64_t row_begin, int64_t row_end, int32_t *out, int64_t cap);
+
 /* FCC lattice of moldyn's InitCoordinates (moldyn/moldyn.cu:596-626):
  * 4*m^3 points, spacing side/m.  pos: 3*4*m^3 doubles. */
 void orc_fcc_moldyn(int m, double side, double *pos);

@@ -56,6 +56,8 @@ def lib():
         L.orc_exec_destroy.argtypes = [P]
         L.orc_neighbor_half_list.argtypes = [i64, P, C.c_float, C.c_float, P, i64]
         L.orc_neighbor_half_list.restype = i64
+        L.orc_neighbor_half_list_rows.argtypes = [i64, P, C.c_float, C.c_float, i64, i64, P, i64]
+        L.orc_neighbor_half_list_rows.restype = i64
         L.orc_fcc_moldyn.argtypes = [C.c_int, C.c_double, P]
         L.orc_fcc_minimd.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, P, i64]
         L.orc_fcc_minimd.restype = i64
@@ -161,6 +163,23 @@ def neighbor_half_list(pos32, box: float, list_cut2: float) -> np.ndarray:
     out = np.zeros((max(cnt, 0), 2), np.int32)
     if cnt:
         L.orc_neighbor_half_list(n, _p(pos32), float(box), float(list_cut2), _p(out), cnt)
+    return out
+
+
+def neighbor_half_list_rows(pos32, box: float, list_cut2: float, row_begin: int,
+                            row_end: int) -> np.ndarray:
+    """Rows [row_begin, row_end) of the half list: a bounded sample of a large list."""
+    pos32 = np.ascontiguousarray(pos32, np.float32).reshape(-1, 3)
+    n = pos32.shape[0]
+    L = lib()
+    cnt = L.orc_neighbor_half_list_rows(n, _p(pos32), float(box), float(list_cut2), row_begin,
+                                        row_end, None, 0)
+    if cnt < 0:
+        raise ValueError("bad neighbour-list arguments")
+    out = np.zeros((max(cnt, 0), 2), np.int32)
+    if cnt:
+        L.orc_neighbor_half_list_rows(n, _p(pos32), float(box), float(list_cut2), row_begin,
+                                      row_end, _p(out), cnt)
     return out
 
 

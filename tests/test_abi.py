@@ -55,7 +55,7 @@ def test_status_strings_and_defaults(built_lib):
 
 def test_create_rejects_bad_config_without_crashing(built_lib):
     import irregular_gb300 as irr
-    for bad in (dict(exec=7), dict(map_idx=9), dict(block_nodes=100), dict(lanes_per_row=3)):
+    for bad in (dict(exec=7), dict(map_idx=9), dict(block_nodes=100), dict(lanes_per_row=3), dict(lanes_per_row=64)):
         with pytest.raises(irr.IrregularError) as ei:
             irr.Handle(irr.default_config(**bad))
         assert ei.value.status in (irr.IRR_ERR_ARG, irr.IRR_ERR_CUDA)

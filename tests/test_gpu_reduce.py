@@ -18,11 +18,13 @@ pytestmark = pytest.mark.gpu
 SHAPES = {
     "plain": dict(exec=0),
     "part": dict(exec=1),
+    "part_g1": dict(exec=1, lanes_per_row=1),
+    "part_g2": dict(exec=1, lanes_per_row=2),
     "part_g4": dict(exec=1, lanes_per_row=4),
     "part_g16": dict(exec=1, lanes_per_row=16),
     "part_g32": dict(exec=1, lanes_per_row=32),
-    "part_smem": dict(exec=1, stage_smem=1),
-    "part_smem_b2048": dict(exec=1, stage_smem=1, block_nodes=2048),
+    "part_direct": dict(exec=1, stage_smem=0),
+    "part_b2048": dict(exec=1, block_nodes=2048),
     "part_b64": dict(exec=1, block_nodes=64),
     "part_noreorder": dict(exec=1, reorder=0),
 }
@@ -75,7 +77,7 @@ def test_partition_bit_exact(built_lib, oracle_lib, name, reorder):
     assert np.array_equal(col, ocol)
 
 
-@pytest.mark.parametrize("shape", ["part", "part_smem", "part_g32"])
+@pytest.mark.parametrize("shape", ["part", "part_direct", "part_g32", "part_g1"])
 def test_partitioned_is_bitwise_reproducible(built_lib, shape):
     import irregular_gb300 as irr
     c = load_golden("moldyn_random_2048")
