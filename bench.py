@@ -166,16 +166,22 @@ def barrier(world: int):
         dist.barrier()
 
 
+# Edges per mutex grab of the CPU executor: CPU_BLOCK_SIZE of the reference's
+# miniMD copy (miniMD/irregular/parameters.h:7); the moldyn copy's 1,000,000
+# would leave most cores idle on a bounded sample of a few million edges.
+CPU_CHUNK = 100000
+
+
 def cpu_port_rate(pos, edges_sample, side, seconds: float, threads: int):
     """Times the ported reference executor (oracle/) over a bounded edge sample."""
     from oracle import oracle as O
 
     p = O.lj_param(CUTOFF * CUTOFF, float(side), True)
     ex = O.Executor(pos.shape[0], threads)
-    ex.run(pos, edges_sample, p)  # warm-up pass (untimed)
+    ex.run(pos, edges_sample, p, chunk=CPU_CHUNK)  # warm-up pass (untimed)
     total, passes = 0.0, 0
     while total < seconds or passes < 1:
-        total += ex.run(pos, edges_sample, p)
+        total += ex.run(pos, edges_sample, p, chunk=CPU_CHUNK)
         passes += 1
     ex.close()
     return edges_sample.shape[0] * passes / total, passes
@@ -194,14 +200,15 @@ def run_reference(args, rank, world):
     p = O.lj_param(CUTOFF * CUTOFF, float(side), True)
     ex = O.Executor(pos.shape[0], threads)
     for _ in range(args.warmup):
-        ex.run(pos, sample, p)
+        ex.run(pos, sample, p, chunk=CPU_CHUNK)
     total = 0.0
     for _ in range(args.steps):
-        total += ex.run(pos, sample, p)
+        total += ex.run(pos, sample, p, chunk=CPU_CHUNK)
     ex.close()
     rate = sample.shape[0] * args.steps / total
     desc = (f"edges of rows [0, {rows}) of the workload's half list ({sample.shape[0]} edges) "
-            f"per step, {threads} threads, table re-initialisation excluded")
+            f"per step, {threads} threads, {CPU_CHUNK}-edge chunks, table re-initialisation "
+            f"excluded")
     line = {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": "edges/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -313,11 +320,12 @@ def run_ours(args, rank, world, local):
     cpu = None
     if rank == 0 and world == 1:
         threads = os.cpu_count() or 1
-        sample = edges.to_host(count=min(E, 4 * 1024 * 1024))
+        sample = edges.to_host(count=min(E, 8 * 1024 * 1024))
         rate, passes = cpu_port_rate(pos, sample, side, args.cpu_seconds, threads)
         cpu = {"value": rate, "unit": "edges/s", "cores": threads, "kind": "port",
                "sample": f"first {sample.shape[0]} edges of the workload's half list, "
-                         f"{passes} timed passes, table re-initialisation excluded"}
+                         f"{passes} timed passes, {CPU_CHUNK}-edge chunks, table "
+                         f"re-initialisation excluded"}
     edges.close()
 
     line = {
