@@ -56,7 +56,12 @@ WORKLOAD = ("moldyn-style LJ irregular reduction: 4,194,304 nodes, float32 posit
 METRIC = "edges/s"
 
 
-def positions(n: int = N_NODES, seed: int = SEED):
+def workload_name(n: int) -> str:
+    return WORKLOAD if n == N_NODES else WORKLOAD.replace("4,194,304", f"{n:,}") + \
+        " (reduced size)"
+
+
+def positions(n: int, seed: int = SEED):
     rng = np.random.Generator(np.random.PCG64(seed))
     side = np.float32((n / DENSITY) ** (1.0 / 3.0))
     pos = (rng.random((n, 3), dtype=np.float32) * side).astype(np.float32)
@@ -194,7 +199,7 @@ def run_reference(args, rank, world):
     from oracle import oracle as O
 
     threads = os.cpu_count() or 1
-    pos, side = positions()
+    pos, side = positions(args.nodes)
     rows = 131072  # rows [0, 131072) of the half list: ~4.2M edges per step
     sample = O.neighbor_half_list_rows(pos, float(side), np.float32(CUTOFF * CUTOFF), 0, rows)
     p = O.lj_param(CUTOFF * CUTOFF, float(side), True)
@@ -214,7 +219,8 @@ def run_reference(args, rank, world):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64 per edge, f32 accumulate", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "nodes": N_NODES, "edges_per_step": int(sample.shape[0]),
+        "config": {"workload": workload_name(args.nodes), "nodes": args.nodes,
+                   "edges_per_step": int(sample.shape[0]),
                    "executor": "reference CPU executor (port of compute_cpu + Cobject)"},
         "cpu_baseline": {"value": rate, "unit": "edges/s", "cores": threads, "kind": "port",
                          "sample": desc},
@@ -244,7 +250,7 @@ def run_ours(args, rank, world, local):
     torch.cuda.set_device(local)
     dev = local
     stream = torch.cuda.Stream(device=dev)
-    pos, side = positions()
+    pos, side = positions(args.nodes)
     n = pos.shape[0]
     edges = irr.neighbor_build(pos, float(side), CUTOFF * CUTOFF, device=dev,
                                stream=stream.cuda_stream)
@@ -274,6 +280,14 @@ def run_ours(args, rank, world, local):
     ms = max_over_ranks(ms, world)
     step_s = ms / 1e3 / args.steps
     value = E * args.steps * world / (ms / 1e3)
+    if args.legs == "value":
+        h.close()
+        edges.close()
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": "edges/s",
+                              "legs": "value only", "nodes": n, "edges": E,
+                              "ms_per_step": ms / args.steps}), flush=True)
+        return 0
 
     # e2e through the public API with host buffers (pinned)
     pin_in = torch.empty((n, 3), dtype=torch.float32, pin_memory=True)
@@ -311,7 +325,7 @@ def run_ours(args, rank, world, local):
     alg_bytes = 8.0 * E + 24.0 * n
     achieved = alg_bytes / step_s / 1e9
     peak, peak_kind = measured_hbm_peak()
-    traffic = ncu_traffic("tiled_kernel_moldyn_4M")
+    traffic = ncu_traffic("tiled_kernel_moldyn_4M") if n == N_NODES else None
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic,
                 "peak_source": f"{peak_kind} (hbm_gbs, MEASURED_PEAKS.json)",
@@ -333,7 +347,7 @@ def run_ours(args, rank, world, local):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded uniform-random positions; edge list built on the GPU)",
-        "config": {"workload": WORKLOAD, "nodes": n, "edges": E,
+        "config": {"workload": workload_name(n), "nodes": n, "edges": E,
                    "exec": "partitioned (Morton blocks, owner-computes tiled kernel)",
                    "lanes_per_row": info.lanes_per_row, "stage_smem": info.stage_smem,
                    "l2": "inputs larger than L2 (1.07 GB entry stream read every step)",
@@ -360,6 +374,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--nodes", type=int, default=N_NODES,
+                    help="workload size (default: the full 4,194,304-node workload; "
+                         "smaller sizes are for profiling captures)")
+    ap.add_argument("--legs", choices=["all", "value"], default="all",
+                    help="'value': only the device-resident timed leg (profiling)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
