@@ -211,6 +211,26 @@ IRR_API int irr_neighbor_build(int device, void *stream, const void *pos, int po
 /* Frees device memory this library allocated for the caller. */
 IRR_API int irr_device_free(int device, void *d_ptr);
 
+/* ------------------------------------------------ allocation-free ordering
+ * No counterpart in the reference.  The partitioner's Morton node ordering
+ * (perm[new] = old node id, bit for bit the perm that irr_get_partition
+ * returns for reorder = 1) for callers that cannot allocate device memory --
+ * an application that has already reserved the GPU's memory for its own
+ * pool, or a latency-bound loop where cudaMalloc/cudaFree (which may
+ * synchronise the device) are not acceptable.  It calls no allocator: its
+ * scratch is a fixed device array inside this library, held by every GPU
+ * that loads the library until the process exits.
+ *   d_pos: n device records of pos_elm bytes (12: float xyz, 16: float xyzw);
+ *   d_perm: n int32 of device output;  n <= IRR_MORTON_STATIC_MAX_NODES, else
+ *   IRR_ERR_CAPACITY.
+ * The first call on a device looks up the array's device address (make that
+ * call before any stream capture).  Every call shares the one array: calls
+ * that overlap on the GPU race, so order them (one stream, or events).
+ * Enqueued on `stream`; the host does not wait. */
+#define IRR_MORTON_STATIC_MAX_NODES 1048576
+IRR_API int irr_morton_order_static(int device, void *stream, const void *d_pos, int pos_elm,
+                                    int64_t n, int32_t *d_perm);
+
 #ifdef __cplusplus
 }
 #endif

@@ -106,6 +106,19 @@ cudaError_t radix_sort_pairs(uint32_t* keys, int32_t* vals, uint32_t* keys_tmp,
 cudaError_t scan_exclusive_u32(const uint32_t* in, uint32_t* out, int64_t n, uint32_t* d_total,
                                cudaStream_t s);
 
+// Scan and radix-sort building blocks (irr_partition.cu).
+constexpr int kScanThreads = 256;
+constexpr int kScanBlock = kScanThreads * 4;
+constexpr int kSortThreads = 256;
+constexpr int kSortTile = kSortThreads * 16;
+__global__ void scan_blocks_kernel(const uint32_t* in, uint32_t* out, int64_t n, uint32_t* block_sums);
+__global__ void add_offsets_kernel(uint32_t* out, int64_t n, const uint32_t* block_off);
+__global__ void radix_hist_kernel(const uint32_t* keys, int64_t n, int shift, uint32_t* hist,
+                                  int64_t ntiles);
+__global__ void radix_scatter_kernel(const uint32_t* kin, const int32_t* vin, uint32_t* kout,
+                                     int32_t* vout, int64_t n, int shift, const uint32_t* offs,
+                                     int64_t ntiles);
+
 // Morton key of one position in a frame (shared with the oracle bit for bit).
 __host__ __device__ __forceinline__ uint32_t spread3(uint32_t v)
 {

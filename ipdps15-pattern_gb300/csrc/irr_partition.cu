@@ -19,9 +19,8 @@
 #include "irr_internal.cuh"
 
 namespace irr {
-namespace {
 
-__device__ __forceinline__ uint32_t lanemask_lt()
+static __device__ __forceinline__ uint32_t lanemask_lt()
 {
     uint32_t m;
     asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
@@ -29,9 +28,7 @@ __device__ __forceinline__ uint32_t lanemask_lt()
 }
 
 // ------------------------------------------------------------------ scan
-constexpr int kScanThreads = 256;
-constexpr int kScanItems = 4;
-constexpr int kScanBlock = kScanThreads * kScanItems;
+constexpr int kScanItems = kScanBlock / kScanThreads;
 
 __global__ void __launch_bounds__(kScanThreads) scan_blocks_kernel(const uint32_t* in,
                                                                    uint32_t* out, int64_t n,
@@ -82,12 +79,10 @@ __global__ void add_offsets_kernel(uint32_t* out, int64_t n, const uint32_t* blo
         if (base + k < n) out[base + k] += add;
 }
 
-__global__ void copy_u32_kernel(const uint32_t* src, uint32_t* dst) { *dst = *src; }
+static __global__ void copy_u32_kernel(const uint32_t* src, uint32_t* dst) { *dst = *src; }
 
 // ------------------------------------------------------------ radix sort
-constexpr int kSortThreads = 256;
-constexpr int kSortRounds = 16;
-constexpr int kSortTile = kSortThreads * kSortRounds;  // items per tile, in order
+constexpr int kSortRounds = kSortTile / kSortThreads;  // a tile's items, in order
 constexpr int kSortWarps = kSortThreads / 32;
 
 __global__ void __launch_bounds__(kSortThreads) radix_hist_kernel(const uint32_t* keys, int64_t n,
@@ -155,6 +150,8 @@ __global__ void __launch_bounds__(kSortThreads) radix_scatter_kernel(
         __syncthreads();
     }
 }
+
+namespace {
 
 // --------------------------------------------------------------- bbox
 __global__ void bbox_partial_kernel(const float4* pos, int64_t n, float* part)

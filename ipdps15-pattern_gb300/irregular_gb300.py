@@ -83,6 +83,7 @@ _SIGS = {
     "irr_neighbor_build": (C.c_int, [C.c_int, P, P, C.c_int, C.c_int, I64, C.c_float, C.c_float,
                                      C.POINTER(P), C.POINTER(I64)]),
     "irr_device_free": (C.c_int, [C.c_int, P]),
+    "irr_morton_order_static": (C.c_int, [C.c_int, P, P, C.c_int, I64, P]),
 }
 
 _lib = None
