@@ -211,6 +211,54 @@ IRR_API int irr_neighbor_build(int device, void *stream, const void *pos, int po
 /* Frees device memory this library allocated for the caller. */
 IRR_API int irr_device_free(int device, void *d_ptr);
 
+/* ------------------------------------------------- molecular dynamics
+ * A Lennard-Jones MD loop around the reduction, all on the GPU: the drivers'
+ * step loops (moldyn/moldyn.cu:331-407; miniMD/ljs.cu:171-176) with the
+ * velocity-Verlet integrator the reference leaves commented out
+ * (miniMD/ljs.cu:39).  Periodic cube of side `side`, mass 1, LJ at
+ * eps = sigma = 1 (force = 48 x the reduction's d (r^-14 - r^-8/2)) cut at
+ * `cutforce`; the neighbour list is rebuilt on the GPU at cutforce + skin
+ * every `rebuild_every` steps, and the nodes are re-partitioned each time.
+ * Positions, velocities, the integration and the energy/virial sums are
+ * FP64; per-edge forces are FP32 (the reduction). */
+typedef struct irr_md_config {
+    int device;
+    int rebuild_every; /* steps between neighbour-list rebuilds (miniMD: 20) */
+    double dt;         /* time step (0.005)                                 */
+    double cutforce;   /* force cutoff (2.5)                                */
+    double skin;       /* neighbour skin (0.3)                              */
+    double side;       /* periodic box side; > 2 (cutforce + skin)          */
+    int reserved[8];
+} irr_md_config;
+
+typedef struct irr_md_info {
+    int64_t num_atoms;
+    int64_t num_edges; /* pairs in the current list */
+    int64_t steps;
+    int64_t rebuilds;
+} irr_md_info;
+
+typedef struct irr_md irr_md;
+
+IRR_API void irr_md_config_default(irr_md_config *cfg);
+/* pos, vel: 3n doubles (host).  Builds the list and the first forces. */
+IRR_API int irr_md_create(const irr_md_config *cfg, const double *pos, const double *vel,
+                          int64_t n, irr_md **out);
+IRR_API int irr_md_destroy(irr_md *m);
+IRR_API const char *irr_md_last_error(const irr_md *m);
+IRR_API int irr_md_set_stream(irr_md *m, void *stream);
+/* Enqueues `steps` velocity-Verlet steps (rebuilds included). */
+IRR_API int irr_md_run(irr_md *m, int steps);
+/* Kinetic and potential energy (4(r^-12 - r^-6) over pairs inside the cutoff)
+ * and the virial sum of r.F, as FP64 sums; synchronises. */
+IRR_API int irr_md_energy(irr_md *m, double *kinetic, double *potential, double *virial);
+/* Positions and velocities (3n doubles each, caller's atom order; either may
+ * be NULL); synchronises. */
+IRR_API int irr_md_get_state(irr_md *m, double *pos, double *vel);
+/* Current forces (3n doubles, caller's atom order); synchronises. */
+IRR_API int irr_md_get_forces(irr_md *m, double *f);
+IRR_API int irr_md_get_info(const irr_md *m, irr_md_info *info);
+
 /* ------------------------------------------------ allocation-free ordering
  * No counterpart in the reference.  The partitioner's Morton node ordering
  * (perm[new] = old node id, bit for bit the perm that irr_get_partition

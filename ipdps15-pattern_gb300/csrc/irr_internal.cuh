@@ -47,11 +47,22 @@ struct TiledShape {
     int periodic;
 };
 
+// Shape of the owner-computes kernel; each can be set at build time
+// (-DIRR_STAGES=... etc.) to build and time variants.
+#ifndef IRR_STAGES
+#define IRR_STAGES 2
+#endif
+#ifndef IRR_STAGE_ENTRIES
+#define IRR_STAGE_ENTRIES 4096
+#endif
+#ifndef IRR_CTAS_PER_SM
+#define IRR_CTAS_PER_SM 4
+#endif
 constexpr int kTiledThreads = 256;
-constexpr int kStages = 4;             // shared-memory ring depth
-constexpr int kStageEntries = 4096;    // entries per stage (16 KB)
-constexpr int kColPad = 4;             // entries allocated past the end of col
-constexpr int kCtasPerSm = 3;        // resident CTAs per SM (registers and the ring)
+constexpr int kStages = IRR_STAGES;              // shared-memory ring depth
+constexpr int kStageEntries = IRR_STAGE_ENTRIES; // entries per stage (16 KB at 4096)
+constexpr int kColPad = 4;                       // entries allocated past the end of col
+constexpr int kCtasPerSm = IRR_CTAS_PER_SM;      // resident CTAs per SM (registers, ring)
 
 // Cuts rows [0, n) into work items of at most max_rows rows and (unless a
 // single row is longer) at most kStageEntries entries.  row_off: host copy.

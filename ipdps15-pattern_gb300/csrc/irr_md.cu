@@ -1,0 +1,535 @@
+// irr_md.cu -- Lennard-Jones molecular dynamics around the irregular reduction.
+//
+// The drivers' step loops (moldyn/moldyn.cu:331-407; miniMD/ljs.cu:171-176,
+// whose integrator is commented out at ljs.cu:39) move positions on the host
+// and call IrregularStart once per step.  Here the whole loop stays on the GPU:
+//   kick + drift   v += dt/2 * F/m, x += dt * v, x wrapped into [0, L)   (FP64)
+//   rebuild        every `rebuild_every` steps: GPU neighbour list at
+//                  cutforce + skin, GPU partition (Morton order), state
+//                  permuted into the new order
+//   force          the owner-computes reduction (FP32 per edge, compensated)
+//   kick           v += dt/2 * F/m                                       (FP64)
+// F = 48 * (the reduction's d * (r^-14 - r^-8/2)), the LJ force at eps = sigma
+// = 1, m = 1.  Energies and the virial are FP64 sums of FP32 per-edge terms.
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "irr_internal.cuh"
+#include "../../include/irregular_gb300.h"
+
+using namespace irr;
+
+struct irr_md {
+    irr_md_config cfg{};
+    int device = 0;
+    int sms = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    int64_t n = 0;
+    LawParams law{};
+    TiledShape shape{};
+    double* x = nullptr;       // [3n] positions, execution order
+    double* v = nullptr;       // [3n] velocities
+    double* tmp = nullptr;     // [3n] permutation scratch
+    float4* pos4 = nullptr;    // float copy of x for the reduction
+    float4* force = nullptr;   // reduction result (F / 48)
+    int32_t* ids = nullptr;    // execution slot -> caller's atom id
+    int32_t* ids_tmp = nullptr;
+    PartitionOut part{};
+    InstDesc* d_inst = nullptr;
+    WorkItem* d_items = nullptr;
+    int num_items = 0;
+    int* d_queue = nullptr;
+    int* d_status = nullptr;
+    double* d_acc = nullptr;   // [4] KE, PE, virial, spare
+    int64_t edges = 0;
+    int64_t steps = 0;
+    int64_t rebuilds = 0;
+    int64_t since_rebuild = 0;
+};
+
+namespace {
+
+int md_fail(irr_md* m, int code, const char* what, cudaError_t e = cudaSuccess)
+{
+    if (m) {
+        m->err = what;
+        if (e != cudaSuccess) {
+            m->err += ": ";
+            m->err += cudaGetErrorString(e);
+        }
+    }
+    cudaGetLastError();
+    return code;
+}
+
+#define MD_CUDA(m, expr, what)                                                            \
+    do {                                                                                  \
+        cudaError_t e_ = (expr);                                                          \
+        if (e_ != cudaSuccess)                                                            \
+            return md_fail((m), e_ == cudaErrorMemoryAllocation ? IRR_ERR_NOMEM : IRR_ERR_CUDA, \
+                           what, e_);                                                     \
+    } while (0)
+
+int grid_of(int64_t n)
+{
+    int64_t g = (n + 255) / 256;
+    return (int)(g < 1 ? 1 : (g > 8192 ? 8192 : g));
+}
+
+__device__ __forceinline__ double wrap_box(double x, double L)
+{
+    x -= L * floor(x / L);
+    if (x >= L) x -= L;  // x = -tiny rounds up to L
+    if (x < 0.0) x = 0.0;
+    return x;
+}
+
+__global__ void kick_drift_kernel(double* __restrict__ x, double* __restrict__ v,
+                                  const float4* __restrict__ f, int64_t n, double dt, double L,
+                                  float4* __restrict__ pos4)
+{
+    const double hk = 0.5 * dt * 48.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const float4 fi = f[i];
+        double* xi = x + 3 * i;
+        double* vi = v + 3 * i;
+        const double vx = vi[0] + hk * (double)fi.x;
+        const double vy = vi[1] + hk * (double)fi.y;
+        const double vz = vi[2] + hk * (double)fi.z;
+        const double px = wrap_box(xi[0] + dt * vx, L);
+        const double py = wrap_box(xi[1] + dt * vy, L);
+        const double pz = wrap_box(xi[2] + dt * vz, L);
+        vi[0] = vx;
+        vi[1] = vy;
+        vi[2] = vz;
+        xi[0] = px;
+        xi[1] = py;
+        xi[2] = pz;
+        // the float copy stays inside [0, L): a value that rounds up to L wraps to 0
+        float fx = (float)px, fy = (float)py, fz = (float)pz;
+        const float Lf = (float)L;
+        if (fx >= Lf) fx = 0.f;
+        if (fy >= Lf) fy = 0.f;
+        if (fz >= Lf) fz = 0.f;
+        pos4[i] = make_float4(fx, fy, fz, 0.f);
+    }
+}
+
+__global__ void kick_kernel(double* __restrict__ v, const float4* __restrict__ f, int64_t n,
+                            double dt)
+{
+    const double hk = 0.5 * dt * 48.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const float4 fi = f[i];
+        double* vi = v + 3 * i;
+        vi[0] += hk * (double)fi.x;
+        vi[1] += hk * (double)fi.y;
+        vi[2] += hk * (double)fi.z;
+    }
+}
+
+__global__ void to_float4_kernel(const double* __restrict__ x, int64_t n, double L,
+                                 float4* __restrict__ pos4)
+{
+    const float Lf = (float)L;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        float fx = (float)x[3 * i], fy = (float)x[3 * i + 1], fz = (float)x[3 * i + 2];
+        if (fx >= Lf) fx = 0.f;
+        if (fy >= Lf) fy = 0.f;
+        if (fz >= Lf) fz = 0.f;
+        pos4[i] = make_float4(fx, fy, fz, 0.f);
+    }
+}
+
+// dst[k] = src[perm[k]] for 3-vectors and ids
+__global__ void gather3_kernel(const double* __restrict__ src, const int32_t* __restrict__ perm,
+                               int64_t n, double* __restrict__ dst)
+{
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t s = perm[k];
+        dst[3 * k] = src[3 * s];
+        dst[3 * k + 1] = src[3 * s + 1];
+        dst[3 * k + 2] = src[3 * s + 2];
+    }
+}
+
+__global__ void gather_ids_kernel(const int32_t* __restrict__ src, const int32_t* __restrict__ perm,
+                                  int64_t n, int32_t* __restrict__ dst)
+{
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * blockDim.x)
+        dst[k] = src[perm[k]];
+}
+
+// out[ids[k]] = src[k]: back to the caller's atom order
+__global__ void scatter3_kernel(const double* __restrict__ src, const int32_t* __restrict__ ids,
+                                int64_t n, double* __restrict__ dst)
+{
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t d = ids[k];
+        dst[3 * d] = src[3 * k];
+        dst[3 * d + 1] = src[3 * k + 1];
+        dst[3 * d + 2] = src[3 * k + 2];
+    }
+}
+
+__device__ __forceinline__ double block_sum(double v, double* red)
+{
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    const int w = threadIdx.x / 32, l = threadIdx.x % 32;
+    __syncthreads();
+    if (l == 0) red[w] = v;
+    __syncthreads();
+    v = 0.0;
+    if (threadIdx.x < blockDim.x / 32) v = red[threadIdx.x];
+    if (w == 0)
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    return v;
+}
+
+__global__ void kinetic_kernel(const double* __restrict__ v, int64_t n, double* acc)
+{
+    __shared__ double red[32];
+    double s = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        s += v[3 * i] * v[3 * i] + v[3 * i + 1] * v[3 * i + 1] + v[3 * i + 2] * v[3 * i + 2];
+    s = block_sum(s, red);
+    if (threadIdx.x == 0) atomicAdd(acc, 0.5 * s);
+}
+
+// Potential energy 4(r^-12 - r^-6) and virial r.F = 48 r^2 s over every
+// directed entry (each pair counted twice, halved), FP32 per entry, FP64 sums.
+__global__ void potential_kernel(const float4* __restrict__ pos, const uint32_t* __restrict__ row_off,
+                                 const int32_t* __restrict__ col, int64_t n, LawParams law,
+                                 double* acc)
+{
+    __shared__ double red[32];
+    double pe = 0.0, vir = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const float4 a = pos[i];
+        float pe_i = 0.f, vir_i = 0.f;
+        for (uint32_t k = row_off[i]; k < row_off[i + 1]; k++) {
+            const float4 b = pos[col[k]];
+            float dx, dy, dz;
+            const float s = lj_scalar<true>(a, b, law, dx, dy, dz);
+            if (s == 0.0f) continue;
+            const float rd = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            const float r = 1.0f / rd;
+            const float r6 = r * r * r;
+            pe_i += 4.0f * r6 * (r6 - 1.0f);
+            vir_i += 48.0f * s * rd;
+        }
+        pe += 0.5 * (double)pe_i;
+        vir += 0.5 * (double)vir_i;
+    }
+    pe = block_sum(pe, red);
+    __syncthreads();
+    vir = block_sum(vir, red);
+    if (threadIdx.x == 0) {
+        atomicAdd(acc + 1, pe);
+        atomicAdd(acc + 2, vir);
+    }
+}
+
+void free_part(irr_md* m)
+{
+    if (m->part.perm) cudaFree(m->part.perm);
+    if (m->part.inv) cudaFree(m->part.inv);
+    if (m->part.row_off) cudaFree(m->part.row_off);
+    if (m->part.col) cudaFree(m->part.col);
+    m->part = PartitionOut{};
+    if (m->d_items) cudaFree(m->d_items);
+    m->d_items = nullptr;
+    m->num_items = 0;
+}
+
+// New neighbour list, partition and execution order from the current positions.
+int rebuild(irr_md* m)
+{
+    cudaStream_t s = m->stream;
+    const double lc = m->cfg.cutforce + m->cfg.skin;
+    int2* d_edges = nullptr;
+    int64_t e = 0;
+    MD_CUDA(m, build_neighbor_list(m->pos4, m->n, (float)m->cfg.side, (float)(lc * lc), &d_edges, &e, s),
+            "neighbour build");
+    free_part(m);
+    PartitionOut p;
+    cudaError_t pe = build_partition(m->pos4, m->n, d_edges, e, 1, &p, s);
+    if (d_edges) cudaFree(d_edges);
+    m->part = p;
+    if (pe != cudaSuccess) return md_fail(m, IRR_ERR_CUDA, "partition", pe);
+    // state into the new order
+    const int g = grid_of(m->n);
+    gather3_kernel<<<g, 256, 0, s>>>(m->x, m->part.perm, m->n, m->tmp);
+    std::swap(m->x, m->tmp);
+    gather3_kernel<<<g, 256, 0, s>>>(m->v, m->part.perm, m->n, m->tmp);
+    std::swap(m->v, m->tmp);
+    gather_ids_kernel<<<g, 256, 0, s>>>(m->ids, m->part.perm, m->n, m->ids_tmp);
+    std::swap(m->ids, m->ids_tmp);
+    to_float4_kernel<<<g, 256, 0, s>>>(m->x, m->n, m->cfg.side, m->pos4);
+    MD_CUDA(m, cudaGetLastError(), "permute state");
+    std::vector<uint32_t> ro((size_t)m->n + 1);
+    MD_CUDA(m, cudaMemcpyAsync(ro.data(), m->part.row_off, sizeof(uint32_t) * (m->n + 1),
+                               cudaMemcpyDeviceToHost, s), "row offsets");
+    MD_CUDA(m, cudaStreamSynchronize(s), "row offsets");
+    std::vector<WorkItem> items;
+    make_work_items(ro.data(), m->n, 0, m->shape.block_nodes, m->shape.stage_smem, items);
+    m->num_items = (int)items.size();
+    MD_CUDA(m, cudaMalloc(&m->d_items, sizeof(WorkItem) * (items.empty() ? 1 : items.size())), "work items");
+    if (!items.empty())
+        MD_CUDA(m, cudaMemcpyAsync(m->d_items, items.data(), sizeof(WorkItem) * items.size(),
+                                   cudaMemcpyHostToDevice, s), "work items");
+    InstDesc d{};
+    d.pos = m->pos4;
+    d.row_off = m->part.row_off;
+    d.col = m->part.col;
+    d.force = m->force;
+    d.law = m->law;
+    d.n = m->n;
+    MD_CUDA(m, cudaMemcpyAsync(m->d_inst, &d, sizeof(d), cudaMemcpyHostToDevice, s), "instance");
+    MD_CUDA(m, cudaStreamSynchronize(s), "rebuild");
+    m->edges = e;
+    m->rebuilds++;
+    m->since_rebuild = 0;
+    return IRR_OK;
+}
+
+int forces(irr_md* m)
+{
+    MD_CUDA(m, cudaMemsetAsync(m->d_queue, 0, sizeof(int), m->stream), "queue");
+    MD_CUDA(m, launch_tiled(m->shape, m->d_inst, m->d_items, m->num_items, m->d_queue,
+                            m->sms * kCtasPerSm, m->d_status, m->stream), "force kernel");
+    return IRR_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void irr_md_config_default(irr_md_config* c)
+{
+    if (!c) return;
+    memset(c, 0, sizeof(*c));
+    c->device = 0;
+    c->dt = 0.005;
+    c->cutforce = 2.5;
+    c->skin = 0.3;
+    c->side = 0.0;
+    c->rebuild_every = 20;
+}
+
+int irr_md_create(const irr_md_config* cfg, const double* pos, const double* vel, int64_t n,
+                  irr_md** out)
+{
+    if (!cfg || !out || n < 2 || !pos || !vel) return IRR_ERR_ARG;
+    *out = nullptr;
+    if (!(cfg->side > 0) || !(cfg->dt > 0) || !(cfg->cutforce > 0) || !(cfg->skin >= 0) ||
+        cfg->rebuild_every < 1)
+        return IRR_ERR_ARG;
+    if (2.0 * (cfg->cutforce + cfg->skin) > cfg->side) return IRR_ERR_ARG;  // one image per pair
+    if (n > 0x7fffffffLL) return IRR_ERR_CAPACITY;
+    irr_md* m = new (std::nothrow) irr_md();
+    if (!m) return IRR_ERR_NOMEM;
+    m->cfg = *cfg;
+    m->device = cfg->device;
+    m->n = n;
+    int rc = IRR_OK;
+    if (cudaSetDevice(m->device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&m->sms, cudaDevAttrMultiProcessorCount, m->device) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&m->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        delete m;
+        return IRR_ERR_CUDA;
+    }
+    m->stream = m->own_stream;
+    const double rc2 = cfg->cutforce * cfg->cutforce;
+    LawParams L{};
+    L.rc2d = rc2;
+    L.rc2 = (float)rc2;
+    L.rc2_lo = (float)(rc2 * (1.0 - 1.0 / 262144.0));
+    L.rc2_hi = (float)(rc2 * (1.0 + 1.0 / 262144.0));
+    L.periodic = 1;
+    L.side = cfg->side;
+    L.halfd = 0.5 * cfg->side;
+    L.half = (float)(0.5 * cfg->side);
+    L.side_hi = (float)cfg->side;
+    L.side_lo = (float)(cfg->side - (double)L.side_hi);
+    L.half2 = (float)(0.25 * cfg->side * cfg->side * (1.0 - 1.0 / 65536.0));
+    L.band = (float)(rc2 * (2.0 / 262144.0));
+    m->law = L;
+    m->shape.lanes_per_row = 4;
+    m->shape.block_nodes = 1024;
+    m->shape.stage_smem = 1;
+    m->shape.periodic = 1;
+    const size_t b3 = sizeof(double) * 3 * (size_t)n;
+    cudaError_t e = cudaSuccess;
+    if (e == cudaSuccess) e = cudaMalloc(&m->x, b3);
+    if (e == cudaSuccess) e = cudaMalloc(&m->v, b3);
+    if (e == cudaSuccess) e = cudaMalloc(&m->tmp, b3);
+    if (e == cudaSuccess) e = cudaMalloc(&m->pos4, sizeof(float4) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&m->force, sizeof(float4) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&m->ids, sizeof(int32_t) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&m->ids_tmp, sizeof(int32_t) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&m->d_inst, sizeof(InstDesc));
+    if (e == cudaSuccess) e = cudaMalloc(&m->d_queue, sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&m->d_status, sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&m->d_acc, 4 * sizeof(double));
+    if (e == cudaSuccess) e = cudaMemsetAsync(m->d_status, 0, sizeof(int), m->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(m->x, pos, b3, cudaMemcpyHostToDevice, m->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(m->v, vel, b3, cudaMemcpyHostToDevice, m->stream);
+    if (e != cudaSuccess) {
+        irr_md_destroy(m);
+        return e == cudaErrorMemoryAllocation ? IRR_ERR_NOMEM : IRR_ERR_CUDA;
+    }
+    std::vector<int32_t> iota((size_t)n);
+    for (int64_t i = 0; i < n; i++) iota[(size_t)i] = (int32_t)i;
+    e = cudaMemcpy(m->ids, iota.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        // wrap the initial positions and make their float copy
+        to_float4_kernel<<<grid_of(n), 256, 0, m->stream>>>(m->x, n, cfg->side, m->pos4);
+        e = cudaGetLastError();
+    }
+    if (e != cudaSuccess) {
+        irr_md_destroy(m);
+        return IRR_ERR_CUDA;
+    }
+    rc = rebuild(m);
+    if (rc == IRR_OK) rc = forces(m);
+    if (rc == IRR_OK && cudaStreamSynchronize(m->stream) != cudaSuccess) rc = IRR_ERR_CUDA;
+    if (rc != IRR_OK) {
+        irr_md_destroy(m);
+        return rc;
+    }
+    *out = m;
+    return IRR_OK;
+}
+
+int irr_md_destroy(irr_md* m)
+{
+    if (!m) return IRR_ERR_ARG;
+    cudaSetDevice(m->device);
+    if (m->stream) cudaStreamSynchronize(m->stream);
+    free_part(m);
+    void* ptrs[] = {m->x, m->v, m->tmp, m->pos4, m->force, m->ids, m->ids_tmp,
+                    m->d_inst, m->d_queue, m->d_status, m->d_acc};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (m->own_stream) cudaStreamDestroy(m->own_stream);
+    delete m;
+    return IRR_OK;
+}
+
+const char* irr_md_last_error(const irr_md* m) { return m ? m->err.c_str() : "null handle"; }
+
+int irr_md_set_stream(irr_md* m, void* stream)
+{
+    if (!m) return IRR_ERR_ARG;
+    m->stream = (cudaStream_t)stream;
+    return IRR_OK;
+}
+
+int irr_md_run(irr_md* m, int steps)
+{
+    if (!m || steps < 0) return IRR_ERR_ARG;
+    cudaSetDevice(m->device);
+    const int g = grid_of(m->n);
+    for (int t = 0; t < steps; t++) {
+        kick_drift_kernel<<<g, 256, 0, m->stream>>>(m->x, m->v, m->force, m->n, m->cfg.dt,
+                                                    m->cfg.side, m->pos4);
+        MD_CUDA(m, cudaGetLastError(), "kick-drift");
+        m->since_rebuild++;
+        if (m->since_rebuild >= m->cfg.rebuild_every) {
+            int rc = rebuild(m);
+            if (rc) return rc;
+        }
+        int rc = forces(m);
+        if (rc) return rc;
+        kick_kernel<<<g, 256, 0, m->stream>>>(m->v, m->force, m->n, m->cfg.dt);
+        MD_CUDA(m, cudaGetLastError(), "kick");
+        m->steps++;
+    }
+    return IRR_OK;
+}
+
+int irr_md_energy(irr_md* m, double* kinetic, double* potential, double* virial)
+{
+    if (!m) return IRR_ERR_ARG;
+    cudaSetDevice(m->device);
+    MD_CUDA(m, cudaMemsetAsync(m->d_acc, 0, 4 * sizeof(double), m->stream), "energy");
+    kinetic_kernel<<<grid_of(m->n) < 1024 ? grid_of(m->n) : 1024, 256, 0, m->stream>>>(m->v, m->n, m->d_acc);
+    potential_kernel<<<grid_of(m->n) < 2048 ? grid_of(m->n) : 2048, 256, 0, m->stream>>>(
+        m->pos4, m->part.row_off, m->part.col, m->n, m->law, m->d_acc);
+    MD_CUDA(m, cudaGetLastError(), "energy kernels");
+    double h[4];
+    MD_CUDA(m, cudaMemcpyAsync(h, m->d_acc, sizeof(h), cudaMemcpyDeviceToHost, m->stream), "energy");
+    MD_CUDA(m, cudaStreamSynchronize(m->stream), "energy");
+    if (kinetic) *kinetic = h[0];
+    if (potential) *potential = h[1];
+    if (virial) *virial = h[2];
+    int st = 0;
+    MD_CUDA(m, cudaMemcpy(&st, m->d_status, sizeof(int), cudaMemcpyDeviceToHost), "status");
+    if (st) return md_fail(m, IRR_ERR_DEVICE, "device status set (a bounded wait gave up)");
+    return IRR_OK;
+}
+
+int irr_md_get_state(irr_md* m, double* pos, double* vel)
+{
+    if (!m) return IRR_ERR_ARG;
+    cudaSetDevice(m->device);
+    const size_t b3 = sizeof(double) * 3 * (size_t)m->n;
+    const int g = grid_of(m->n);
+    std::vector<double> host;
+    double* outs[2] = {pos, vel};
+    double* srcs[2] = {m->x, m->v};
+    for (int k = 0; k < 2; k++) {
+        if (!outs[k]) continue;
+        scatter3_kernel<<<g, 256, 0, m->stream>>>(srcs[k], m->ids, m->n, m->tmp);
+        MD_CUDA(m, cudaGetLastError(), "state");
+        MD_CUDA(m, cudaMemcpyAsync(outs[k], m->tmp, b3, cudaMemcpyDeviceToHost, m->stream), "state");
+        MD_CUDA(m, cudaStreamSynchronize(m->stream), "state");
+    }
+    return IRR_OK;
+}
+
+int irr_md_get_forces(irr_md* m, double* f)
+{
+    if (!m || !f) return IRR_ERR_ARG;
+    cudaSetDevice(m->device);
+    // F = 48 * reduction result, in the caller's atom order
+    std::vector<float4> fr((size_t)m->n);
+    std::vector<int32_t> ids((size_t)m->n);
+    MD_CUDA(m, cudaMemcpyAsync(fr.data(), m->force, sizeof(float4) * m->n, cudaMemcpyDeviceToHost, m->stream), "forces");
+    MD_CUDA(m, cudaMemcpyAsync(ids.data(), m->ids, sizeof(int32_t) * m->n, cudaMemcpyDeviceToHost, m->stream), "forces");
+    MD_CUDA(m, cudaStreamSynchronize(m->stream), "forces");
+    for (int64_t k = 0; k < m->n; k++) {
+        const int64_t d = ids[(size_t)k];
+        f[3 * d] = 48.0 * fr[(size_t)k].x;
+        f[3 * d + 1] = 48.0 * fr[(size_t)k].y;
+        f[3 * d + 2] = 48.0 * fr[(size_t)k].z;
+    }
+    return IRR_OK;
+}
+
+int irr_md_get_info(const irr_md* m, irr_md_info* info)
+{
+    if (!m || !info) return IRR_ERR_ARG;
+    memset(info, 0, sizeof(*info));
+    info->num_atoms = m->n;
+    info->num_edges = m->edges;
+    info->steps = m->steps;
+    info->rebuilds = m->rebuilds;
+    return IRR_OK;
+}
+
+}  // extern "C"

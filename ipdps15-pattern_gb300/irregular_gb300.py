@@ -17,7 +17,8 @@ from typing import Optional
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libirregular_gb300.so")
+# IRR_LIBRARY selects another build of the library (e.g. a variant build).
+LIB_PATH = os.environ.get("IRR_LIBRARY") or os.path.join(HERE, "libirregular_gb300.so")
 
 IRR_OK = 0
 IRR_ERR_ARG = 1
@@ -56,6 +57,17 @@ class Info(C.Structure):
                 ("stage_smem", C.c_int32), ("exec", C.c_int32)]
 
 
+class MDConfig(C.Structure):
+    _fields_ = [("device", C.c_int), ("rebuild_every", C.c_int), ("dt", C.c_double),
+                ("cutforce", C.c_double), ("skin", C.c_double), ("side", C.c_double),
+                ("reserved", C.c_int * 8)]
+
+
+class MDInfo(C.Structure):
+    _fields_ = [("num_atoms", C.c_int64), ("num_edges", C.c_int64), ("steps", C.c_int64),
+                ("rebuilds", C.c_int64)]
+
+
 # name -> (restype, argtypes); every symbol include/irregular_gb300.h declares
 P = C.c_void_p
 I64 = C.c_int64
@@ -84,6 +96,17 @@ _SIGS = {
                                      C.POINTER(P), C.POINTER(I64)]),
     "irr_device_free": (C.c_int, [C.c_int, P]),
     "irr_morton_order_static": (C.c_int, [C.c_int, P, P, C.c_int, I64, P]),
+    "irr_md_config_default": (None, [C.POINTER(MDConfig)]),
+    "irr_md_create": (C.c_int, [C.POINTER(MDConfig), P, P, I64, C.POINTER(P)]),
+    "irr_md_destroy": (C.c_int, [P]),
+    "irr_md_last_error": (C.c_char_p, [P]),
+    "irr_md_set_stream": (C.c_int, [P, P]),
+    "irr_md_run": (C.c_int, [P, C.c_int]),
+    "irr_md_energy": (C.c_int, [P, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                C.POINTER(C.c_double)]),
+    "irr_md_get_state": (C.c_int, [P, P, P]),
+    "irr_md_get_forces": (C.c_int, [P, P]),
+    "irr_md_get_info": (C.c_int, [P, C.POINTER(MDInfo)]),
 }
 
 _lib = None
@@ -324,6 +347,70 @@ class Handle:
         self._check(load().irr_get_partition(self._h, _ptr(perm), _ptr(row_off), _ptr(col)),
                     "irr_get_partition")
         return perm, row_off, col[:m]
+
+
+class MD:
+    """GPU Lennard-Jones MD (irr_md_*): FP64 state and integration, FP32 forces."""
+
+    def __init__(self, pos, vel, side: float, dt: float = 0.005, cutforce: float = 2.5,
+                 skin: float = 0.3, rebuild_every: int = 20, device: int = 0):
+        L = load()
+        cfg = MDConfig()
+        L.irr_md_config_default(C.byref(cfg))
+        cfg.device, cfg.dt, cfg.cutforce, cfg.skin = device, dt, cutforce, skin
+        cfg.side, cfg.rebuild_every = side, rebuild_every
+        p = np.ascontiguousarray(pos, np.float64).reshape(-1, 3)
+        v = np.ascontiguousarray(vel, np.float64).reshape(-1, 3)
+        self.n = p.shape[0]
+        h = C.c_void_p()
+        rc = L.irr_md_create(C.byref(cfg), _ptr(p), _ptr(v), self.n, C.byref(h))
+        if rc != IRR_OK:
+            raise IrregularError(rc, f"irr_md_create: {L.irr_status_string(rc).decode()}")
+        self._h = h
+
+    def _check(self, rc, what):
+        if rc != IRR_OK:
+            msg = load().irr_md_last_error(self._h)
+            raise IrregularError(rc, f"{what}: {msg.decode() if msg else ''}")
+
+    def set_stream(self, stream_ptr: int):
+        self._check(load().irr_md_set_stream(self._h, C.c_void_p(stream_ptr)), "irr_md_set_stream")
+
+    def run(self, steps: int):
+        self._check(load().irr_md_run(self._h, int(steps)), "irr_md_run")
+
+    def energy(self):
+        ke, pe, vir = C.c_double(), C.c_double(), C.c_double()
+        self._check(load().irr_md_energy(self._h, C.byref(ke), C.byref(pe), C.byref(vir)),
+                    "irr_md_energy")
+        return ke.value, pe.value, vir.value
+
+    def state(self):
+        p = np.empty((self.n, 3), np.float64)
+        v = np.empty((self.n, 3), np.float64)
+        self._check(load().irr_md_get_state(self._h, _ptr(p), _ptr(v)), "irr_md_get_state")
+        return p, v
+
+    def forces(self):
+        f = np.empty((self.n, 3), np.float64)
+        self._check(load().irr_md_get_forces(self._h, _ptr(f)), "irr_md_get_forces")
+        return f
+
+    def info(self) -> MDInfo:
+        inf = MDInfo()
+        self._check(load().irr_md_get_info(self._h, C.byref(inf)), "irr_md_get_info")
+        return inf
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().irr_md_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class IrregularRuntime:

@@ -647,3 +647,92 @@ int orc_partition(int64_t n, const float *pos, const float lo[3], const float sc
     free(fill);
     return 0;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Reference MD (FP64).                                                      */
+/* ------------------------------------------------------------------------ */
+
+static double wrap_box(double x, double L)
+{
+    x -= L * floor(x / L);
+    if (x >= L) x -= L;
+    if (x < 0.0) x = 0.0;
+    return x;
+}
+
+static int64_t md_list(int64_t n, const double *pos, double side, double lc, float **fpos,
+                       int32_t **edges)
+{
+    float *fp = *fpos;
+    float Lf = (float)side;
+    for (int64_t k = 0; k < 3 * n; k++) {
+        float v = (float)pos[k];
+        fp[k] = v >= Lf ? 0.0f : v;
+    }
+    int64_t e = orc_neighbor_half_list(n, fp, Lf, (float)(lc * lc), NULL, 0);
+    free(*edges);
+    *edges = (int32_t *)malloc(sizeof(int32_t) * 2 * (size_t)(e > 0 ? e : 1));
+    orc_neighbor_half_list(n, fp, Lf, (float)(lc * lc), *edges, e);
+    return e;
+}
+
+static void md_forces(int64_t n, const double *pos, int64_t e, const int32_t *edges,
+                      const orc_lj_param *p, double *f, double *pe)
+{
+    memset(f, 0, sizeof(double) * 3 * (size_t)n);
+    double u = 0.0;
+    for (int64_t t = 0; t < e; t++) {
+        int32_t i = edges[2 * t], j = edges[2 * t + 1];
+        double d[3], s;
+        if (!lj_edge_f64(pos, i, j, p, d, &s, NULL)) continue;
+        double rd = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+        double r6 = 1.0 / (rd * rd * rd);
+        u += 4.0 * r6 * (r6 - 1.0);
+        for (int c = 0; c < 3; c++) {
+            f[3 * (int64_t)i + c] += 48.0 * d[c] * s;
+            f[3 * (int64_t)j + c] -= 48.0 * d[c] * s;
+        }
+    }
+    if (pe) *pe = u;
+}
+
+int orc_md_run(int64_t n, double *pos, double *vel, double side, double cutforce, double skin,
+               double dt, int steps, int rebuild_every, double *ke, double *pe)
+{
+    if (n < 2 || !(side > 0) || rebuild_every < 1) return -1;
+    orc_lj_param p = {side, cutforce * cutforce, 1};
+    float *fpos = (float *)malloc(sizeof(float) * 3 * (size_t)n);
+    double *f = (double *)malloc(sizeof(double) * 3 * (size_t)n);
+    int32_t *edges = NULL;
+    if (!fpos || !f) {
+        free(fpos);
+        free(f);
+        return -1;
+    }
+    for (int64_t k = 0; k < 3 * n; k++) pos[k] = wrap_box(pos[k], side);
+    int64_t e = md_list(n, pos, side, cutforce + skin, &fpos, &edges);
+    md_forces(n, pos, e, edges, &p, f, NULL);
+    int since = 0;
+    for (int t = 0; t < steps; t++) {
+        for (int64_t k = 0; k < 3 * n; k++) {
+            vel[k] += 0.5 * dt * f[k];
+            pos[k] = wrap_box(pos[k] + dt * vel[k], side);
+        }
+        if (++since >= rebuild_every) {
+            e = md_list(n, pos, side, cutforce + skin, &fpos, &edges);
+            since = 0;
+        }
+        md_forces(n, pos, e, edges, &p, f, NULL);
+        for (int64_t k = 0; k < 3 * n; k++) vel[k] += 0.5 * dt * f[k];
+    }
+    if (pe) md_forces(n, pos, e, edges, &p, f, pe);
+    if (ke) {
+        double s = 0.0;
+        for (int64_t k = 0; k < 3 * n; k++) s += vel[k] * vel[k];
+        *ke = 0.5 * s;
+    }
+    free(fpos);
+    free(f);
+    free(edges);
+    return 0;
+}

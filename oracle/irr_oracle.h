@@ -96,6 +96,16 @@ int64_t orc_neighbor_half_list(int64_t n, const float *pos, float box, float lis
 int64_t orc_neighbor_half_list_rows(int64_t n, const float *pos, float box, float list_cut2,
                                     int64_t row_begin, int64_t row_end, int32_t *out, int64_t cap);
 
+/* FP64 reference MD for the GPU loop: velocity Verlet (m = 1), forces
+ * 48 d (r^-14 - r^-8/2) for pairs inside `cutforce` with moldyn's minimum
+ * image, positions wrapped into [0, side) after each drift, the half list
+ * (orc_neighbor_half_list on the float copy of the positions, cutoff
+ * cutforce + skin) rebuilt after the drift of every rebuild_every-th step.
+ * pos, vel: 3n doubles, updated in place.  ke / pe (optional) receive the
+ * final kinetic and potential (4(r^-12 - r^-6) inside the cutoff) energy. */
+int orc_md_run(int64_t n, double *pos, double *vel, double side, double cutforce, double skin,
+               double dt, int steps, int rebuild_every, double *ke, double *pe);
+
 /* FCC lattice of moldyn's InitCoordinates (moldyn/moldyn.cu:596-626):
  * 4*m^3 points, spacing side/m.  pos: 3*4*m^3 doubles. */
 void orc_fcc_moldyn(int m, double side, double *pos);

@@ -58,6 +58,9 @@ def lib():
         L.orc_neighbor_half_list.restype = i64
         L.orc_neighbor_half_list_rows.argtypes = [i64, P, C.c_float, C.c_float, i64, i64, P, i64]
         L.orc_neighbor_half_list_rows.restype = i64
+        L.orc_md_run.argtypes = [i64, P, P, C.c_double, C.c_double, C.c_double, C.c_double,
+                                 C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.orc_md_run.restype = C.c_int
         L.orc_fcc_moldyn.argtypes = [C.c_int, C.c_double, P]
         L.orc_fcc_minimd.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, P, i64]
         L.orc_fcc_minimd.restype = i64
@@ -187,6 +190,19 @@ def neighbor_count(pos32, box: float, list_cut2: float) -> int:
     pos32 = np.ascontiguousarray(pos32, np.float32).reshape(-1, 3)
     return int(lib().orc_neighbor_half_list(pos32.shape[0], _p(pos32), float(box),
                                             float(list_cut2), None, 0))
+
+
+def md_run(pos, vel, side: float, cutforce: float, skin: float, dt: float, steps: int,
+           rebuild_every: int):
+    """FP64 reference MD; returns (pos, vel, kinetic, potential)."""
+    p = np.array(pos, np.float64).reshape(-1, 3).copy()
+    v = np.array(vel, np.float64).reshape(-1, 3).copy()
+    ke, pe = C.c_double(), C.c_double()
+    rc = lib().orc_md_run(p.shape[0], _p(p), _p(v), float(side), float(cutforce), float(skin),
+                          float(dt), int(steps), int(rebuild_every), C.byref(ke), C.byref(pe))
+    if rc != 0:
+        raise ValueError("orc_md_run failed")
+    return p, v, ke.value, pe.value
 
 
 def fcc_moldyn(m: int, side: float) -> np.ndarray:

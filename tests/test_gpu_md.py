@@ -1,0 +1,89 @@
+"""The GPU MD loop (irr_md_*) against the FP64 reference MD of the oracle (GPU)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def system(cells=6, rho=0.8442, temp=1.44, seed=20260003, jitter=0.03):
+    import workloads as W
+    pos, side = W.fcc_lattice(cells, cells, cells, rho)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    pos = (pos + rng.normal(0, jitter, pos.shape)) % side
+    vel = W.maxwell_velocities(pos.shape[0], temp, seed + 1)
+    return pos, vel, side
+
+
+def test_initial_forces_match_fp64(built_lib, oracle_lib):
+    import irregular_gb300 as irr
+    O = oracle_lib
+    pos, vel, side = system()
+    md = irr.MD(pos, vel, side)
+    f = md.forces()
+    # FP64 forces of the positions the GPU computes with (the float copy of
+    # the FP64 state), list at 2.8
+    p32 = pos.astype(np.float32)
+    edges = O.neighbor_half_list(p32, float(np.float32(side)), np.float32(2.8 ** 2))
+    f64, sabs = O.lj_reduce_f64(p32.astype(np.float64), edges, O.lj_param(2.5 ** 2, side, True))
+    f64 *= 48.0
+    assert np.abs(f - f64).max() / np.abs(f64).max() <= 1e-6
+    assert md.info().num_edges == edges.shape[0]
+    md.close()
+
+
+def test_short_trajectory_matches_fp64_reference(built_lib, oracle_lib):
+    import irregular_gb300 as irr
+    O = oracle_lib
+    pos, vel, side = system()
+    steps = 25  # crosses one rebuild (every 20 steps)
+    md = irr.MD(pos, vel, side, dt=0.005, rebuild_every=20)
+    md.run(steps)
+    gp, gv = md.state()
+    info = md.info()
+    assert info.steps == steps and info.rebuilds == 2  # the initial build + one
+    rp, rv, _, _ = O.md_run(pos, vel, side, 2.5, 0.3, 0.005, steps, 20)
+    dx = gp - rp
+    dx -= side * np.round(dx / side)
+    assert np.abs(dx).max() <= 1e-5
+    assert np.abs(gv - rv).max() <= 1e-4
+    md.close()
+
+
+def test_energy_and_momentum_conservation(built_lib):
+    import irregular_gb300 as irr
+    pos, vel, side = system(cells=8)
+    md = irr.MD(pos, vel, side, dt=0.005)
+    ke0, pe0, _ = md.energy()
+    e0 = ke0 + pe0
+    md.run(400)
+    ke1, pe1, vir = md.energy()
+    e1 = ke1 + pe1
+    n = pos.shape[0]
+    assert abs(e1 - e0) / abs(e0) <= 2e-3, (e0, e1)
+    _, v = md.state()
+    assert np.abs(v.sum(axis=0)).max() <= 1e-6 * n
+    assert md.info().rebuilds == 1 + 400 // 20
+    # temperature stays in the liquid's range
+    t = 2.0 * ke1 / (3 * n - 3)
+    assert 0.5 < t < 2.5
+    md.close()
+
+
+def test_energies_match_fp64(built_lib, oracle_lib):
+    import irregular_gb300 as irr
+    O = oracle_lib
+    pos, vel, side = system()
+    md = irr.MD(pos, vel, side)
+    ke, pe, _ = md.energy()
+    _, _, rke, rpe = O.md_run(pos, vel, side, 2.5, 0.3, 0.005, 0, 20)
+    assert abs(ke - rke) <= 1e-9 * abs(rke)
+    assert abs(pe - rpe) <= 1e-5 * abs(rpe)
+    md.close()
+
+
+def test_bad_md_config_is_rejected(built_lib):
+    import irregular_gb300 as irr
+    pos, vel, side = system(cells=2)  # side 6.7 < 2 * (2.5 + 0.3)
+    with pytest.raises(irr.IrregularError) as ei:
+        irr.MD(pos, vel, side)
+    assert ei.value.status == irr.IRR_ERR_ARG
