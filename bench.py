@@ -367,6 +367,92 @@ def run_ours(args, rank, world, local):
     return 0
 
 
+def run_batched(args):
+    """Config 4: 512 instances, sizes log-uniform in [1,024, 262,144] atoms, each
+    uniform-random in its own periodic box at density 0.8442, cutoff 2.5; one
+    persistent launch per step (CUDA graph, autotuned shape) vs the same
+    instances one by one through the single-instance paths."""
+    import torch
+
+    import irregular_gb300 as irr
+    import workloads as W
+
+    dev = 0
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.Stream(device=dev)
+    rng = np.random.Generator(np.random.PCG64(SEED + 2))
+    count = args.instances
+    sizes = np.floor(np.exp(rng.uniform(math.log(1024), math.log(262144), count))).astype(int)
+    t_setup = time.perf_counter()
+    part, plain = [], []
+    E = 0
+    for k, n in enumerate(sizes):
+        pos, side = W.random_box(int(n), 0.8442, SEED + 100 + k)
+        edges = irr.neighbor_build(pos, side, CUTOFF * CUTOFF, device=dev, stream=stream.cuda_stream)
+        E += edges.count
+        for mode, bucket in ((irr.IRR_EXEC_PARTITIONED, part), (irr.IRR_EXEC_PLAIN, plain)):
+            h = irr.Handle(irr.default_config(device=dev, map_idx=irr.IRR_MAP_LJ_MOLDYN, exec=mode))
+            h.set_stream(stream.cuda_stream)
+            h.set_params(irr.moldyn_params(side, CUTOFF))
+            h.set_edges(edges)
+            h.set_nodes(pos, 12)
+            h.init()
+            bucket.append(h)
+        edges.close()
+    b = irr.Batch(dev)
+    b.set_stream(stream.cuda_stream)
+    for h in part:
+        b.add(h)
+    b.finalize(autotune=True)
+    b.capture()
+    setup_s = time.perf_counter() - t_setup
+    for _ in range(args.warmup):
+        b.step()
+    b.sync()
+    ms_batch = time_steps(b, stream, args.batch_steps)
+    b.sync()
+
+    class Serial:
+        def __init__(self, hs):
+            self.hs = hs
+
+        def step(self):
+            for h in self.hs:
+                h.step()
+
+    for _ in range(2):
+        Serial(part).step()
+    ms_part = time_steps(Serial(part), stream, args.batch_steps)
+    ser_steps = max(3, args.batch_steps // 10)
+    Serial(plain).step()
+    ms_plain = time_steps(Serial(plain), stream, ser_steps)
+    torch.cuda.synchronize()
+    inf = b.info()
+    batched = E * args.batch_steps / (ms_batch / 1e3)
+    serial_part = E * args.batch_steps / (ms_part / 1e3)
+    serial_plain = E * ser_steps / (ms_plain / 1e3)
+    line = {"leg": "batched", "metric": "aggregate edges/s", "unit": "edges/s",
+            "instances": int(count), "nodes": int(sizes.sum()), "edges_per_step": int(E),
+            "steps": args.batch_steps, "batched": batched,
+            "serial_partitioned": serial_part, "serial_plain": serial_plain,
+            "speedup_vs_serial_partitioned": batched / serial_part,
+            "speedup_vs_serial_plain": batched / serial_plain,
+            "ms_per_step": {"batched": ms_batch / args.batch_steps,
+                            "serial_partitioned": ms_part / args.batch_steps,
+                            "serial_plain": ms_plain / ser_steps},
+            "shape": {"lanes_per_row": inf.lanes_per_row, "rows_per_item": inf.block_nodes,
+                      "work_items": int(inf.num_items), "cuda_graph": bool(inf.graph)},
+            "setup_s": setup_s,
+            "roofline": {"algorithmic_bytes_per_step": 8.0 * E + 24.0 * float(sizes.sum()),
+                         "achieved_GBs": (8.0 * E + 24.0 * float(sizes.sum())) /
+                         (ms_batch / 1e3 / args.batch_steps) / 1e9,
+                         "peak_GBs": measured_hbm_peak()[0]},
+            "data": "synthetic (seeded sizes and positions; lists built on the GPU)"}
+    b.close()
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -377,8 +463,11 @@ def main():
     ap.add_argument("--nodes", type=int, default=N_NODES,
                     help="workload size (default: the full 4,194,304-node workload; "
                          "smaller sizes are for profiling captures)")
-    ap.add_argument("--legs", choices=["all", "value"], default="all",
-                    help="'value': only the device-resident timed leg (profiling)")
+    ap.add_argument("--legs", choices=["all", "value", "batched", "md", "served"], default="all",
+                    help="'value': only the device-resident timed leg (profiling); "
+                         "'batched' / 'md' / 'served': the other configurations' measurements")
+    ap.add_argument("--instances", type=int, default=512)
+    ap.add_argument("--batch-steps", type=int, default=200)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -386,6 +475,8 @@ def main():
         world = int(os.environ.get("WORLD_SIZE", "1"))
         rank = int(os.environ.get("RANK", "0"))
         return run_reference(args, rank, world)
+    if args.legs == "batched":
+        return run_batched(args)
     rank, world, local = dist_init(args)
     rc = run_ours(args, rank, world, local)
     if world > 1:

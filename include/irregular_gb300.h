@@ -194,6 +194,48 @@ IRR_API int irr_get_info(const irr_handle *h, irr_info *info);
  * be NULL. */
 IRR_API int irr_get_partition(irr_handle *h, int32_t *perm, int64_t *row_off, int32_t *col);
 
+/* ----------------------------------------------------- batched instances
+ * Many independent instances reduced by ONE persistent launch per step: the
+ * reference's per-part work queue (moldyn/irregular/gpu_kernel.cu:60-77)
+ * widened to (instance, node block) work items.  No counterpart in the
+ * reference's API, which runs one edge set per runtime (paper Sec. II-C).
+ * Instances are partitioned handles, borrowed: they must outlive the batch,
+ * and their node data may change between steps (irr_set_nodes on the handle,
+ * on the batch's stream or synchronised with it); results are read from each
+ * handle (irr_get_result).  All instances share periodic or open
+ * boundaries. */
+typedef struct irr_batch irr_batch;
+typedef struct irr_batch_info {
+    int64_t num_instances;
+    int64_t num_nodes;
+    int64_t num_edges;
+    int64_t num_items;
+    int32_t lanes_per_row;
+    int32_t block_nodes;
+    int32_t graph;      /* 1 once a step is captured as a CUDA graph */
+    int32_t reserved;
+} irr_batch_info;
+
+IRR_API int irr_batch_create(int device, irr_batch **out);
+IRR_API int irr_batch_destroy(irr_batch *b);
+IRR_API const char *irr_batch_last_error(const irr_batch *b);
+IRR_API int irr_batch_set_stream(irr_batch *b, void *stream);
+IRR_API int irr_batch_add(irr_batch *b, irr_handle *h);
+/* Builds the instance table and the work-item list.  autotune != 0 times
+ * candidate shapes (lanes per node row x rows per work item) on this data and
+ * keeps the fastest, remembered per GPU and size class for the process. */
+IRR_API int irr_batch_finalize(irr_batch *b, int autotune);
+/* One reduction of every instance: one queue reset + one launch, or one CUDA
+ * graph replay once irr_batch_capture has run.  Enqueued; does not wait. */
+IRR_API int irr_batch_step(irr_batch *b);
+/* Captures one step (queue reset + launch) into a CUDA graph replayed by
+ * later irr_batch_step calls; needs a non-default stream. */
+IRR_API int irr_batch_capture(irr_batch *b);
+IRR_API int irr_batch_sync(irr_batch *b);
+IRR_API int irr_batch_get_info(const irr_batch *b, irr_batch_info *info);
+/* Picks the kernel shape of one partitioned handle by timing candidates. */
+IRR_API int irr_autotune(irr_handle *h);
+
 /* ------------------------------------------------------ neighbour lists
  * The half neighbour list the drivers build before the reduction, on the GPU
  * as a counting-sort cell list: miniMD's binned build (miniMD/neighbor.cpp:

@@ -10,48 +10,9 @@
 #include <string>
 #include <vector>
 
-#include "irr_internal.cuh"
-#include "../../include/irregular_gb300.h"
+#include "irr_handle.cuh"
 
 using namespace irr;
-
-struct irr_handle {
-    irr_config cfg{};
-    int device = 0;
-    int sms = 0;
-    cudaStream_t own_stream = nullptr;
-    cudaStream_t stream = nullptr;
-    std::string err;
-
-    int map_idx = IRR_MAP_LJ_MOLDYN;
-    int reduce_idx = IRR_REDUCE_SUM;
-    std::vector<unsigned char> param;
-    bool have_law = false;
-    LawParams law{};
-
-    int64_t n = -1;
-    int64_t e = -1;
-    void* d_raw = nullptr;       // node records as the caller passed them
-    size_t raw_cap = 0;
-    int raw_elm = 0;
-    bool raw_pending = false;    // d_raw holds records not yet converted
-    int2* d_edges = nullptr;     // caller's half list
-    size_t edges_cap = 0;
-
-    bool inited = false;
-    TiledShape shape{};
-    float4* d_pos = nullptr;     // execution order
-    float4* d_force = nullptr;
-    PartitionOut part{};
-    InstDesc* d_inst = nullptr;
-    WorkItem* d_items = nullptr;
-    int num_items = 0;
-    int* d_status = nullptr;
-    int* d_queue = nullptr;      // work-queue cursor, cleared before each launch
-    void* d_out = nullptr;       // result staging for host reads
-    size_t out_cap = 0;
-    int64_t dev_bytes = 0;
-};
 
 namespace {
 

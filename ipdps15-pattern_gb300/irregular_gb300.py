@@ -68,6 +68,12 @@ class MDInfo(C.Structure):
                 ("rebuilds", C.c_int64)]
 
 
+class BatchInfo(C.Structure):
+    _fields_ = [("num_instances", C.c_int64), ("num_nodes", C.c_int64), ("num_edges", C.c_int64),
+                ("num_items", C.c_int64), ("lanes_per_row", C.c_int32),
+                ("block_nodes", C.c_int32), ("graph", C.c_int32), ("reserved", C.c_int32)]
+
+
 # name -> (restype, argtypes); every symbol include/irregular_gb300.h declares
 P = C.c_void_p
 I64 = C.c_int64
@@ -96,6 +102,17 @@ _SIGS = {
                                      C.POINTER(P), C.POINTER(I64)]),
     "irr_device_free": (C.c_int, [C.c_int, P]),
     "irr_morton_order_static": (C.c_int, [C.c_int, P, P, C.c_int, I64, P]),
+    "irr_batch_create": (C.c_int, [C.c_int, C.POINTER(P)]),
+    "irr_batch_destroy": (C.c_int, [P]),
+    "irr_batch_last_error": (C.c_char_p, [P]),
+    "irr_batch_set_stream": (C.c_int, [P, P]),
+    "irr_batch_add": (C.c_int, [P, P]),
+    "irr_batch_finalize": (C.c_int, [P, C.c_int]),
+    "irr_batch_step": (C.c_int, [P]),
+    "irr_batch_capture": (C.c_int, [P]),
+    "irr_batch_sync": (C.c_int, [P]),
+    "irr_batch_get_info": (C.c_int, [P, C.POINTER(BatchInfo)]),
+    "irr_autotune": (C.c_int, [P]),
     "irr_md_config_default": (None, [C.POINTER(MDConfig)]),
     "irr_md_create": (C.c_int, [C.POINTER(MDConfig), P, P, I64, C.POINTER(P)]),
     "irr_md_destroy": (C.c_int, [P]),
@@ -338,6 +355,9 @@ class Handle:
         self._check(load().irr_get_info(self._h, C.byref(inf)), "irr_get_info")
         return inf
 
+    def autotune(self):
+        self._check(load().irr_autotune(self._h), "irr_autotune")
+
     def partition(self):
         inf = self.info()
         n, m = inf.num_nodes, inf.num_entries
@@ -347,6 +367,58 @@ class Handle:
         self._check(load().irr_get_partition(self._h, _ptr(perm), _ptr(row_off), _ptr(col)),
                     "irr_get_partition")
         return perm, row_off, col[:m]
+
+
+class Batch:
+    """Many partitioned handles reduced by one persistent launch per step."""
+
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        rc = load().irr_batch_create(device, C.byref(h))
+        if rc != IRR_OK:
+            raise IrregularError(rc, "irr_batch_create")
+        self._h = h
+        self.handles = []
+
+    def _check(self, rc, what):
+        if rc != IRR_OK:
+            msg = load().irr_batch_last_error(self._h)
+            raise IrregularError(rc, f"{what}: {msg.decode() if msg else ''}")
+
+    def set_stream(self, stream_ptr: int):
+        self._check(load().irr_batch_set_stream(self._h, C.c_void_p(stream_ptr)), "set_stream")
+
+    def add(self, handle: "Handle"):
+        self._check(load().irr_batch_add(self._h, handle.raw), "irr_batch_add")
+        self.handles.append(handle)  # keep the instance alive
+
+    def finalize(self, autotune: bool = False):
+        self._check(load().irr_batch_finalize(self._h, 1 if autotune else 0), "irr_batch_finalize")
+
+    def capture(self):
+        self._check(load().irr_batch_capture(self._h), "irr_batch_capture")
+
+    def step(self):
+        self._check(load().irr_batch_step(self._h), "irr_batch_step")
+
+    def sync(self):
+        self._check(load().irr_batch_sync(self._h), "irr_batch_sync")
+
+    def info(self) -> BatchInfo:
+        inf = BatchInfo()
+        self._check(load().irr_batch_get_info(self._h, C.byref(inf)), "irr_batch_get_info")
+        return inf
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().irr_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class MD:
