@@ -453,6 +453,72 @@ def run_batched(args):
     return 0
 
 
+def run_md(args):
+    """Config 3: miniMD-style LJ MD, FCC 4 x 64^3 = 1,048,576 atoms at density
+    0.8442, Maxwell velocities at T = 1.44, cutoff 2.5, skin 0.3, rebuild every
+    20 steps, velocity Verlet dt = 0.005, 1000 steps; FP32 forces, FP64
+    integration and energies."""
+    import torch
+
+    import irregular_gb300 as irr
+    import workloads as W
+
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    pos, side = W.fcc_lattice(64, 64, 64, 0.8442)
+    vel = W.maxwell_velocities(pos.shape[0], 1.44, SEED + 3)
+    md = irr.MD(pos, vel, side, dt=0.005, cutforce=2.5, skin=0.3, rebuild_every=20)
+    md.set_stream(stream.cuda_stream)
+    ke0, pe0, vir0 = md.energy()
+    md.run(20)  # warm-up (includes one rebuild)
+    ke_w, pe_w, _ = md.energy()
+    steps = args.md_steps
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    md.run(steps)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    ke1, pe1, vir1 = md.energy()
+    n = pos.shape[0]
+    info = md.info()
+    line = {"leg": "md", "metric": "ms per MD step", "unit": "ms", "atoms": n,
+            "steps": steps, "ms_per_step": ms / steps, "atom_steps_per_s": n * steps / (ms / 1e3),
+            "pairs_in_list": int(info.num_edges), "rebuilds": int(info.rebuilds),
+            "energy_per_atom": {"start": (ke0 + pe0) / n, "after_warmup": (ke_w + pe_w) / n,
+                                "end": (ke1 + pe1) / n},
+            "energy_drift_rel": abs((ke1 + pe1) - (ke_w + pe_w)) / abs(ke_w + pe_w),
+            "temperature_end": 2.0 * ke1 / (3 * n - 3),
+            "pressure_end": (2.0 * ke1 / 3.0 + vir1 / 3.0) / side ** 3,
+            "precision": "FP32 per-edge forces (compensated sums), FP64 integration and energies",
+            "data": "synthetic (miniMD FCC lattice, seeded Maxwell velocities)"}
+    md.close()
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_served(args):
+    """Config 5: Poisson arrivals at 200 jobs/s, sizes log-uniform in
+    [2,048, 2,097,152] atoms, density 0.8442, cutoff 2.5, 50 velocity-Verlet
+    steps each, 120 GB admission budget; continuous batching vs serial."""
+    import irregular_gb300 as irr
+
+    out = {"leg": "served", "jobs": args.jobs, "arrival_rate_per_s": 200.0,
+           "steps_per_job": 50, "budget_GB": 120.0,
+           "data": "synthetic (seeded arrivals and sizes; FCC + jitter, Maxwell velocities)"}
+    for mode, name in ((irr.IRR_SERVE_CONTINUOUS, "continuous"), (irr.IRR_SERVE_SERIAL, "serial")):
+        st, _ = irr.serve(num_jobs=args.jobs, mode=mode, arrival_rate=200.0, steps_per_job=50,
+                          budget_bytes=120e9, seed=SEED + 5)
+        out[name] = {"p50_ms": st.p50_ms, "p99_ms": st.p99_ms, "mean_ms": st.mean_ms,
+                     "max_ms": st.max_ms, "makespan_s": st.makespan_s,
+                     "edges_per_s": st.edges_per_s, "jobs_done": int(st.jobs_done),
+                     "max_resident": int(st.max_resident)}
+    out["speedup_edges_per_s"] = out["continuous"]["edges_per_s"] / out["serial"]["edges_per_s"]
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -467,6 +533,8 @@ def main():
                     help="'value': only the device-resident timed leg (profiling); "
                          "'batched' / 'md' / 'served': the other configurations' measurements")
     ap.add_argument("--instances", type=int, default=512)
+    ap.add_argument("--md-steps", type=int, default=1000)
+    ap.add_argument("--jobs", type=int, default=200)
     ap.add_argument("--batch-steps", type=int, default=200)
     args = ap.parse_args()
     if args.warmup < 3:
@@ -477,6 +545,10 @@ def main():
         return run_reference(args, rank, world)
     if args.legs == "batched":
         return run_batched(args)
+    if args.legs == "md":
+        return run_md(args)
+    if args.legs == "served":
+        return run_served(args)
     rank, world, local = dist_init(args)
     rc = run_ours(args, rank, world, local)
     if world > 1:

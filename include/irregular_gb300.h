@@ -301,6 +301,73 @@ IRR_API int irr_md_get_state(irr_md *m, double *pos, double *vel);
 IRR_API int irr_md_get_forces(irr_md *m, double *f);
 IRR_API int irr_md_get_info(const irr_md *m, irr_md_info *info);
 
+/* ------------------------------------------------------------ serving
+ * A request loop for MD jobs with continuous batching (no counterpart in the
+ * reference, which serves one edge set per process).  Jobs arrive as a seeded
+ * Poisson stream; each is a Lennard-Jones system (miniMD's FCC lattice with a
+ * small jitter, Maxwell velocities) of log-uniform size asking for
+ * steps_per_job velocity-Verlet steps.  Arrived jobs are admitted in order
+ * while their estimated device memory fits budget_bytes; every tick advances
+ * every resident job one step with ONE batched force launch over all of
+ * them; finished jobs leave and free their memory.  IRR_SERVE_SERIAL runs the
+ * same jobs one at a time.  A job's trajectory is bitwise the same alone
+ * (only_job = its index) and in the mix. */
+enum irr_serve_mode { IRR_SERVE_CONTINUOUS = 0, IRR_SERVE_SERIAL = 1 };
+
+typedef struct irr_serve_config {
+    int device;
+    int num_jobs;
+    int steps_per_job;
+    int rebuild_every;
+    int mode;           /* enum irr_serve_mode                                 */
+    int only_job;       /* >= 0: run that job alone (arriving at t = 0)        */
+    int max_resident;   /* slot limit on concurrently resident jobs            */
+    int reserved0;
+    double arrival_rate; /* jobs per second (Poisson)                         */
+    double density;
+    double cutforce;
+    double skin;
+    double dt;
+    double temperature;
+    int64_t min_atoms;  /* sizes log-uniform in [min_atoms, max_atoms]         */
+    int64_t max_atoms;
+    double budget_bytes; /* admission budget of device memory                 */
+    uint64_t seed;
+    int reserved[8];
+} irr_serve_config;
+
+typedef struct irr_serve_stats {
+    int64_t jobs_done;
+    int64_t rejected;     /* jobs larger than the whole budget                 */
+    int64_t max_resident;
+    int64_t reserved0;
+    double p50_ms;        /* job latency: completion - arrival                 */
+    double p99_ms;
+    double mean_ms;
+    double max_ms;
+    double makespan_s;
+    double pair_evals;    /* sum over jobs and steps of listed pairs reduced   */
+    double edges_per_s;   /* pair_evals / makespan                             */
+    double peak_budget_bytes;
+} irr_serve_stats;
+
+typedef struct irr_serve_job {
+    int64_t atoms;
+    int64_t edges;        /* pairs in the job's last list                      */
+    double arrival_s;
+    double admit_s;
+    double done_s;
+    double energy;        /* final kinetic + potential energy                  */
+    uint64_t state_hash;  /* FNV-1a of the final positions (FP64, atom order)  */
+    int32_t status;
+    int32_t reserved;
+} irr_serve_job;
+
+IRR_API void irr_serve_config_default(irr_serve_config *cfg);
+/* Runs the stream to completion; jobs_out (optional) has num_jobs records. */
+IRR_API int irr_serve_run(const irr_serve_config *cfg, irr_serve_stats *stats,
+                          irr_serve_job *jobs_out);
+
 /* ------------------------------------------------ allocation-free ordering
  * No counterpart in the reference.  The partitioner's Morton node ordering
  * (perm[new] = old node id, bit for bit the perm that irr_get_partition

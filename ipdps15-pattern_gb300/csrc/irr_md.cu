@@ -16,40 +16,9 @@
 #include <string>
 #include <vector>
 
-#include "irr_internal.cuh"
-#include "../../include/irregular_gb300.h"
+#include "irr_md.cuh"
 
 using namespace irr;
-
-struct irr_md {
-    irr_md_config cfg{};
-    int device = 0;
-    int sms = 0;
-    cudaStream_t own_stream = nullptr;
-    cudaStream_t stream = nullptr;
-    std::string err;
-    int64_t n = 0;
-    LawParams law{};
-    TiledShape shape{};
-    double* x = nullptr;       // [3n] positions, execution order
-    double* v = nullptr;       // [3n] velocities
-    double* tmp = nullptr;     // [3n] permutation scratch
-    float4* pos4 = nullptr;    // float copy of x for the reduction
-    float4* force = nullptr;   // reduction result (F / 48)
-    int32_t* ids = nullptr;    // execution slot -> caller's atom id
-    int32_t* ids_tmp = nullptr;
-    PartitionOut part{};
-    InstDesc* d_inst = nullptr;
-    WorkItem* d_items = nullptr;
-    int num_items = 0;
-    int* d_queue = nullptr;
-    int* d_status = nullptr;
-    double* d_acc = nullptr;   // [4] KE, PE, virial, spare
-    int64_t edges = 0;
-    int64_t steps = 0;
-    int64_t rebuilds = 0;
-    int64_t since_rebuild = 0;
-};
 
 namespace {
 
@@ -254,8 +223,12 @@ void free_part(irr_md* m)
     m->num_items = 0;
 }
 
+}  // namespace
+
+namespace irr {
+
 // New neighbour list, partition and execution order from the current positions.
-int rebuild(irr_md* m)
+int md_rebuild(irr_md* m)
 {
     cudaStream_t s = m->stream;
     const double lc = m->cfg.cutforce + m->cfg.skin;
@@ -302,10 +275,11 @@ int rebuild(irr_md* m)
     m->edges = e;
     m->rebuilds++;
     m->since_rebuild = 0;
+    m->host_items = std::move(items);
     return IRR_OK;
 }
 
-int forces(irr_md* m)
+int md_forces(irr_md* m)
 {
     MD_CUDA(m, cudaMemsetAsync(m->d_queue, 0, sizeof(int), m->stream), "queue");
     MD_CUDA(m, launch_tiled(m->shape, m->d_inst, m->d_items, m->num_items, m->d_queue,
@@ -313,7 +287,36 @@ int forces(irr_md* m)
     return IRR_OK;
 }
 
-}  // namespace
+int md_kick_drift(irr_md* m)
+{
+    kick_drift_kernel<<<grid_of(m->n), 256, 0, m->stream>>>(m->x, m->v, m->force, m->n, m->cfg.dt,
+                                                            m->cfg.side, m->pos4);
+    MD_CUDA(m, cudaGetLastError(), "kick-drift");
+    m->since_rebuild++;
+    return IRR_OK;
+}
+
+int md_kick(irr_md* m)
+{
+    kick_kernel<<<grid_of(m->n), 256, 0, m->stream>>>(m->v, m->force, m->n, m->cfg.dt);
+    MD_CUDA(m, cudaGetLastError(), "kick");
+    m->steps++;
+    return IRR_OK;
+}
+
+InstDesc md_instance(const irr_md* m)
+{
+    InstDesc d{};
+    d.pos = m->pos4;
+    d.row_off = m->part.row_off;
+    d.col = m->part.col;
+    d.force = m->force;
+    d.law = m->law;
+    d.n = m->n;
+    return d;
+}
+
+}  // namespace irr
 
 extern "C" {
 
@@ -404,8 +407,8 @@ int irr_md_create(const irr_md_config* cfg, const double* pos, const double* vel
         irr_md_destroy(m);
         return IRR_ERR_CUDA;
     }
-    rc = rebuild(m);
-    if (rc == IRR_OK) rc = forces(m);
+    rc = md_rebuild(m);
+    if (rc == IRR_OK) rc = md_forces(m);
     if (rc == IRR_OK && cudaStreamSynchronize(m->stream) != cudaSuccess) rc = IRR_ERR_CUDA;
     if (rc != IRR_OK) {
         irr_md_destroy(m);
@@ -443,21 +446,12 @@ int irr_md_run(irr_md* m, int steps)
 {
     if (!m || steps < 0) return IRR_ERR_ARG;
     cudaSetDevice(m->device);
-    const int g = grid_of(m->n);
     for (int t = 0; t < steps; t++) {
-        kick_drift_kernel<<<g, 256, 0, m->stream>>>(m->x, m->v, m->force, m->n, m->cfg.dt,
-                                                    m->cfg.side, m->pos4);
-        MD_CUDA(m, cudaGetLastError(), "kick-drift");
-        m->since_rebuild++;
-        if (m->since_rebuild >= m->cfg.rebuild_every) {
-            int rc = rebuild(m);
-            if (rc) return rc;
-        }
-        int rc = forces(m);
+        int rc = md_kick_drift(m);
+        if (!rc && m->since_rebuild >= m->cfg.rebuild_every) rc = md_rebuild(m);
+        if (!rc) rc = md_forces(m);
+        if (!rc) rc = md_kick(m);
         if (rc) return rc;
-        kick_kernel<<<g, 256, 0, m->stream>>>(m->v, m->force, m->n, m->cfg.dt);
-        MD_CUDA(m, cudaGetLastError(), "kick");
-        m->steps++;
     }
     return IRR_OK;
 }

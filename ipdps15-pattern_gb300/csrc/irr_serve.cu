@@ -1,0 +1,358 @@
+// irr_serve.cu -- a request loop that serves MD jobs with continuous batching.
+//
+// No counterpart in the reference, whose runtime serves one edge set per
+// process.  Jobs (Lennard-Jones systems of different sizes, each asking for a
+// number of velocity-Verlet steps) arrive as a Poisson stream.  The loop:
+//   * admits arrived jobs in arrival order while their estimated device memory
+//     fits the budget (their state then stays resident until they finish);
+//   * every tick advances each resident job by one step: per-job kick/drift,
+//     rebuilds that are due, ONE batched force launch over all resident jobs'
+//     (instance, node block) work items, per-job kick;
+//   * retires finished jobs (their memory frees up for waiting arrivals).
+// A job's rows are computed by the same kernel code whatever else shares the
+// launch, so its trajectory is bitwise the same alone and in the mix.
+// Serial mode runs the same jobs one at a time for comparison.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <random>
+#include <thread>
+#include <vector>
+
+#include "irr_md.cuh"
+
+using namespace irr;
+
+namespace {
+
+struct JobSpec {
+    double arrival;
+    int cells;
+    int64_t atoms;
+    uint64_t seed;
+    double side;
+    size_t est_bytes;
+};
+
+struct Live {
+    int id;
+    irr_md* md;
+    int steps;
+    double admit_s;
+    double pair_evals;
+};
+
+uint64_t mix64(uint64_t x)
+{
+    x += 0x9e3779b97f4a7c15ull;
+    x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ull;
+    x = (x ^ (x >> 27)) * 0x94d049bb133111ebull;
+    return x ^ (x >> 31);
+}
+
+// Job k's size, seed and arrival derive from (config seed, k) alone.
+std::vector<JobSpec> make_jobs(const irr_serve_config* c)
+{
+    std::vector<JobSpec> jobs;
+    std::mt19937_64 arr(c->seed);
+    std::exponential_distribution<double> gap(c->arrival_rate > 0 ? c->arrival_rate : 1.0);
+    double t = 0.0;
+    const double alat = std::cbrt(4.0 / c->density);
+    const int min_cells = (int)std::ceil(2.0 * (c->cutforce + c->skin) / alat + 1e-9);
+    for (int k = 0; k < c->num_jobs; k++) {
+        t += c->arrival_rate > 0 ? gap(arr) : 0.0;
+        std::mt19937_64 g(mix64(c->seed ^ (0x51ed2701ull * (uint64_t)(k + 1))));
+        std::uniform_real_distribution<double> u(std::log((double)c->min_atoms), std::log((double)c->max_atoms));
+        const double n = std::floor(std::exp(u(g)));
+        int cells = (int)std::lround(std::cbrt(n / 4.0));
+        cells = std::max(cells, min_cells);
+        JobSpec j;
+        j.arrival = t;
+        j.cells = cells;
+        j.atoms = 4ll * cells * cells * cells;
+        j.seed = g();
+        j.side = cells * alat;
+        // resident state + list + partition temporaries, per atom (bytes)
+        j.est_bytes = (size_t)j.atoms * 1600 + (64u << 20);
+        jobs.push_back(j);
+    }
+    return jobs;
+}
+
+// FCC lattice (miniMD's site order), a small Gaussian jitter, Maxwell
+// velocities at the temperature with zero total momentum.
+void initial_state(const JobSpec& j, const irr_serve_config* c, std::vector<double>& pos,
+                   std::vector<double>& vel)
+{
+    const double alat = std::cbrt(4.0 / c->density);
+    const int m = 2 * j.cells;
+    pos.clear();
+    for (int k = 0; k < m; k++)
+        for (int jj = 0; jj < m; jj++)
+            for (int i = 0; i < m; i++)
+                if ((i + jj + k) % 2 == 0) {
+                    pos.push_back(0.5 * alat * i);
+                    pos.push_back(0.5 * alat * jj);
+                    pos.push_back(0.5 * alat * k);
+                }
+    std::mt19937_64 g(j.seed);
+    std::normal_distribution<double> jit(0.0, 0.03);
+    for (double& x : pos) {
+        x += jit(g);
+        x -= j.side * std::floor(x / j.side);
+        if (x >= j.side) x = 0.0;
+    }
+    const int64_t n = j.atoms;
+    vel.assign(3 * n, 0.0);
+    std::normal_distribution<double> mv(0.0, std::sqrt(c->temperature));
+    double mean[3] = {0, 0, 0};
+    for (int64_t i = 0; i < n; i++)
+        for (int d = 0; d < 3; d++) {
+            vel[3 * i + d] = mv(g);
+            mean[d] += vel[3 * i + d];
+        }
+    double ke = 0.0;
+    for (int64_t i = 0; i < n; i++)
+        for (int d = 0; d < 3; d++) {
+            vel[3 * i + d] -= mean[d] / n;
+            ke += vel[3 * i + d] * vel[3 * i + d];
+        }
+    const double s = std::sqrt(c->temperature * (3 * n - 3) / ke);
+    for (double& v : vel) v *= s;
+}
+
+uint64_t fnv1a(const void* data, size_t bytes)
+{
+    const unsigned char* p = static_cast<const unsigned char*>(data);
+    uint64_t h = 1469598103934665603ull;
+    for (size_t i = 0; i < bytes; i++) h = (h ^ p[i]) * 1099511628211ull;
+    return h;
+}
+
+double pct(std::vector<double> v, double q)
+{
+    if (v.empty()) return 0.0;
+    std::sort(v.begin(), v.end());
+    const double r = q * (v.size() - 1);
+    const size_t lo = (size_t)std::floor(r), hi = (size_t)std::ceil(r);
+    return v[lo] + (v[hi] - v[lo]) * (r - lo);
+}
+
+}  // namespace
+
+extern "C" {
+
+void irr_serve_config_default(irr_serve_config* c)
+{
+    if (!c) return;
+    memset(c, 0, sizeof(*c));
+    c->device = 0;
+    c->num_jobs = 100;
+    c->steps_per_job = 50;
+    c->rebuild_every = 20;
+    c->mode = IRR_SERVE_CONTINUOUS;
+    c->only_job = -1;
+    c->max_resident = 1 << 20;
+    c->arrival_rate = 200.0;
+    c->density = 0.8442;
+    c->cutforce = 2.5;
+    c->skin = 0.3;
+    c->dt = 0.005;
+    c->temperature = 1.44;
+    c->min_atoms = 2048;
+    c->max_atoms = 2097152;
+    c->budget_bytes = 120e9;
+    c->seed = 20260005;
+}
+
+int irr_serve_run(const irr_serve_config* cfg, irr_serve_stats* st, irr_serve_job* out)
+{
+    if (!cfg || !st) return IRR_ERR_ARG;
+    if (cfg->num_jobs < 0 || cfg->steps_per_job < 1 || cfg->rebuild_every < 1 ||
+        cfg->min_atoms < 32 || cfg->max_atoms < cfg->min_atoms || !(cfg->density > 0) ||
+        !(cfg->budget_bytes > 0) || cfg->max_resident < 1)
+        return IRR_ERR_ARG;
+    if (cfg->only_job >= cfg->num_jobs) return IRR_ERR_ARG;
+    memset(st, 0, sizeof(*st));
+    if (cudaSetDevice(cfg->device) != cudaSuccess) {
+        cudaGetLastError();
+        return IRR_ERR_CUDA;
+    }
+    int sms = 0;
+    cudaStream_t s = nullptr;
+    int *d_queue = nullptr, *d_status = nullptr;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, cfg->device) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMalloc(&d_queue, sizeof(int)) != cudaSuccess || cudaMalloc(&d_status, sizeof(int)) != cudaSuccess ||
+        cudaMemset(d_status, 0, sizeof(int)) != cudaSuccess) {
+        cudaGetLastError();
+        return IRR_ERR_CUDA;
+    }
+    std::vector<JobSpec> jobs = make_jobs(cfg);
+    std::vector<int> order;
+    if (cfg->only_job >= 0) {
+        order.push_back(cfg->only_job);
+        jobs[cfg->only_job].arrival = 0.0;
+    } else {
+        for (int k = 0; k < cfg->num_jobs; k++) order.push_back(k);
+    }
+    const int max_res = cfg->mode == IRR_SERVE_SERIAL ? 1 : cfg->max_resident;
+    std::vector<double> latency;
+    std::vector<Live> live;
+    InstDesc* d_insts = nullptr;
+    WorkItem* d_items = nullptr;
+    size_t insts_cap = 0, items_cap = 0;
+    double used = 0.0, peak = 0.0, pair_evals = 0.0;
+    size_t next = 0;
+    int rc = IRR_OK;
+    TiledShape shape{};
+    shape.lanes_per_row = 4;
+    shape.block_nodes = 1024;
+    shape.stage_smem = 1;
+    shape.periodic = 1;
+    const auto t0 = std::chrono::steady_clock::now();
+    auto now = [&]() { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); };
+    std::vector<double> hpos, hvel;
+    while (rc == IRR_OK && (next < order.size() || !live.empty())) {
+        // admission, in arrival order, within the budget and the slot limit
+        while (next < order.size()) {
+            const JobSpec& j = jobs[order[next]];
+            if (j.arrival > now()) break;
+            if ((double)j.est_bytes > cfg->budget_bytes) {  // can never fit: rejected
+                if (out) {
+                    out[order[next]] = irr_serve_job{};
+                    out[order[next]].atoms = j.atoms;
+                    out[order[next]].arrival_s = j.arrival;
+                    out[order[next]].status = IRR_ERR_BUDGET;
+                }
+                st->rejected++;
+                next++;
+                continue;
+            }
+            if ((int)live.size() >= max_res || used + (double)j.est_bytes > cfg->budget_bytes) break;
+            initial_state(j, cfg, hpos, hvel);
+            irr_md_config mc;
+            irr_md_config_default(&mc);
+            mc.device = cfg->device;
+            mc.dt = cfg->dt;
+            mc.cutforce = cfg->cutforce;
+            mc.skin = cfg->skin;
+            mc.side = j.side;
+            mc.rebuild_every = cfg->rebuild_every;
+            irr_md* m = nullptr;
+            rc = irr_md_create(&mc, hpos.data(), hvel.data(), j.atoms, &m);
+            if (rc) break;
+            cudaStreamSynchronize(m->stream);
+            m->stream = s;
+            live.push_back(Live{order[next], m, 0, now(), 0.0});
+            used += (double)j.est_bytes;
+            peak = std::max(peak, used);
+            st->max_resident = std::max<int64_t>(st->max_resident, (int64_t)live.size());
+            next++;
+        }
+        if (rc) break;
+        if (live.empty()) {
+            if (next < order.size()) {
+                const double wait = jobs[order[next]].arrival - now();
+                if (wait > 0) std::this_thread::sleep_for(std::chrono::duration<double>(std::min(wait, 0.01)));
+            }
+            continue;
+        }
+        // one tick: every resident job advances one step
+        std::vector<InstDesc> insts;
+        std::vector<WorkItem> items;
+        for (size_t k = 0; k < live.size() && rc == IRR_OK; k++) {
+            irr_md* m = live[k].md;
+            rc = md_kick_drift(m);
+            if (!rc && m->since_rebuild >= m->cfg.rebuild_every) {
+                rc = md_rebuild(m);
+                m->stream = s;
+            }
+            if (rc) break;
+            insts.push_back(md_instance(m));
+            for (WorkItem w : m->host_items) {
+                w.inst = (int)k;
+                items.push_back(w);
+            }
+            live[k].pair_evals += (double)m->edges;
+        }
+        if (rc) break;
+        if (insts.size() > insts_cap) {
+            if (d_insts) cudaFree(d_insts);
+            insts_cap = insts.size() * 2;
+            if (cudaMalloc(&d_insts, sizeof(InstDesc) * insts_cap) != cudaSuccess) { rc = IRR_ERR_NOMEM; break; }
+        }
+        if (items.size() > items_cap) {
+            if (d_items) cudaFree(d_items);
+            items_cap = items.size() * 2;
+            if (cudaMalloc(&d_items, sizeof(WorkItem) * items_cap) != cudaSuccess) { rc = IRR_ERR_NOMEM; break; }
+        }
+        if (cudaMemcpyAsync(d_insts, insts.data(), sizeof(InstDesc) * insts.size(), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+            cudaMemcpyAsync(d_items, items.data(), sizeof(WorkItem) * items.size(), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+            cudaMemsetAsync(d_queue, 0, sizeof(int), s) != cudaSuccess ||
+            launch_tiled(shape, d_insts, d_items, (int)items.size(), d_queue, sms * kCtasPerSm, d_status, s) != cudaSuccess) {
+            rc = IRR_ERR_CUDA;
+            break;
+        }
+        for (auto& L : live) {
+            rc = md_kick(L.md);
+            if (rc) break;
+            L.steps++;
+        }
+        if (rc) break;
+        // the host copies of the tables are reused next tick: wait for this one
+        if (cudaStreamSynchronize(s) != cudaSuccess) { rc = IRR_ERR_CUDA; break; }
+        // retire finished jobs
+        for (size_t k = 0; k < live.size();) {
+            if (live[k].steps < cfg->steps_per_job) { k++; continue; }
+            Live L = live[k];
+            const JobSpec& j = jobs[L.id];
+            const double done = now();
+            latency.push_back(done - j.arrival);
+            pair_evals += L.pair_evals;
+            if (out) {
+                irr_serve_job r{};
+                r.atoms = j.atoms;
+                r.edges = L.md->edges;
+                r.arrival_s = j.arrival;
+                r.admit_s = L.admit_s;
+                r.done_s = done;
+                hpos.resize(3 * j.atoms);
+                irr_md_get_state(L.md, hpos.data(), nullptr);
+                r.state_hash = fnv1a(hpos.data(), sizeof(double) * hpos.size());
+                double ke = 0, pe = 0;
+                irr_md_energy(L.md, &ke, &pe, nullptr);
+                r.energy = ke + pe;
+                r.status = IRR_OK;
+                out[L.id] = r;
+            }
+            irr_md_destroy(L.md);
+            used -= (double)j.est_bytes;
+            live.erase(live.begin() + k);
+            st->jobs_done++;
+        }
+    }
+    const double makespan = now();
+    for (auto& L : live) irr_md_destroy(L.md);
+    int dev_status = 0;
+    cudaMemcpy(&dev_status, d_status, sizeof(int), cudaMemcpyDeviceToHost);
+    if (d_insts) cudaFree(d_insts);
+    if (d_items) cudaFree(d_items);
+    cudaFree(d_queue);
+    cudaFree(d_status);
+    cudaStreamDestroy(s);
+    if (rc == IRR_OK && dev_status) rc = IRR_ERR_DEVICE;
+    st->makespan_s = makespan;
+    st->p50_ms = 1e3 * pct(latency, 0.50);
+    st->p99_ms = 1e3 * pct(latency, 0.99);
+    st->mean_ms = latency.empty() ? 0.0 : 1e3 * std::accumulate(latency.begin(), latency.end(), 0.0) / latency.size();
+    st->max_ms = latency.empty() ? 0.0 : 1e3 * *std::max_element(latency.begin(), latency.end());
+    st->pair_evals = pair_evals;
+    st->edges_per_s = makespan > 0 ? pair_evals / makespan : 0.0;
+    st->peak_budget_bytes = peak;
+    return rc;
+}
+
+}  // extern "C"

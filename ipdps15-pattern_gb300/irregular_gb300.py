@@ -74,6 +74,34 @@ class BatchInfo(C.Structure):
                 ("block_nodes", C.c_int32), ("graph", C.c_int32), ("reserved", C.c_int32)]
 
 
+class ServeConfig(C.Structure):
+    _fields_ = [("device", C.c_int), ("num_jobs", C.c_int), ("steps_per_job", C.c_int),
+                ("rebuild_every", C.c_int), ("mode", C.c_int), ("only_job", C.c_int),
+                ("max_resident", C.c_int), ("reserved0", C.c_int), ("arrival_rate", C.c_double),
+                ("density", C.c_double), ("cutforce", C.c_double), ("skin", C.c_double),
+                ("dt", C.c_double), ("temperature", C.c_double), ("min_atoms", C.c_int64),
+                ("max_atoms", C.c_int64), ("budget_bytes", C.c_double), ("seed", C.c_uint64),
+                ("reserved", C.c_int * 8)]
+
+
+class ServeStats(C.Structure):
+    _fields_ = [("jobs_done", C.c_int64), ("rejected", C.c_int64), ("max_resident", C.c_int64),
+                ("reserved0", C.c_int64), ("p50_ms", C.c_double), ("p99_ms", C.c_double),
+                ("mean_ms", C.c_double), ("max_ms", C.c_double), ("makespan_s", C.c_double),
+                ("pair_evals", C.c_double), ("edges_per_s", C.c_double),
+                ("peak_budget_bytes", C.c_double)]
+
+
+class ServeJob(C.Structure):
+    _fields_ = [("atoms", C.c_int64), ("edges", C.c_int64), ("arrival_s", C.c_double),
+                ("admit_s", C.c_double), ("done_s", C.c_double), ("energy", C.c_double),
+                ("state_hash", C.c_uint64), ("status", C.c_int32), ("reserved", C.c_int32)]
+
+
+IRR_SERVE_CONTINUOUS = 0
+IRR_SERVE_SERIAL = 1
+
+
 # name -> (restype, argtypes); every symbol include/irregular_gb300.h declares
 P = C.c_void_p
 I64 = C.c_int64
@@ -113,6 +141,8 @@ _SIGS = {
     "irr_batch_sync": (C.c_int, [P]),
     "irr_batch_get_info": (C.c_int, [P, C.POINTER(BatchInfo)]),
     "irr_autotune": (C.c_int, [P]),
+    "irr_serve_config_default": (None, [C.POINTER(ServeConfig)]),
+    "irr_serve_run": (C.c_int, [C.POINTER(ServeConfig), C.POINTER(ServeStats), P]),
     "irr_md_config_default": (None, [C.POINTER(MDConfig)]),
     "irr_md_create": (C.c_int, [C.POINTER(MDConfig), P, P, I64, C.POINTER(P)]),
     "irr_md_destroy": (C.c_int, [P]),
@@ -419,6 +449,21 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+def serve(**kw):
+    """Runs the MD serving loop (irr_serve_run); returns (stats, jobs)."""
+    L = load()
+    cfg = ServeConfig()
+    L.irr_serve_config_default(C.byref(cfg))
+    for k, v in kw.items():
+        setattr(cfg, k, v)
+    stats = ServeStats()
+    jobs = (ServeJob * max(cfg.num_jobs, 1))()
+    rc = L.irr_serve_run(C.byref(cfg), C.byref(stats), C.cast(jobs, C.c_void_p))
+    if rc != IRR_OK:
+        raise IrregularError(rc, f"irr_serve_run: {L.irr_status_string(rc).decode()}")
+    return stats, list(jobs)[: cfg.num_jobs]
 
 
 class MD:
