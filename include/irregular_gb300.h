@@ -194,6 +194,26 @@ IRR_API int irr_get_info(const irr_handle *h, irr_info *info);
  * be NULL. */
 IRR_API int irr_get_partition(irr_handle *h, int32_t *perm, int64_t *row_off, int32_t *col);
 
+/* ---------------------------------------------------------- file formats
+ * The drivers' input files (host code; no GPU needed).
+ * irr_read_graph: moldyn's adjacency format (moldyn/misc.c:62-146): '%'
+ * comment lines before a "<nodes> <edges>" header, then one line per node of
+ * 1-based neighbour ids, read up to the first value <= 0; only neighbours
+ * j >= i are kept, so each pair is listed once, and their count must equal
+ * the header's (else IRR_ERR_STATE).  Pairs are written to `edges` (at most
+ * `cap`; NULL to count), 1-based when one_based != 0 as the reference's build
+ * returns them, else 0-based.
+ * irr_read_coords: num_nodes whitespace-separated "x y z" triples
+ * (moldyn/misc.c:224-246); a different count is IRR_ERR_STATE.
+ * irr_write_graph / irr_write_coords: the same formats from a 0-based half
+ * list (each pair on both endpoints' lines) and FP64 coordinates (%.17g). */
+IRR_API int irr_read_graph(const char *path, int64_t *num_nodes, int64_t *num_edges,
+                           int32_t *edges, int64_t cap, int one_based);
+IRR_API int irr_read_coords(const char *path, int64_t num_nodes, double *xyz);
+IRR_API int irr_write_graph(const char *path, int64_t num_nodes, const int32_t *edges,
+                            int64_t num_edges);
+IRR_API int irr_write_coords(const char *path, int64_t num_nodes, const double *xyz);
+
 /* ----------------------------------------------------- batched instances
  * Many independent instances reduced by ONE persistent launch per step: the
  * reference's per-part work queue (moldyn/irregular/gpu_kernel.cu:60-77)

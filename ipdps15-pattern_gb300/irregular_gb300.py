@@ -130,6 +130,10 @@ _SIGS = {
                                      C.POINTER(P), C.POINTER(I64)]),
     "irr_device_free": (C.c_int, [C.c_int, P]),
     "irr_morton_order_static": (C.c_int, [C.c_int, P, P, C.c_int, I64, P]),
+    "irr_read_graph": (C.c_int, [C.c_char_p, C.POINTER(I64), C.POINTER(I64), P, I64, C.c_int]),
+    "irr_read_coords": (C.c_int, [C.c_char_p, I64, P]),
+    "irr_write_graph": (C.c_int, [C.c_char_p, I64, P, I64]),
+    "irr_write_coords": (C.c_int, [C.c_char_p, I64, P]),
     "irr_batch_create": (C.c_int, [C.c_int, C.POINTER(P)]),
     "irr_batch_destroy": (C.c_int, [P]),
     "irr_batch_last_error": (C.c_char_p, [P]),
@@ -397,6 +401,43 @@ class Handle:
         self._check(load().irr_get_partition(self._h, _ptr(perm), _ptr(row_off), _ptr(col)),
                     "irr_get_partition")
         return perm, row_off, col[:m]
+
+
+def read_graph(path: str, one_based: bool = False) -> np.ndarray:
+    """moldyn's adjacency file -> (e, 2) int32 half list (irr_read_graph)."""
+    L = load()
+    n, e = C.c_int64(), C.c_int64()
+    p = os.fsencode(path)
+    rc = L.irr_read_graph(p, C.byref(n), C.byref(e), None, 0, int(one_based))
+    if rc not in (IRR_OK,):
+        raise IrregularError(rc, f"irr_read_graph({path}): {L.irr_status_string(rc).decode()}")
+    out = np.zeros((e.value, 2), np.int32)
+    rc = L.irr_read_graph(p, C.byref(n), C.byref(e), _ptr(out), e.value, int(one_based))
+    if rc != IRR_OK:
+        raise IrregularError(rc, f"irr_read_graph({path})")
+    return out
+
+
+def read_coords(path: str, num_nodes: int) -> np.ndarray:
+    out = np.zeros((num_nodes, 3), np.float64)
+    rc = load().irr_read_coords(os.fsencode(path), num_nodes, _ptr(out))
+    if rc != IRR_OK:
+        raise IrregularError(rc, f"irr_read_coords({path})")
+    return out
+
+
+def write_graph(path: str, num_nodes: int, edges) -> None:
+    e = np.ascontiguousarray(edges, np.int32).reshape(-1, 2)
+    rc = load().irr_write_graph(os.fsencode(path), num_nodes, _ptr(e), e.shape[0])
+    if rc != IRR_OK:
+        raise IrregularError(rc, f"irr_write_graph({path})")
+
+
+def write_coords(path: str, xyz) -> None:
+    a = np.ascontiguousarray(xyz, np.float64).reshape(-1, 3)
+    rc = load().irr_write_coords(os.fsencode(path), a.shape[0], _ptr(a))
+    if rc != IRR_OK:
+        raise IrregularError(rc, f"irr_write_coords({path})")
 
 
 class Batch:
