@@ -165,7 +165,11 @@ __device__ __forceinline__ double block_sum(double v, double* red)
     return v;
 }
 
-__global__ void kinetic_kernel(const double* __restrict__ v, int64_t n, double* acc)
+// Energies are summed in a fixed order (per-block partials, then one final
+// pass), so they are bitwise reproducible.
+constexpr int kEnergyBlocks = 1024;
+
+__global__ void kinetic_kernel(const double* __restrict__ v, int64_t n, double* part)
 {
     __shared__ double red[32];
     double s = 0.0;
@@ -173,14 +177,28 @@ __global__ void kinetic_kernel(const double* __restrict__ v, int64_t n, double* 
          i += (int64_t)gridDim.x * blockDim.x)
         s += v[3 * i] * v[3 * i] + v[3 * i + 1] * v[3 * i + 1] + v[3 * i + 2] * v[3 * i + 2];
     s = block_sum(s, red);
-    if (threadIdx.x == 0) atomicAdd(acc, 0.5 * s);
+    if (threadIdx.x == 0) part[3 * blockIdx.x] = 0.5 * s;
+}
+
+__global__ void energy_final_kernel(const double* __restrict__ part, int blocks, double* acc)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double k = 0.0, p = 0.0, w = 0.0;
+    for (int b = 0; b < blocks; b++) {
+        k += part[3 * b];
+        p += part[3 * b + 1];
+        w += part[3 * b + 2];
+    }
+    acc[0] = k;
+    acc[1] = p;
+    acc[2] = w;
 }
 
 // Potential energy 4(r^-12 - r^-6) and virial r.F = 48 r^2 s over every
 // directed entry (each pair counted twice, halved), FP32 per entry, FP64 sums.
 __global__ void potential_kernel(const float4* __restrict__ pos, const uint32_t* __restrict__ row_off,
                                  const int32_t* __restrict__ col, int64_t n, LawParams law,
-                                 double* acc)
+                                 double* part)
 {
     __shared__ double red[32];
     double pe = 0.0, vir = 0.0;
@@ -206,8 +224,8 @@ __global__ void potential_kernel(const float4* __restrict__ pos, const uint32_t*
     __syncthreads();
     vir = block_sum(vir, red);
     if (threadIdx.x == 0) {
-        atomicAdd(acc + 1, pe);
-        atomicAdd(acc + 2, vir);
+        part[3 * blockIdx.x + 1] = pe;
+        part[3 * blockIdx.x + 2] = vir;
     }
 }
 
@@ -387,7 +405,7 @@ int irr_md_create(const irr_md_config* cfg, const double* pos, const double* vel
     if (e == cudaSuccess) e = cudaMalloc(&m->d_inst, sizeof(InstDesc));
     if (e == cudaSuccess) e = cudaMalloc(&m->d_queue, sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc(&m->d_status, sizeof(int));
-    if (e == cudaSuccess) e = cudaMalloc(&m->d_acc, 4 * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&m->d_acc, (4 + 3 * kEnergyBlocks) * sizeof(double));
     if (e == cudaSuccess) e = cudaMemsetAsync(m->d_status, 0, sizeof(int), m->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(m->x, pos, b3, cudaMemcpyHostToDevice, m->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(m->v, vel, b3, cudaMemcpyHostToDevice, m->stream);
@@ -460,10 +478,12 @@ int irr_md_energy(irr_md* m, double* kinetic, double* potential, double* virial)
 {
     if (!m) return IRR_ERR_ARG;
     cudaSetDevice(m->device);
-    MD_CUDA(m, cudaMemsetAsync(m->d_acc, 0, 4 * sizeof(double), m->stream), "energy");
-    kinetic_kernel<<<grid_of(m->n) < 1024 ? grid_of(m->n) : 1024, 256, 0, m->stream>>>(m->v, m->n, m->d_acc);
-    potential_kernel<<<grid_of(m->n) < 2048 ? grid_of(m->n) : 2048, 256, 0, m->stream>>>(
-        m->pos4, m->part.row_off, m->part.col, m->n, m->law, m->d_acc);
+    const int blocks = grid_of(m->n) < kEnergyBlocks ? grid_of(m->n) : kEnergyBlocks;
+    double* part = m->d_acc + 4;
+    kinetic_kernel<<<blocks, 256, 0, m->stream>>>(m->v, m->n, part);
+    potential_kernel<<<blocks, 256, 0, m->stream>>>(m->pos4, m->part.row_off, m->part.col, m->n,
+                                                    m->law, part);
+    energy_final_kernel<<<1, 32, 0, m->stream>>>(part, blocks, m->d_acc);
     MD_CUDA(m, cudaGetLastError(), "energy kernels");
     double h[4];
     MD_CUDA(m, cudaMemcpyAsync(h, m->d_acc, sizeof(h), cudaMemcpyDeviceToHost, m->stream), "energy");

@@ -645,6 +645,9 @@ int orc_partition(int64_t n, const float *pos, const float lo[3], const float sc
         col[fill[aj]++] = ai;
     }
     free(fill);
+    /* Columns of each row ascending: the canonical (row, col) order. */
+    for (int64_t r = 0; r < n; r++)
+        qsort(col + row_off[r], (size_t)(row_off[r + 1] - row_off[r]), sizeof(int32_t), cmp_i32);
     return 0;
 }
 

@@ -120,8 +120,9 @@ void orc_morton_keys(int64_t n, const float *pos, const float lo[3], const float
                      uint32_t *keys);
 /* Full partition: stable sort by key (ties by node id) gives perm[new]=old
  * and inv[old]=new; every half edge (i, j) at list position t yields the
- * directed entries (inv[i] <- inv[j]) then (inv[j] <- inv[i]); a stable
- * bin of all entries by row gives row_off[n+1] and col[2e]. */
+ * directed entries (inv[i] <- inv[j]) and (inv[j] <- inv[i]); binning all
+ * entries by row gives row_off[n+1], and each row's columns are sorted
+ * ascending, so col[2e] is in (row, col) order whatever the edge order. */
 int orc_partition(int64_t n, const float *pos, const float lo[3], const float scale[3],
                   int64_t e, const int32_t *edges, int32_t *perm, int32_t *inv,
                   int64_t *row_off, int32_t *col);

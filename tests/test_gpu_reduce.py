@@ -89,6 +89,22 @@ def test_partitioned_is_bitwise_reproducible(built_lib, shape):
     assert np.array_equal(f1.view(np.uint32), f3.view(np.uint32))
 
 
+@pytest.mark.parametrize("shape", ["part", "part_g1", "part_noreorder"])
+def test_partitioned_result_ignores_edge_order(built_lib, shape):
+    """Rows are laid out in (row, col) order, so a shuffled edge list with
+    flipped endpoints gives the same bits."""
+    import irregular_gb300 as irr
+    c = dict(load_golden("moldyn_shuffled_dups_1500"))
+    f1, _ = run_case(irr, c, **SHAPES[shape])
+    rng = np.random.default_rng(11)
+    e = c["edges"][rng.permutation(c["edges"].shape[0])].copy()
+    flip = rng.random(e.shape[0]) < 0.5
+    e[flip] = e[flip][:, ::-1]
+    c["edges"] = e
+    f2, _ = run_case(irr, c, **SHAPES[shape])
+    assert np.array_equal(f1.view(np.uint32), f2.view(np.uint32))
+
+
 @pytest.mark.parametrize("exec_mode", [0, 1])
 def test_result_formats_agree(built_lib, exec_mode):
     import irregular_gb300 as irr

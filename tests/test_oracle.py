@@ -107,7 +107,7 @@ def test_partition_oracle_properties(oracle_lib):
     deg = np.bincount(inv[e[:, 0]], minlength=n) + np.bincount(inv[e[:, 1]], minlength=n)
     assert np.array_equal(np.diff(row_off), deg)
     assert row_off[-1] == 2 * e.shape[0]
-    # entry order within a row: (edge index, idx0 side first)
+    # entry order within a row: columns ascending (duplicate edges adjacent)
     r = int(np.argmax(deg))
     seq = []
     for t, (a, b) in enumerate(e):
@@ -115,4 +115,13 @@ def test_partition_oracle_properties(oracle_lib):
             seq.append(inv[b])
         if inv[b] == r:
             seq.append(inv[a])
-    assert np.array_equal(col[row_off[r]:row_off[r + 1]], np.array(seq, np.int32))
+    assert np.array_equal(col[row_off[r]:row_off[r + 1]], np.sort(np.array(seq, np.int32)))
+    for q in range(n):
+        assert np.all(np.diff(col[row_off[q]:row_off[q + 1]]) >= 0)
+    # the layout does not depend on the order of the edge list
+    rng = np.random.default_rng(5)
+    shuf = e[rng.permutation(e.shape[0])].copy()
+    flip = rng.random(e.shape[0]) < 0.5
+    shuf[flip] = shuf[flip][:, ::-1]
+    _, _, row_off2, col2 = O.partition(pos32, lo, scale, shuf)
+    assert np.array_equal(row_off2, row_off) and np.array_equal(col2, col)
