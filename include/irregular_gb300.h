@@ -80,6 +80,20 @@ enum irr_exec {
     IRR_EXEC_PARTITIONED = 1
 };
 
+/* Partitioned: how each node block's directed entries are laid out. */
+enum irr_layout {
+    /* Sliced when its padding is at most half the entry count, else CSR. */
+    IRR_LAYOUT_AUTO = 0,
+    /* Rows of entries (CSR), columns ascending within a row. */
+    IRR_LAYOUT_CSR = 1,
+    /* Slices of 32 / lanes_per_row consecutive rows, each row padded to the
+     * slice's longest (rounded up to 2 * lanes_per_row entries) and the
+     * slice's entries interleaved so that one warp's lanes read one
+     * contiguous, bank-conflict-free 256-byte line per step.  Same sums, in
+     * the same order, as CSR. */
+    IRR_LAYOUT_SLICED = 2
+};
+
 /* Node-data formats: the node_data_elm_size the reference passes. */
 enum irr_node_format {
     IRR_NODES_F32X3 = 12, /* float xyz                                              */
@@ -105,10 +119,11 @@ typedef struct irr_config {
                           32); 0 = tuned default                                     */
     int reorder;       /* partitioned: 1 = Morton order (default), 0 = keep the
                           caller's order (blocks are then cut from it)              */
-    int stage_smem;    /* partitioned: 1 = copy each block's positions into shared
-                          memory with a bulk (TMA) copy, 0 = read them through L1;
-                          -1 = tuned default                                         */
-    int reserved[8];
+    int stage_smem;    /* partitioned: 1 = copy each block's entries (neighbour ids)
+                          into a shared-memory ring with a bulk (TMA) copy, 0 = read
+                          them from global memory; -1 = tuned default               */
+    int layout;        /* partitioned: enum irr_layout                               */
+    int reserved[7];
 } irr_config;
 
 typedef struct irr_handle irr_handle;
@@ -124,6 +139,9 @@ typedef struct irr_info {
     int32_t lanes_per_row;
     int32_t stage_smem;
     int32_t exec;
+    int32_t layout;          /* enum irr_layout in use (CSR or SLICED)              */
+    int32_t reserved;
+    int64_t num_slots;       /* entry slots stored: num_entries plus padding        */
 } irr_info;
 
 IRR_API void irr_config_default(irr_config *cfg);

@@ -43,7 +43,6 @@ struct irr_batch {
     cudaGraphExec_t exec = nullptr;
     int64_t nodes = 0;
     int64_t edges = 0;
-    std::vector<std::vector<uint32_t>> row_offs;  // host copies, per instance
 };
 
 namespace {
@@ -74,13 +73,49 @@ void drop_graph(irr_batch* b)
     b->graph = nullptr;
 }
 
+// Rebuilds the instance table from the handles' current layouts.
+int upload_insts(irr_batch* b)
+{
+    std::vector<InstDesc> insts;
+    for (irr_handle* h : b->handles) {
+        InstDesc d{};
+        d.pos = h->d_pos;
+        d.row_off = h->part.row_off;
+        d.col = h->part.col;
+        d.force = h->d_force;
+        d.slice_off = h->sl.lanes ? h->sl.slice_off : nullptr;
+        d.scol = h->sl.lanes ? h->sl.col : nullptr;
+        d.law = h->law;
+        d.n = h->n;
+        insts.push_back(d);
+    }
+    if (!b->d_insts)
+        B_CUDA(b, cudaMalloc(&b->d_insts, sizeof(InstDesc) * insts.size()), "instance table");
+    B_CUDA(b, cudaMemcpy(b->d_insts, insts.data(), sizeof(InstDesc) * insts.size(), cudaMemcpyHostToDevice),
+           "instance table");
+    return IRR_OK;
+}
+
+// Every instance's layout for G lanes per row (each handle rebuilds its own
+// descriptor and items with it), then the batch's instance table.
+int set_lanes(irr_batch* b, int lanes)
+{
+    for (irr_handle* h : b->handles) {
+        if (h->shape.lanes_per_row == lanes) continue;  // already laid out for G
+        const int rc = irr_ensure_layout(h, lanes, h->shape.block_nodes);
+        if (rc) return bfail(b, rc, std::string("instance layout: ") + irr_last_error(h));
+    }
+    return upload_insts(b);
+}
+
 // Rebuilds the concatenated work-item list for `shape` and uploads it.
 int upload_items(irr_batch* b, const TiledShape& shape)
 {
     std::vector<WorkItem> items;
-    for (size_t k = 0; k < b->handles.size(); k++)
-        make_work_items(b->row_offs[k].data(), b->handles[k]->n, (int)k, shape.block_nodes,
-                        shape.stage_smem, items);
+    for (size_t k = 0; k < b->handles.size(); k++) {
+        const irr_handle* h = b->handles[k];
+        make_instance_items(h->host_row_off.data(), h->sl, h->n, (int)k, shape, items);
+    }
     if (b->d_items) cudaFree(b->d_items);
     b->d_items = nullptr;
     B_CUDA(b, cudaMalloc(&b->d_items, sizeof(WorkItem) * (items.empty() ? 1 : items.size())), "work items");
@@ -145,16 +180,19 @@ int autotune(irr_batch* b)
     {
         std::lock_guard<std::mutex> lock(g_tune_mutex);
         auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) b->shape = it->second;
         if (it != g_tune_cache.end()) {
-            b->shape = it->second;
-            return upload_items(b, b->shape);
+            const int rc = set_lanes(b, b->shape.lanes_per_row);
+            return rc ? rc : upload_items(b, b->shape);
         }
     }
     const int lanes[] = {4, 8, 16};
     const int rows[] = {64, 256, 1024};
     TiledShape best = b->shape;
     double best_ms = 1e30;
-    for (int g : lanes)
+    for (int g : lanes) {
+        const int rc = set_lanes(b, g);
+        if (rc) return rc;
         for (int r : rows) {
             TiledShape s = b->shape;
             s.lanes_per_row = g;
@@ -166,12 +204,14 @@ int autotune(irr_batch* b)
                 best = s;
             }
         }
+    }
     b->shape = best;
     {
         std::lock_guard<std::mutex> lock(g_tune_mutex);
         g_tune_cache[key] = best;
     }
-    return upload_items(b, b->shape);
+    const int rc = set_lanes(b, b->shape.lanes_per_row);
+    return rc ? rc : upload_items(b, b->shape);
 }
 
 }  // namespace
@@ -253,30 +293,14 @@ int irr_batch_finalize(irr_batch* b, int autotune_shape)
     if (b->finalized) return IRR_OK;
     if (b->handles.empty()) return bfail(b, IRR_ERR_STATE, "empty batch");
     cudaSetDevice(b->device);
-    std::vector<InstDesc> insts;
-    b->row_offs.clear();
     b->nodes = b->edges = 0;
     for (irr_handle* h : b->handles) {
         cudaStreamSynchronize(h->stream);
-        InstDesc d{};
-        d.pos = h->d_pos;
-        d.row_off = h->part.row_off;
-        d.col = h->part.col;
-        d.force = h->d_force;
-        d.law = h->law;
-        d.n = h->n;
-        insts.push_back(d);
-        std::vector<uint32_t> ro((size_t)h->n + 1);
-        B_CUDA(b, cudaMemcpy(ro.data(), h->part.row_off, sizeof(uint32_t) * (h->n + 1), cudaMemcpyDeviceToHost),
-               "row offsets");
-        b->row_offs.push_back(std::move(ro));
         b->nodes += h->n;
         b->edges += h->e;
     }
-    B_CUDA(b, cudaMalloc(&b->d_insts, sizeof(InstDesc) * insts.size()), "instance table");
-    B_CUDA(b, cudaMemcpy(b->d_insts, insts.data(), sizeof(InstDesc) * insts.size(), cudaMemcpyHostToDevice),
-           "instance table");
-    int rc = autotune_shape ? autotune(b) : upload_items(b, b->shape);
+    int rc = autotune_shape ? autotune(b) : set_lanes(b, b->shape.lanes_per_row);
+    if (!rc && !autotune_shape) rc = upload_items(b, b->shape);
     if (rc) return rc;
     b->finalized = true;
     return IRR_OK;
@@ -363,20 +387,8 @@ int irr_autotune(irr_handle* h)
     rc = irr_batch_add(b, h);
     if (!rc) rc = irr_batch_finalize(b, 1);
     if (!rc) {
-        h->shape.lanes_per_row = b->shape.lanes_per_row;
-        h->shape.block_nodes = b->shape.block_nodes;
-        // the handle's own work items for the chosen rows per item
-        std::vector<WorkItem> items;
-        make_work_items(b->row_offs[0].data(), h->n, 0, h->shape.block_nodes, h->shape.stage_smem, items);
-        if (h->d_items) cudaFree(h->d_items);
-        h->d_items = nullptr;
-        if (cudaMalloc(&h->d_items, sizeof(WorkItem) * (items.empty() ? 1 : items.size())) != cudaSuccess ||
-            (!items.empty() && cudaMemcpy(h->d_items, items.data(), sizeof(WorkItem) * items.size(),
-                                          cudaMemcpyHostToDevice) != cudaSuccess)) {
-            cudaGetLastError();
-            rc = IRR_ERR_CUDA;
-        }
-        h->num_items = (int)items.size();
+        // the handle's own layout and work items for the chosen shape
+        rc = irr_ensure_layout(h, b->shape.lanes_per_row, b->shape.block_nodes);
     } else {
         h->err = std::string("autotune: ") + b->err;
     }

@@ -57,6 +57,8 @@ void free_layout(irr_handle* h)
     dfree(h->part.inv);
     dfree(h->part.row_off);
     dfree(h->part.col);
+    free_sliced(&h->sl);
+    h->host_row_off.clear();
     dfree(h->d_inst);
     dfree(h->d_items);
     h->num_items = 0;
@@ -126,11 +128,28 @@ int upload_inst(irr_handle* h)
     d.row_off = h->part.row_off;
     d.col = h->part.col;
     d.force = h->d_force;
+    d.slice_off = h->sl.lanes ? h->sl.slice_off : nullptr;
+    d.scol = h->sl.lanes ? h->sl.col : nullptr;
     d.law = h->law;
     d.n = h->n;
     H_CUDA(h, cudaMemcpyAsync(h->d_inst, &d, sizeof(d), cudaMemcpyHostToDevice, h->stream),
            "upload instance descriptor");
     H_CUDA(h, cudaStreamSynchronize(h->stream), "upload instance descriptor");
+    return IRR_OK;
+}
+
+int upload_items(irr_handle* h)
+{
+    std::vector<WorkItem> items;
+    make_instance_items(h->host_row_off.data(), h->sl, h->n, 0, h->shape, items);
+    dfree(h->d_items);
+    h->num_items = 0;
+    H_CUDA(h, cudaMalloc(&h->d_items, sizeof(WorkItem) * (items.size() ? items.size() : 1)), "allocate work items");
+    if (!items.empty())
+        H_CUDA(h, cudaMemcpyAsync(h->d_items, items.data(), sizeof(WorkItem) * items.size(),
+                                  cudaMemcpyHostToDevice, h->stream), "upload work items");
+    H_CUDA(h, cudaStreamSynchronize(h->stream), "upload work items");
+    h->num_items = (int)items.size();
     return IRR_OK;
 }
 
@@ -214,6 +233,40 @@ int set_edges_common(irr_handle* h, const int32_t* src, int64_t e, cudaMemcpyKin
 
 }  // namespace
 
+int irr_ensure_layout(irr_handle* h, int lanes_per_row, int block_nodes)
+{
+    if (!h || !h->inited || h->cfg.exec != IRR_EXEC_PARTITIONED) return IRR_ERR_STATE;
+    cudaSetDevice(h->device);
+    H_CUDA(h, cudaStreamSynchronize(h->stream), "layout");  // no launch may use the old layout
+    const int64_t n = h->n, e = h->e;
+    h->shape.lanes_per_row = lanes_per_row;
+    h->shape.block_nodes = block_nodes;
+    const int want = h->cfg.layout;
+    if (want == IRR_LAYOUT_CSR) {
+        free_sliced(&h->sl);
+    } else if (h->sl.lanes != lanes_per_row) {
+        const cudaError_t se = build_sliced(h->part.row_off, h->part.col, n, lanes_per_row, &h->sl, h->stream);
+        if (se != cudaSuccess) {
+            cudaGetLastError();
+            free_sliced(&h->sl);
+            if (want == IRR_LAYOUT_SLICED)
+                return se == cudaErrorInvalidValue
+                           ? fail(h, IRR_ERR_CAPACITY, "sliced layout above 2^32 words")
+                           : cuda_fail(h, se, "build sliced layout");
+        } else if (want == IRR_LAYOUT_AUTO && !sliced_pays(h->sl, 2 * e)) {
+            free_sliced(&h->sl);
+        }
+    }
+    int rc = upload_inst(h);
+    if (rc) return rc;
+    rc = upload_items(h);
+    if (rc) return rc;
+    h->dev_bytes = 2 * (int64_t)(n > 0 ? n : 1) * (int64_t)sizeof(float4) + (int64_t)h->raw_cap +
+                   (int64_t)(2 * n + n + 1) * 4 + 2 * e * 4 +
+                   (h->sl.lanes ? 4 * (h->sl.words + h->sl.slices + 1) : 0);
+    return IRR_OK;
+}
+
 extern "C" {
 
 void irr_config_default(irr_config* cfg)
@@ -260,6 +313,7 @@ int irr_create(const irr_config* cfg, irr_handle** out)
     if (c.map_idx < IRR_MAP_LJ_MOLDYN || c.map_idx > IRR_MAP_LJ_MINIMD_PBC) return IRR_ERR_ARG;
     if (c.block_nodes != 0 && (c.block_nodes < 64 || c.block_nodes > 4096 || (c.block_nodes & (c.block_nodes - 1))))
         return IRR_ERR_ARG;
+    if (c.layout < IRR_LAYOUT_AUTO || c.layout > IRR_LAYOUT_SLICED) return IRR_ERR_ARG;
     if (c.lanes_per_row != 0 && c.lanes_per_row != 1 && c.lanes_per_row != 2 && c.lanes_per_row != 4 &&
         c.lanes_per_row != 8 && c.lanes_per_row != 16 && c.lanes_per_row != 32)
         return IRR_ERR_ARG;
@@ -430,23 +484,15 @@ int irr_init(irr_handle* h)
     H_CUDA(h, launch_load_nodes(h->d_raw, h->raw_elm, h->part.perm, n, h->d_pos, s), "gather node data");
     h->raw_pending = false;
     // node blocks -> work items (cut on the row offsets)
-    std::vector<uint32_t> ro((size_t)n + 1);
-    H_CUDA(h, cudaMemcpyAsync(ro.data(), h->part.row_off, sizeof(uint32_t) * (n + 1), cudaMemcpyDeviceToHost, s),
-           "copy row offsets");
+    h->host_row_off.resize((size_t)n + 1);
+    H_CUDA(h, cudaMemcpyAsync(h->host_row_off.data(), h->part.row_off, sizeof(uint32_t) * (n + 1),
+                              cudaMemcpyDeviceToHost, s), "copy row offsets");
     H_CUDA(h, cudaStreamSynchronize(s), "copy row offsets");
-    std::vector<WorkItem> items;
-    make_work_items(ro.data(), n, 0, h->shape.block_nodes, h->shape.stage_smem, items);
-    h->num_items = (int)items.size();
-    H_CUDA(h, cudaMalloc(&h->d_items, sizeof(WorkItem) * (items.size() ? items.size() : 1)), "allocate work items");
-    if (!items.empty())
-        H_CUDA(h, cudaMemcpyAsync(h->d_items, items.data(), sizeof(WorkItem) * items.size(),
-                                  cudaMemcpyHostToDevice, s), "upload work items");
     H_CUDA(h, cudaMalloc(&h->d_inst, sizeof(InstDesc)), "allocate instance descriptor");
     h->shape.periodic = h->law.periodic;
     h->inited = true;
-    rc = upload_inst(h);
+    rc = irr_ensure_layout(h, h->shape.lanes_per_row, h->shape.block_nodes);
     if (rc) return rc;
-    h->dev_bytes += (int64_t)(2 * n + n + 1) * 4 + 2 * e * 4;
     // the half list is not needed by the partitioned kernel
     dfree(h->d_edges);
     h->edges_cap = 0;
@@ -528,6 +574,8 @@ int irr_get_info(const irr_handle* h, irr_info* info)
     info->lanes_per_row = h->shape.lanes_per_row;
     info->stage_smem = h->shape.stage_smem;
     info->exec = h->cfg.exec;
+    info->layout = h->sl.lanes ? IRR_LAYOUT_SLICED : IRR_LAYOUT_CSR;
+    info->num_slots = h->sl.lanes ? h->sl.words : info->num_entries;
     return IRR_OK;
 }
 

@@ -40,6 +40,8 @@ struct irr_handle {
     float4* d_pos = nullptr;     // execution order
     float4* d_force = nullptr;
     PartitionOut part{};
+    std::vector<uint32_t> host_row_off;  // host copy of part.row_off (cuts work items)
+    irr::Sliced sl{};                    // sliced layout, when in use
     InstDesc* d_inst = nullptr;
     WorkItem* d_items = nullptr;
     int num_items = 0;
@@ -50,3 +52,7 @@ struct irr_handle {
     int64_t dev_bytes = 0;
 };
 
+// (Re)builds the handle's entry layout for G lanes per row as its config asks
+// (sliced or CSR), then its instance descriptor and work items, so that the
+// three always agree.  Partitioned, initialised handles only.
+int irr_ensure_layout(irr_handle* h, int lanes_per_row, int block_nodes);

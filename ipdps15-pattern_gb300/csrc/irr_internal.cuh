@@ -23,12 +23,16 @@ struct InstDesc {
     const uint32_t* row_off;  // n + 1 entry offsets
     const int32_t* col;       // neighbour of each directed entry (instance-local id)
     float4* force;            // per-node result, execution order
+    const uint32_t* slice_off;  // sliced layout: word offset of each slice (or null)
+    const int32_t* scol;        // sliced layout: interleaved, padded entries
     LawParams law;
     int64_t n;
 };
 
 // One node block: rows [row0, row0 + nrows) of instance `inst`, whose
-// directed entries are [ent0, ent0 + nent) of the instance's col array.
+// directed entries are [ent0, ent0 + nent) of the instance's col array (or,
+// with kItemSliced, words [ent0, ent0 + nent) of its sliced array: whole
+// slices, so row0 is a multiple of the slice height).
 struct WorkItem {
     int32_t inst;
     int32_t row0;
@@ -38,7 +42,24 @@ struct WorkItem {
     uint32_t nent;
 };
 
-enum : int { kItemDirect = 1 };
+enum : int { kItemDirect = 1, kItemSliced = 2 };
+
+// Sliced entry layout of one instance, for G lanes per row.  A slice is
+// R = 32 / G consecutive rows; each row is padded to the slice's longest row
+// rounded up to 2G entries, so a slice is T = ceil(maxlen / 2G) steps of 64
+// words.  In step t, lane i*G + l of a warp handles entries (2Gt + l,
+// 2Gt + G + l) of row i, read together as the int2 at word 64t + 2(iG + l):
+// the warp reads one contiguous 256-byte line, the same entry pairs the CSR
+// path gives that lane, in the same order.  Padding words hold the row's
+// own id (0 past the last row).
+struct Sliced {
+    uint32_t* slice_off = nullptr;   // [slices + 1] word offsets (multiples of 64)
+    int32_t* col = nullptr;          // [words]
+    int64_t slices = 0;
+    int64_t words = 0;
+    int lanes = 0;                   // G it was built for; 0 = not built
+    std::vector<uint32_t> host_off;  // host copy of slice_off (cuts work items)
+};
 
 struct TiledShape {
     int lanes_per_row;   // 4, 8, 16 or 32
@@ -53,21 +74,46 @@ struct TiledShape {
 #define IRR_STAGES 2
 #endif
 #ifndef IRR_STAGE_ENTRIES
-#define IRR_STAGE_ENTRIES 4096
+#define IRR_STAGE_ENTRIES 5120
 #endif
 #ifndef IRR_CTAS_PER_SM
 #define IRR_CTAS_PER_SM 4
 #endif
 constexpr int kTiledThreads = 256;
 constexpr int kStages = IRR_STAGES;              // shared-memory ring depth
-constexpr int kStageEntries = IRR_STAGE_ENTRIES; // entries per stage (16 KB at 4096)
+constexpr int kStageEntries = IRR_STAGE_ENTRIES; // entries per stage (20 KB at 5120)
 constexpr int kColPad = 4;                       // entries allocated past the end of col
 constexpr int kCtasPerSm = IRR_CTAS_PER_SM;      // resident CTAs per SM (registers, ring)
 
 // Cuts rows [0, n) into work items of at most max_rows rows and (unless a
-// single row is longer) at most kStageEntries entries.  row_off: host copy.
+// single row is longer) at most kStageEntries entries, at a multiple of
+// `round_rows` rows (the consumer warps' row groups) where that fits.
+// row_off: host copy.
 void make_work_items(const uint32_t* row_off, int64_t n, int inst, int max_rows, int staged,
-                     std::vector<WorkItem>& out);
+                     std::vector<WorkItem>& out, int round_rows = 1);
+// The same for a sliced layout: whole slices, at most max_rows rows and
+// kStageEntries words per item (a longer slice is read from global memory),
+// cut at multiples of kConsumerSlices slices where that fits.
+void make_sliced_items(const Sliced& sl, int64_t n, int inst, int max_rows, int staged,
+                       std::vector<WorkItem>& out);
+constexpr int kConsumerSlices = 8;  // consumer warps of the tiled kernel
+// One instance's items for `shape`: sliced items if sl was built for
+// shape.lanes_per_row, else CSR items from the host row offsets.
+void make_instance_items(const uint32_t* host_row_off, const Sliced& sl, int64_t n, int inst,
+                         const TiledShape& shape, std::vector<WorkItem>& out);
+
+// -- sliced layout (irr_partition.cu) --
+// Builds sl for G lanes per row from a CSR (row_off, col) of n rows on the
+// device; synchronises s (the host keeps the slice offsets).  Fails with
+// cudaErrorInvalidValue if the layout would exceed 2^32 - 1 words.
+cudaError_t build_sliced(const uint32_t* row_off, const int32_t* col, int64_t n, int G,
+                         Sliced* sl, cudaStream_t s);
+void free_sliced(Sliced* sl);
+// The automatic choice: sliced when padding adds at most half the entries.
+inline bool sliced_pays(const Sliced& sl, int64_t entries)
+{
+    return sl.words <= entries + entries / 2 + 64;
+}
 
 // -- reduction kernels (irr_reduce.cu) --
 cudaError_t launch_plain(const float4* pos, const int2* edges, int64_t e, float4* force,

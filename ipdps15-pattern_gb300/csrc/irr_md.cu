@@ -236,6 +236,7 @@ void free_part(irr_md* m)
     if (m->part.row_off) cudaFree(m->part.row_off);
     if (m->part.col) cudaFree(m->part.col);
     m->part = PartitionOut{};
+    free_sliced(&m->sl);
     if (m->d_items) cudaFree(m->d_items);
     m->d_items = nullptr;
     m->num_items = 0;
@@ -274,8 +275,14 @@ int md_rebuild(irr_md* m)
     MD_CUDA(m, cudaMemcpyAsync(ro.data(), m->part.row_off, sizeof(uint32_t) * (m->n + 1),
                                cudaMemcpyDeviceToHost, s), "row offsets");
     MD_CUDA(m, cudaStreamSynchronize(s), "row offsets");
+    if (build_sliced(m->part.row_off, m->part.col, m->n, m->shape.lanes_per_row, &m->sl, s) != cudaSuccess) {
+        cudaGetLastError();
+        free_sliced(&m->sl);  // CSR
+    } else if (!sliced_pays(m->sl, 2 * e)) {
+        free_sliced(&m->sl);
+    }
     std::vector<WorkItem> items;
-    make_work_items(ro.data(), m->n, 0, m->shape.block_nodes, m->shape.stage_smem, items);
+    make_instance_items(ro.data(), m->sl, m->n, 0, m->shape, items);
     m->num_items = (int)items.size();
     MD_CUDA(m, cudaMalloc(&m->d_items, sizeof(WorkItem) * (items.empty() ? 1 : items.size())), "work items");
     if (!items.empty())
@@ -286,6 +293,8 @@ int md_rebuild(irr_md* m)
     d.row_off = m->part.row_off;
     d.col = m->part.col;
     d.force = m->force;
+    d.slice_off = m->sl.lanes ? m->sl.slice_off : nullptr;
+    d.scol = m->sl.lanes ? m->sl.col : nullptr;
     d.law = m->law;
     d.n = m->n;
     MD_CUDA(m, cudaMemcpyAsync(m->d_inst, &d, sizeof(d), cudaMemcpyHostToDevice, s), "instance");
@@ -329,6 +338,8 @@ InstDesc md_instance(const irr_md* m)
     d.row_off = m->part.row_off;
     d.col = m->part.col;
     d.force = m->force;
+    d.slice_off = m->sl.lanes ? m->sl.slice_off : nullptr;
+    d.scol = m->sl.lanes ? m->sl.col : nullptr;
     d.law = m->law;
     d.n = m->n;
     return d;

@@ -30,6 +30,7 @@ struct irr_md {
     int32_t* ids = nullptr;    // execution slot -> caller's atom id
     int32_t* ids_tmp = nullptr;
     PartitionOut part{};
+    irr::Sliced sl{};          // sliced entry layout (when it pays)
     InstDesc* d_inst = nullptr;
     WorkItem* d_items = nullptr;
     int num_items = 0;

@@ -10,10 +10,13 @@
 //      box frame (float ops, each rounded), bits interleaved;
 //   2. stable LSD radix sort of (key, node) -> perm[new] = old, inv[old] = new;
 //   3. every half edge (i, j) at list position t becomes the directed entries
-//      (inv[i] <- inv[j]) and (inv[j] <- inv[i]); a stable radix sort by row
-//      bins them, and a degree count + scan gives the row offsets.
+//      (inv[i] <- inv[j]) and (inv[j] <- inv[i]); stable radix sorts by
+//      column, then by row, put them in (row, col) order, and a degree
+//      count + scan gives the row offsets.
 // Node blocks are then consecutive ranges of rows.  Every output is an
 // integer function of the inputs, reproduced bit for bit by the CPU oracle.
+// 4. Optionally the sliced layout (struct Sliced): the same entries regrouped
+//    so that one warp reads one contiguous line per step.
 #include <algorithm>
 
 #include "irr_internal.cuh"
@@ -320,6 +323,52 @@ cudaError_t alloc_async(T** p, int64_t count, cudaStream_t s)
                            s);
 }
 
+// ------------------------------------------------------- sliced layout
+// words[q] = 64 * ceil(longest row of slice q / 2G); *total += words[q] (64-bit,
+// so an overflowing layout is seen by the host before the 32-bit scan is used).
+__global__ void slice_words_kernel(const uint32_t* row_off, int64_t n, int G, int64_t slices,
+                                   uint32_t* words, unsigned long long* total)
+{
+    const int R = 32 / G;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < slices;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        uint32_t longest = 0;
+        const int64_t r0 = q * R;
+        const int64_t r1 = r0 + R < n ? r0 + R : n;
+        for (int64_t r = r0; r < r1; r++) {
+            const uint32_t len = row_off[r + 1] - row_off[r];
+            longest = len > longest ? len : longest;
+        }
+        const unsigned long long w = 64ull * ((longest + 2ull * G - 1) / (2ull * G));
+        words[q] = (uint32_t)w;
+        atomicAdd(total, w);
+    }
+}
+
+// One thread per row slot (rows past n are empty): writes the row's T * 2G
+// words of its slice, entries then padding.  A padding word holds the row's
+// own id (0 for a row past n), so the kernel's gathers need no predicate:
+// a padded slot reads its own position, d = 0, and is masked to 0.
+__global__ void slice_fill_kernel(const uint32_t* row_off, const int32_t* col, int64_t n, int G,
+                                  int64_t slices, const uint32_t* slice_off, int32_t* out)
+{
+    const int R = 32 / G;
+    const int64_t rows = slices * R;
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows;
+         r += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t q = r / R;
+        const int i = (int)(r - q * R);
+        const uint32_t o = slice_off[q];
+        const uint32_t slots = (slice_off[q + 1] - o) / 64u * (2u * G);
+        const uint32_t beg = r < n ? row_off[r] : 0u;
+        const uint32_t len = r < n ? row_off[r + 1] - beg : 0u;
+        for (uint32_t k = 0; k < slots; k++) {
+            const uint32_t t = k / (2u * G), h = (k / G) & 1u, l = k % G;
+            out[o + 64u * t + 2u * (i * G + l) + h] = k < len ? col[beg + k] : (r < n ? (int32_t)r : 0);
+        }
+    }
+}
+
 }  // namespace
 
 cudaError_t scan_exclusive_u32(const uint32_t* in, uint32_t* out, int64_t n, uint32_t* d_total,
@@ -483,6 +532,67 @@ cudaError_t build_partition(const float4* pos_user, int64_t n, const int2* edges
     }
     IRR_CUDA_TRY(scan_exclusive_u32(deg, out->row_off, n + 1, nullptr, s));
     return cudaSuccess;
+}
+
+cudaError_t build_sliced(const uint32_t* row_off, const int32_t* col, int64_t n, int G,
+                         Sliced* sl, cudaStream_t s)
+{
+    free_sliced(sl);
+    if (n < 0 || (G != 1 && G != 2 && G != 4 && G != 8 && G != 16 && G != 32))
+        return cudaErrorInvalidValue;
+    const int R = 32 / G;
+    const int64_t slices = (n + R - 1) / R;
+    uint32_t* words = nullptr;
+    unsigned long long* d_total = nullptr;
+    IRR_CUDA_TRY(alloc_async(&sl->slice_off, slices + 1, s));
+    IRR_CUDA_TRY(alloc_async(&words, slices + 1, s));
+    IRR_CUDA_TRY(alloc_async(&d_total, 1, s));
+    IRR_CUDA_TRY(cudaMemsetAsync(words, 0, sizeof(uint32_t) * (size_t)(slices + 1), s));
+    IRR_CUDA_TRY(cudaMemsetAsync(d_total, 0, sizeof(unsigned long long), s));
+    if (slices > 0) {
+        slice_words_kernel<<<grid_for(slices), 256, 0, s>>>(row_off, n, G, slices, words, d_total);
+        IRR_CUDA_TRY(cudaGetLastError());
+    }
+    unsigned long long total = 0;
+    IRR_CUDA_TRY(cudaMemcpyAsync(&total, d_total, sizeof(total), cudaMemcpyDeviceToHost, s));
+    IRR_CUDA_TRY(cudaStreamSynchronize(s));
+    cudaError_t err = cudaSuccess;
+    if (total > 0xffffffffull) err = cudaErrorInvalidValue;
+    if (err == cudaSuccess) err = scan_exclusive_u32(words, sl->slice_off, slices + 1, nullptr, s);
+    if (err == cudaSuccess) err = alloc_async(&sl->col, (int64_t)total, s);
+    if (err == cudaSuccess && slices > 0) {
+        slice_fill_kernel<<<grid_for(slices * R), 256, 0, s>>>(row_off, col, n, G, slices,
+                                                               sl->slice_off, sl->col);
+        err = cudaGetLastError();
+    }
+    if (err == cudaSuccess) {
+        sl->host_off.resize((size_t)slices + 1);
+        err = cudaMemcpyAsync(sl->host_off.data(), sl->slice_off,
+                              sizeof(uint32_t) * (size_t)(slices + 1), cudaMemcpyDeviceToHost, s);
+    }
+    cudaFreeAsync(words, s);
+    cudaFreeAsync(d_total, s);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(s);
+    if (err != cudaSuccess) {
+        free_sliced(sl);
+        return err;
+    }
+    sl->slices = slices;
+    sl->words = (int64_t)total;
+    sl->lanes = G;
+    return cudaSuccess;
+}
+
+void free_sliced(Sliced* sl)
+{
+    if (sl->slice_off) cudaFree(sl->slice_off);
+    if (sl->col) cudaFree(sl->col);
+    sl->slice_off = nullptr;
+    sl->col = nullptr;
+    sl->slices = sl->words = 0;
+    sl->lanes = 0;
+    sl->host_off.clear();
+    sl->host_off.shrink_to_fit();
 }
 
 cudaError_t launch_load_nodes(const void* raw, int elm_size, const int32_t* perm, int64_t n,

@@ -21,6 +21,14 @@
 //   per item moves them into a ring of shared-memory stages a few items
 //   ahead of the consumers: the entry stream, which is most of the traffic,
 //   is kept in flight while positions are gathered through L1.
+//   Entries come in one of two layouts.  CSR rows (consume_item): the rows
+//   of a warp start at unrelated offsets, so its reads of the stage collide
+//   in shared-memory banks.  Slices (consume_sliced, struct Sliced): the
+//   rows of a warp are interleaved and padded, so each step of the warp is
+//   one contiguous 256-byte read and the trip count is uniform; with Morton-
+//   ordered rows whose columns ascend, the lanes of one gather also land on
+//   few cache lines.
+#include <algorithm>
 #include <vector>
 
 #include "irr_internal.cuh"
@@ -136,13 +144,13 @@ __device__ __forceinline__ float rd_of(float dx, float dy, float dz)
 // Two entries (b0, b1) of the row of node a, evaluated with packed FP32x2
 // arithmetic (each half rounds exactly as the scalar law in irr_law.cuh), and
 // accumulated into the lane's packed partials.  An unused slot passes b == a
-// and v1 == false: d = 0 and its scalar is replaced by 0.
+// and v == false: d = 0 and its scalar is replaced by 0.
 //
 // A component |d| > side/2 implies rd > (side/2)^2, so the wrap test is one
 // compare on rd; a pair that fails it is re-examined exactly (rare: only a
 // pair across the box wall or beyond half the box).
 template <bool PERIODIC>
-__device__ __forceinline__ void lj_pair(float4 a, float4 b0, float4 b1, bool v1, const HotLaw& H,
+__device__ __forceinline__ void lj_pair(float4 a, float4 b0, float4 b1, bool v0, bool v1, const HotLaw& H,
                                         const LawParams* __restrict__ cold, float2& ax, float2& ay,
                                         float2& az)
 {
@@ -179,29 +187,18 @@ __device__ __forceinline__ void lj_pair(float4 a, float4 b0, float4 b1, bool v1,
     r = __ffma2_rn(r, e, r);                                     // rd^-1 (one Newton step)
     const float2 r2 = __fmul2_rn(r, r);                          // rd^-2
     float2 s = __fmul2_rn(__fmul2_rn(r2, r2), __ffma2_rn(r2, r, make_float2(-0.5f, -0.5f)));
-    s.x = in0 ? s.x : 0.0f;
+    s.x = (in0 && v0) ? s.x : 0.0f;
     s.y = (in1 && v1) ? s.y : 0.0f;
     ax = __ffma2_rn(dx, s, ax);
     ay = __ffma2_rn(dy, s, ay);
     az = __ffma2_rn(dz, s, az);
 }
 
-// One row: G lanes; each lane takes entry pairs (k, k + G) with stride 2G.
-// Partials: two per lane (the packed halves), joined by TwoSum, then the G
-// lanes by a TwoSum butterfly.  Entry k of the row is cols[k - shift].
-template <bool PERIODIC, int G>
-__device__ __forceinline__ float3 row_sum(const float4* __restrict__ pos, const int32_t* cols,
-                                          uint32_t shift, float4 a, uint32_t beg, uint32_t end,
-                                          int lane, const HotLaw& H,
-                                          const LawParams* __restrict__ cold)
+// The row's result from its G lanes' packed partials: the two halves of each
+// lane joined by TwoSum, then the G lanes by a TwoSum butterfly.
+template <int G>
+__device__ __forceinline__ float3 join_partials(float2 ax, float2 ay, float2 az)
 {
-    float2 ax = make_float2(0.f, 0.f), ay = ax, az = ax;
-    for (uint32_t k = beg + lane; k < end; k += 2 * G) {
-        const bool v1 = k + G < end;
-        const float4 b0 = __ldg(pos + cols[k - shift]);
-        const float4 b1 = v1 ? __ldg(pos + cols[k + G - shift]) : a;
-        lj_pair<PERIODIC>(a, b0, b1, v1, H, cold, ax, ay, az);
-    }
     float hx, hy, hz, cx, cy, cz;
     two_sum(ax.x, ax.y, hx, cx);
     two_sum(ay.x, ay.y, hy, cy);
@@ -225,7 +222,25 @@ __device__ __forceinline__ float3 row_sum(const float4* __restrict__ pos, const 
     return make_float3(__fadd_rn(hx, cx), __fadd_rn(hy, cy), __fadd_rn(hz, cz));
 }
 
-constexpr int kConsumerWarps = 8;
+// One row: G lanes; each lane takes entry pairs (k, k + G) with stride 2G.
+// Entry k of the row is cols[k - shift].
+template <bool PERIODIC, int G>
+__device__ __forceinline__ float3 row_sum(const float4* __restrict__ pos, const int32_t* cols,
+                                          uint32_t shift, float4 a, uint32_t beg, uint32_t end,
+                                          int lane, const HotLaw& H,
+                                          const LawParams* __restrict__ cold)
+{
+    float2 ax = make_float2(0.f, 0.f), ay = ax, az = ax;
+    for (uint32_t k = beg + lane; k < end; k += 2 * G) {
+        const bool v1 = k + G < end;
+        const float4 b0 = __ldg(pos + cols[k - shift]);
+        const float4 b1 = v1 ? __ldg(pos + cols[k + G - shift]) : a;
+        lj_pair<PERIODIC>(a, b0, b1, true, v1, H, cold, ax, ay, az);
+    }
+    return join_partials<G>(ax, ay, az);
+}
+
+constexpr int kConsumerWarps = kConsumerSlices;
 constexpr int kPipeThreads = (kConsumerWarps + 1) * 32;
 
 // The rows of one work item that belong to consumer warp `cw`.
@@ -260,6 +275,72 @@ __device__ __forceinline__ void consume_item(const WorkItem& w, const InstDesc* 
         }
         const float3 f = row_sum<PERIODIC, G>(pos, cols, shift, a, beg, end, lane, H, cold);
         if (valid && lane == 0) force[r] = make_float4(f.x, f.y, f.z, 0.f);
+    }
+}
+
+// One lane's entry pair of a slice step, as a single 8-byte load (kept whole
+// so the two halves are not split into separately predicated loads).  The
+// shared form is volatile: it must stay after the stage's mbarrier wait
+// (itself volatile asm), which the compiler could otherwise move it across.
+template <bool SHARED>
+__device__ __forceinline__ int2 load_pair(const int2* p)
+{
+    int2 c;
+    if (SHARED)
+        asm volatile("ld.shared.v2.b32 {%0, %1}, [%2];" : "=r"(c.x), "=r"(c.y) : "r"(smem_u32(p)));
+    else
+        asm("ld.global.nc.v2.b32 {%0, %1}, [%2];" : "=r"(c.x), "=r"(c.y) : "l"(p));
+    return c;
+}
+
+// The slices of a sliced work item that belong to consumer warp `cw` (one
+// slice per warp at a time: lane i*G + l serves row i of the slice).  Word w
+// of the instance's sliced array is words[w - shift] (shared memory when
+// SHARED).  Each step is one 8-byte load per lane of a contiguous 256-byte
+// line; the trip count is the slice's, uniform across the warp, and slots
+// past a row's end (padding: the row's own id) are masked.
+template <bool PERIODIC, int G, bool SHARED>
+__device__ __forceinline__ void consume_sliced(const WorkItem& w, const InstDesc* __restrict__ insts,
+                                               const int32_t* words, uint32_t shift, int cw,
+                                               int lane32)
+{
+    constexpr int R = 32 / G;
+    const int lane = lane32 % G;
+    const InstDesc* __restrict__ I = insts + w.inst;
+    const float4* __restrict__ pos = I->pos;
+    const uint32_t* __restrict__ row_off = I->row_off;
+    const uint32_t* __restrict__ slice_off = I->slice_off;
+    float4* __restrict__ force = I->force;
+    const LawParams* __restrict__ cold = &I->law;
+    const int64_t n = I->n;
+    HotLaw H;
+    H.half2 = I->law.half2;
+    H.rc2 = I->law.rc2;
+    H.band = I->law.band;
+    const int s0 = w.row0 / R;
+    const int ns = (w.nrows + R - 1) / R;
+    for (int q = cw; q < ns; q += kConsumerWarps) {
+        const uint32_t o0 = __ldg(slice_off + s0 + q);
+        const uint32_t steps = (__ldg(slice_off + s0 + q + 1) - o0) >> 6;
+        const int64_t r = (int64_t)(s0 + q) * R + lane32 / G;
+        float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
+        uint32_t len = 0;
+        if (r < n) {
+            a = __ldg(pos + r);
+            len = __ldg(row_off + r + 1) - __ldg(row_off + r);
+        }
+        const int2* line = reinterpret_cast<const int2*>(words + (o0 - shift)) + lane32;
+        float2 ax = make_float2(0.f, 0.f), ay = ax, az = ax;
+        for (uint32_t t = 0; t < steps; t++) {
+            const int2 c = load_pair<SHARED>(line + 32 * t);
+            const uint32_t k0 = 2 * G * t + lane;
+            const bool v0 = k0 < len, v1 = k0 + G < len;
+            const float4 b0 = __ldg(pos + c.x);
+            const float4 b1 = __ldg(pos + c.y);
+            lj_pair<PERIODIC>(a, b0, b1, v0, v1, H, cold, ax, ay, az);
+        }
+        const float3 f = join_partials<G>(ax, ay, az);
+        if (r < n && lane == 0) force[r] = make_float4(f.x, f.y, f.z, 0.f);
     }
 }
 
@@ -315,8 +396,9 @@ __global__ void __launch_bounds__(kPipeThreads, kCtasPerSm) tiled_kernel(
                     s_smem[s] = 1;
                     const uint32_t a0 = w.ent0 & ~3u;
                     const uint32_t words = ((w.ent0 + w.nent - a0) + 3u) & ~3u;
-                    bulk_load(stage_base + s * kStageInts, insts[w.inst].col + a0, words * 4u,
-                              &full[s]);
+                    const int32_t* src =
+                        (w.flags & kItemSliced) ? insts[w.inst].scol : insts[w.inst].col;
+                    bulk_load(stage_base + s * kStageInts, src + a0, words * 4u, &full[s]);
                 }
             }
             if (!issue) {
@@ -337,10 +419,17 @@ __global__ void __launch_bounds__(kPipeThreads, kCtasPerSm) tiled_kernel(
         const int it = s_item[s];
         if (it >= num_items) return;
         const WorkItem w = items[it];
-        if (s_smem[s])
+        if (w.flags & kItemSliced) {
+            if (s_smem[s])
+                consume_sliced<PERIODIC, G, true>(w, insts, stage_base + s * kStageInts, w.ent0, warp,
+                                                  lane);
+            else
+                consume_sliced<PERIODIC, G, false>(w, insts, insts[w.inst].scol, 0u, warp, lane);
+        } else if (s_smem[s]) {
             consume_item<PERIODIC, G>(w, insts, stage_base + s * kStageInts, w.ent0 & ~3u, warp, lane);
-        else
+        } else {
             consume_item<PERIODIC, G>(w, insts, insts[w.inst].col, 0u, warp, lane);
+        }
         __syncwarp();
         if (lane == 0) mbar_arrive(&empty[s]);
     }
@@ -407,7 +496,7 @@ cudaError_t launch_tiled(const TiledShape& shape, const InstDesc* d_insts,
 }
 
 void make_work_items(const uint32_t* row_off, int64_t n, int inst, int max_rows, int staged,
-                     std::vector<WorkItem>& out)
+                     std::vector<WorkItem>& out, int round_rows)
 {
     int64_t r = 0;
     while (r < n) {
@@ -421,12 +510,52 @@ void make_work_items(const uint32_t* row_off, int64_t n, int inst, int max_rows,
         } else {
             while (q < n && q - r < max_rows && (int64_t)(row_off[q + 1] - row_off[r]) <= kStageEntries)
                 q++;
+            if (q < n && q - r > round_rows) q = r + (q - r) / round_rows * round_rows;
         }
         w.nrows = (int32_t)(q - r);
         w.nent = row_off[q] - row_off[r];
         if (!staged || w.nent == 0) w.flags |= kItemDirect;
         out.push_back(w);
         r = q;
+    }
+}
+
+void make_instance_items(const uint32_t* host_row_off, const Sliced& sl, int64_t n, int inst,
+                         const TiledShape& shape, std::vector<WorkItem>& out)
+{
+    if (sl.lanes != 0 && sl.lanes == shape.lanes_per_row)
+        make_sliced_items(sl, n, inst, shape.block_nodes, shape.stage_smem, out);
+    else
+        make_work_items(host_row_off, n, inst, shape.block_nodes, shape.stage_smem, out,
+                        kConsumerSlices * (32 / shape.lanes_per_row));
+}
+
+void make_sliced_items(const Sliced& sl, int64_t n, int inst, int max_rows, int staged,
+                       std::vector<WorkItem>& out)
+{
+    const int R = 32 / sl.lanes;
+    const int64_t max_slices = std::max<int64_t>(1, max_rows / R);
+    const uint32_t* off = sl.host_off.data();
+    int64_t q = 0;
+    while (q < sl.slices) {
+        int64_t e = q + 1;
+        if ((int64_t)(off[e] - off[q]) <= kStageEntries) {
+            while (e < sl.slices && e - q < max_slices &&
+                   (int64_t)(off[e + 1] - off[q]) <= kStageEntries)
+                e++;
+            // whole rounds of the consumer warps where the item allows it
+            if (e < sl.slices && e - q > kConsumerSlices) e = q + (e - q) / kConsumerSlices * kConsumerSlices;
+        }
+        WorkItem w{};
+        w.inst = inst;
+        w.row0 = (int32_t)(q * R);
+        w.nrows = (int32_t)(std::min<int64_t>(n, e * R) - q * R);
+        w.ent0 = off[q];
+        w.nent = off[e] - off[q];
+        w.flags = kItemSliced;
+        if (!staged || w.nent == 0 || (int64_t)w.nent > kStageEntries) w.flags |= kItemDirect;
+        out.push_back(w);
+        q = e;
     }
 }
 

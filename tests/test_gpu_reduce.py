@@ -27,6 +27,16 @@ SHAPES = {
     "part_b2048": dict(exec=1, block_nodes=2048),
     "part_b64": dict(exec=1, block_nodes=64),
     "part_noreorder": dict(exec=1, reorder=0),
+    "csr": dict(exec=1, layout=1),
+    "sliced": dict(exec=1, layout=2),
+    "sliced_g1": dict(exec=1, layout=2, lanes_per_row=1),
+    "sliced_g2": dict(exec=1, layout=2, lanes_per_row=2),
+    "sliced_g8": dict(exec=1, layout=2, lanes_per_row=8),
+    "sliced_g16": dict(exec=1, layout=2, lanes_per_row=16),
+    "sliced_g32": dict(exec=1, layout=2, lanes_per_row=32),
+    "sliced_direct": dict(exec=1, layout=2, stage_smem=0),
+    "sliced_b64": dict(exec=1, layout=2, block_nodes=64),
+    "sliced_noreorder": dict(exec=1, layout=2, reorder=0),
 }
 
 
@@ -103,6 +113,44 @@ def test_partitioned_result_ignores_edge_order(built_lib, shape):
     c["edges"] = e
     f2, _ = run_case(irr, c, **SHAPES[shape])
     assert np.array_equal(f1.view(np.uint32), f2.view(np.uint32))
+
+
+@pytest.mark.parametrize("lanes", [1, 2, 4, 8, 16, 32])
+@pytest.mark.parametrize("name", golden_names())
+def test_sliced_layout_gives_the_csr_sums(built_lib, name, lanes):
+    """The sliced layout hands every lane the entry pairs CSR gives it, in the
+    same order, so the sums agree exactly."""
+    import irregular_gb300 as irr
+    c = load_golden(name)
+    f_csr, h1 = run_case(irr, c, exec=1, layout=irr.IRR_LAYOUT_CSR, lanes_per_row=lanes)
+    f_sl, h2 = run_case(irr, c, exec=1, layout=irr.IRR_LAYOUT_SLICED, lanes_per_row=lanes)
+    f_dir, h3 = run_case(irr, c, exec=1, layout=irr.IRR_LAYOUT_SLICED, lanes_per_row=lanes,
+                         stage_smem=0)
+    assert h1.info().layout == irr.IRR_LAYOUT_CSR and h2.info().layout == irr.IRR_LAYOUT_SLICED
+    assert np.array_equal(f_csr, f_sl) and np.array_equal(f_csr, f_dir)
+    inf = h2.info()
+    assert inf.num_slots >= inf.num_entries and inf.num_slots % 64 == 0
+
+
+def test_auto_layout_choice(built_lib):
+    """AUTO takes the sliced layout for near-uniform rows and keeps CSR when
+    one long row would make the padding dominate."""
+    import irregular_gb300 as irr
+    c = load_golden("moldyn_random_2048")
+    _, h = run_case(irr, c, exec=1)
+    assert h.info().layout == irr.IRR_LAYOUT_SLICED
+    n = c["pos"].shape[0]
+    # 32 hub nodes joined to every other node: their slices pad 8 rows each
+    # to ~n entries, far more than half the entries
+    hubs = [np.stack([np.full(n - 1, k, np.int32), np.delete(np.arange(n, dtype=np.int32), k)],
+                     axis=1) for k in range(0, n, n // 32)]
+    skew = dict(c)
+    skew["edges"] = np.concatenate([c["edges"]] + hubs).astype(np.int32)
+    f, h2 = run_case(irr, skew, exec=1)
+    assert h2.info().layout == irr.IRR_LAYOUT_CSR
+    f_sl, h3 = run_case(irr, skew, exec=1, layout=irr.IRR_LAYOUT_SLICED)
+    assert h3.info().layout == irr.IRR_LAYOUT_SLICED
+    assert np.array_equal(f, f_sl)
 
 
 @pytest.mark.parametrize("exec_mode", [0, 1])
