@@ -141,23 +141,14 @@ __device__ __forceinline__ float rd_of(float dx, float dy, float dz)
     return fmaf(dx, dx, fmaf(dy, dy, __fmul_rn(dz, dz)));
 }
 
-// Two entries (b0, b1) of the row of node a, evaluated with packed FP32x2
-// arithmetic (each half rounds exactly as the scalar law in irr_law.cuh), and
-// accumulated into the lane's packed partials.  An unused slot passes b == a
-// and v == false: d = 0 and its scalar is replaced by 0.
-//
-// A component |d| > side/2 implies rd > (side/2)^2, so the wrap test is one
-// compare on rd; a pair that fails it is re-examined exactly (rare: only a
-// pair across the box wall or beyond half the box).
+// The rare cases of an entry pair: a pair past half the box (periodic) is
+// re-wrapped exactly, and a pair whose rd lies within `band` of the cutoff
+// takes the reference's FP64 decision.  Updates d, rd and the in-flags.
 template <bool PERIODIC>
-__device__ __forceinline__ void lj_pair(float4 a, float4 b0, float4 b1, bool v0, bool v1, const HotLaw& H,
-                                        const LawParams* __restrict__ cold, float2& ax, float2& ay,
-                                        float2& az)
+__device__ __forceinline__ void rare_pair(float4 a, float4 b0, float4 b1, const HotLaw& H,
+                                          const LawParams* __restrict__ cold, float2& dx,
+                                          float2& dy, float2& dz, float2& rd, bool& in0, bool& in1)
 {
-    float2 dx = __fadd2_rn(make_float2(a.x, a.x), make_float2(-b0.x, -b1.x));
-    float2 dy = __fadd2_rn(make_float2(a.y, a.y), make_float2(-b0.y, -b1.y));
-    float2 dz = __fadd2_rn(make_float2(a.z, a.z), make_float2(-b0.z, -b1.z));
-    float2 rd = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
     if (PERIODIC && fmaxf(rd.x, rd.y) > H.half2) {
         const LawParams* P = cold;
         const float half = P->half;
@@ -175,13 +166,39 @@ __device__ __forceinline__ void lj_pair(float4 a, float4 b0, float4 b1, bool v0,
             dz.y = w.z;
             rd.y = rd_of(w.x, w.y, w.z);
         }
+        in0 = rd.x < H.rc2;
+        in1 = rd.y < H.rc2;
     }
-    bool in0 = rd.x < H.rc2, in1 = rd.y < H.rc2;
+    if (fabsf(__fsub_rn(rd.x, H.rc2)) < H.band) in0 = exact_inside_g<PERIODIC>(a, b0, cold);
+    if (fabsf(__fsub_rn(rd.y, H.rc2)) < H.band) in1 = exact_inside_g<PERIODIC>(a, b1, cold);
+}
+
+// Two entries (b0, b1) of the row of node a, evaluated with packed FP32x2
+// arithmetic (each half rounds exactly as the scalar law in irr_law.cuh), and
+// accumulated into the lane's packed partials.  A slot with v == false
+// contributes 0 (its b is the row's own position or any valid node).
+//
+// The differences are formed by scalar subtractions written straight into
+// register pairs (the two positions come from separate loads, so a packed
+// subtraction would first have to move them into pairs).  A component
+// |d| > side/2 implies rd > (side/2)^2, so the wrap test is one compare on
+// rd; it and the cutoff-band test are folded into one branch to the rare
+// path (a pair across the box wall, beyond half the box, or within 2^-18 of
+// the cutoff).  (A warp vote in front of it measured slower.)
+template <bool PERIODIC>
+__device__ __forceinline__ void lj_pair(float4 a, float4 b0, float4 b1, bool v0, bool v1, const HotLaw& H,
+                                        const LawParams* __restrict__ cold, float2& ax, float2& ay,
+                                        float2& az)
+{
+    float2 dx = make_float2(__fsub_rn(a.x, b0.x), __fsub_rn(a.x, b1.x));
+    float2 dy = make_float2(__fsub_rn(a.y, b0.y), __fsub_rn(a.y, b1.y));
+    float2 dz = make_float2(__fsub_rn(a.z, b0.z), __fsub_rn(a.z, b1.z));
+    float2 rd = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
     const float2 t = __fadd2_rn(rd, make_float2(-H.rc2, -H.rc2));
-    if (fminf(fabsf(t.x), fabsf(t.y)) < H.band) {
-        if (fabsf(t.x) < H.band) in0 = exact_inside_g<PERIODIC>(a, b0, cold);
-        if (fabsf(t.y) < H.band) in1 = exact_inside_g<PERIODIC>(a, b1, cold);
-    }
+    bool rare = fminf(fabsf(t.x), fabsf(t.y)) < H.band;
+    if (PERIODIC) rare = rare || fmaxf(rd.x, rd.y) > H.half2;
+    bool in0 = rd.x < H.rc2, in1 = rd.y < H.rc2;
+    if (rare) rare_pair<PERIODIC>(a, b0, b1, H, cold, dx, dy, dz, rd, in0, in1);
     float2 r = make_float2(rcp_approx(rd.x), rcp_approx(rd.y));
     const float2 e = __ffma2_rn(make_float2(-rd.x, -rd.y), r, make_float2(1.0f, 1.0f));
     r = __ffma2_rn(r, e, r);                                     // rd^-1 (one Newton step)
