@@ -82,23 +82,42 @@ __device__ __forceinline__ void bulk_load(void* dst_smem, const void* src, uint3
         : "memory");
 }
 
-// Waits for phase `parity` of the barrier; gives up after `limit` polls.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int limit)
+// One test of phase `parity`; a thread whose phase is not complete may be
+// suspended for up to kSuspendNs (it resumes as soon as the phase completes),
+// so a waiting warp does not keep issuing polls.
+constexpr uint32_t kSuspendNs = 100000;
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
 {
-    for (int i = 0; i < limit; i++) {
-        uint32_t done;
-        asm volatile(
-            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-            " selp.u32 %0, 1, 0, p;\n}\n"
-            : "=r"(done)
-            : "r"(smem_u32(bar)), "r"(parity)
-            : "memory");
-        if (done) return true;
-    }
-    return false;
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(smem_u32(bar)), "r"(parity), "r"(kSuspendNs)
+        : "memory");
+    return done != 0;
 }
 
-constexpr int kWaitPolls = 1 << 20;
+__device__ __forceinline__ uint64_t global_ns()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Waits for phase `parity` of the barrier; gives up after `limit_ns`
+// nanoseconds of wall-clock time (whatever the suspension granted per test).
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint64_t limit_ns)
+{
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = global_ns();
+    for (;;) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if (global_ns() - t0 > limit_ns) return false;
+    }
+}
+
+constexpr uint64_t kWaitNs = 2000000000ull;  // 2 s: far above any item's time
 
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar)
 {
@@ -113,6 +132,34 @@ struct HotLaw {
     float rc2;
     float band;    // |rd - rc2| < band: take the reference's FP64 decision
 };
+
+// What the consumers read of an instance, kept in registers across work
+// items of the same instance (items of one instance are consecutive).
+struct InstHot {
+    const float4* __restrict__ pos;
+    const uint32_t* __restrict__ row_off;
+    const uint32_t* __restrict__ slice_off;
+    float4* __restrict__ force;
+    const LawParams* __restrict__ cold;
+    int64_t n;
+    HotLaw H;
+};
+
+__device__ __forceinline__ InstHot load_hot(const InstDesc* __restrict__ insts, int inst)
+{
+    const InstDesc* __restrict__ I = insts + inst;
+    InstHot h;
+    h.pos = I->pos;
+    h.row_off = I->row_off;
+    h.slice_off = I->slice_off;
+    h.force = I->force;
+    h.cold = &I->law;
+    h.n = I->n;
+    h.H.half2 = I->law.half2;
+    h.H.rc2 = I->law.rc2;
+    h.H.band = I->law.band;
+    return h;
+}
 
 // A pair wrapped across the box wall, recomputed exactly (irr_law.cuh).
 __device__ __noinline__ float3 wrap_exact(float4 a, float4 b, const LawParams* __restrict__ P)
@@ -258,26 +305,29 @@ __device__ __forceinline__ float3 row_sum(const float4* __restrict__ pos, const 
 }
 
 constexpr int kConsumerWarps = kConsumerSlices;
+// Items per queue claim (a run of consecutive node blocks on one SM shares
+// neighbourhood positions in its L1, but runs of 2, 4 and 8 measured slower
+// than single items on the 4M-node workload: load balance wins).
+#ifndef IRR_CLAIM_CHUNK
+#define IRR_CLAIM_CHUNK 1
+#endif
+constexpr int kClaimChunk = IRR_CLAIM_CHUNK;
 constexpr int kPipeThreads = (kConsumerWarps + 1) * 32;
 
 // The rows of one work item that belong to consumer warp `cw`.
 template <bool PERIODIC, int G>
-__device__ __forceinline__ void consume_item(const WorkItem& w, const InstDesc* __restrict__ insts,
+__device__ __forceinline__ void consume_item(const WorkItem& w, const InstHot& I,
                                              const int32_t* cols, uint32_t shift, int cw, int lane32)
 {
     constexpr int kGroupsPerWarp = 32 / G;
     constexpr int kGroups = kConsumerWarps * kGroupsPerWarp;
     const int lane = lane32 % G;
     const int gid = cw * kGroupsPerWarp + lane32 / G;
-    const InstDesc* __restrict__ I = insts + w.inst;
-    const float4* __restrict__ pos = I->pos;
-    const uint32_t* __restrict__ row_off = I->row_off;
-    float4* __restrict__ force = I->force;
-    const LawParams* __restrict__ cold = &I->law;
-    HotLaw H;
-    H.half2 = I->law.half2;
-    H.rc2 = I->law.rc2;
-    H.band = I->law.band;
+    const float4* __restrict__ pos = I.pos;
+    const uint32_t* __restrict__ row_off = I.row_off;
+    float4* __restrict__ force = I.force;
+    const LawParams* __restrict__ cold = I.cold;
+    const HotLaw H = I.H;
     const int rounds = (w.nrows + kGroups - 1) / kGroups;
     for (int q = 0; q < rounds; q++) {
         const int rl = q * kGroups + gid;
@@ -317,23 +367,19 @@ __device__ __forceinline__ int2 load_pair(const int2* p)
 // line; the trip count is the slice's, uniform across the warp, and slots
 // past a row's end (padding: the row's own id) are masked.
 template <bool PERIODIC, int G, bool SHARED>
-__device__ __forceinline__ void consume_sliced(const WorkItem& w, const InstDesc* __restrict__ insts,
+__device__ __forceinline__ void consume_sliced(const WorkItem& w, const InstHot& I,
                                                const int32_t* words, uint32_t shift, int cw,
                                                int lane32)
 {
     constexpr int R = 32 / G;
     const int lane = lane32 % G;
-    const InstDesc* __restrict__ I = insts + w.inst;
-    const float4* __restrict__ pos = I->pos;
-    const uint32_t* __restrict__ row_off = I->row_off;
-    const uint32_t* __restrict__ slice_off = I->slice_off;
-    float4* __restrict__ force = I->force;
-    const LawParams* __restrict__ cold = &I->law;
-    const int64_t n = I->n;
-    HotLaw H;
-    H.half2 = I->law.half2;
-    H.rc2 = I->law.rc2;
-    H.band = I->law.band;
+    const float4* __restrict__ pos = I.pos;
+    const uint32_t* __restrict__ row_off = I.row_off;
+    const uint32_t* __restrict__ slice_off = I.slice_off;
+    float4* __restrict__ force = I.force;
+    const LawParams* __restrict__ cold = I.cold;
+    const int64_t n = I.n;
+    const HotLaw H = I.H;
     const int s0 = w.row0 / R;
     const int ns = (w.nrows + R - 1) / R;
     for (int q = cw; q < ns; q += kConsumerWarps) {
@@ -362,13 +408,15 @@ __device__ __forceinline__ void consume_sliced(const WorkItem& w, const InstDesc
 }
 
 // Persistent owner-computes kernel, warp-specialised.  Warp kConsumerWarps is
-// the producer: its lane 0 claims work items from *queue in order, and for
-// each one waits until its ring stage is empty, publishes the item id and
+// the producer: its lane 0 claims runs of kClaimChunk consecutive work items
+// from *queue, and for each item waits until its ring stage is empty,
+// publishes the item id and
 // either bulk-copies the item's entry segment (widened to 16-byte bounds)
 // into the stage -- the stage's `full` mbarrier completes on the byte count --
 // or, for items read from global memory, just arrives.  The consumer warps
 // walk the ring independently: wait `full`, sum their share of the item's
-// rows, arrive on `empty` (kConsumerWarps arrivals free the stage).  Every
+// rows, arrive on `empty` (kConsumerWarps arrivals free the stage).  Waits
+// suspend the thread until the phase completes (mbar_try_wait).  Every
 // wait is bounded; a wait that gives up sets kStatusWaitTimeout, waits once
 // more (bounded) for a copy that may be in flight, and leaves.
 template <bool PERIODIC, int G>
@@ -396,14 +444,21 @@ __global__ void __launch_bounds__(kPipeThreads, kCtasPerSm) tiled_kernel(
 
     if (warp == kConsumerWarps) {
         if (lane != 0) return;
+        int next_item = 0, chunk_left = 0;
         for (int k = 0;; k++) {
             const int s = k % kStages;
             const int use = k / kStages;
-            if (use > 0 && !mbar_wait_bounded(&empty[s], (uint32_t)(use - 1) & 1u, kWaitPolls)) {
+            if (use > 0 && !mbar_wait_bounded(&empty[s], (uint32_t)(use - 1) & 1u, kWaitNs)) {
                 atomicOr(status, kStatusWaitTimeout);
                 return;  // nothing of this stage is in flight: its last copy was consumed
             }
-            const int it = atomicAdd(queue, 1);
+            if (chunk_left == 0) {  // a run of kClaimChunk consecutive items
+                const long long first = (long long)atomicAdd(queue, 1) * kClaimChunk;
+                next_item = first < num_items ? (int)first : num_items;
+                chunk_left = kClaimChunk;
+            }
+            const int it = next_item++;
+            chunk_left--;
             s_item[s] = it;
             bool issue = false;
             if (it < num_items && use_stages) {
@@ -426,26 +481,32 @@ __global__ void __launch_bounds__(kPipeThreads, kCtasPerSm) tiled_kernel(
         }
     }
 
+    int cur = -1;  // instance whose fields `hot` holds
+    InstHot hot{};
     for (int k = 0;; k++) {
         const int s = k % kStages;
-        if (!mbar_wait_bounded(&full[s], (uint32_t)(k / kStages) & 1u, kWaitPolls)) {
+        if (!mbar_wait_bounded(&full[s], (uint32_t)(k / kStages) & 1u, kWaitNs)) {
             if (lane == 0) atomicOr(status, kStatusWaitTimeout);
-            mbar_wait_bounded(&full[s], (uint32_t)(k / kStages) & 1u, kWaitPolls);
+            mbar_wait_bounded(&full[s], (uint32_t)(k / kStages) & 1u, kWaitNs);
             return;
         }
         const int it = s_item[s];
         if (it >= num_items) return;
         const WorkItem w = items[it];
+        if (w.inst != cur) {
+            hot = load_hot(insts, w.inst);
+            cur = w.inst;
+        }
         if (w.flags & kItemSliced) {
             if (s_smem[s])
-                consume_sliced<PERIODIC, G, true>(w, insts, stage_base + s * kStageInts, w.ent0, warp,
+                consume_sliced<PERIODIC, G, true>(w, hot, stage_base + s * kStageInts, w.ent0, warp,
                                                   lane);
             else
-                consume_sliced<PERIODIC, G, false>(w, insts, insts[w.inst].scol, 0u, warp, lane);
+                consume_sliced<PERIODIC, G, false>(w, hot, insts[w.inst].scol, 0u, warp, lane);
         } else if (s_smem[s]) {
-            consume_item<PERIODIC, G>(w, insts, stage_base + s * kStageInts, w.ent0 & ~3u, warp, lane);
+            consume_item<PERIODIC, G>(w, hot, stage_base + s * kStageInts, w.ent0 & ~3u, warp, lane);
         } else {
-            consume_item<PERIODIC, G>(w, insts, insts[w.inst].col, 0u, warp, lane);
+            consume_item<PERIODIC, G>(w, hot, insts[w.inst].col, 0u, warp, lane);
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(&empty[s]);
