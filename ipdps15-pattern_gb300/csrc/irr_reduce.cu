@@ -161,13 +161,14 @@ __device__ __forceinline__ InstHot load_hot(const InstDesc* __restrict__ insts, 
     return h;
 }
 
-// A pair wrapped across the box wall, recomputed exactly (irr_law.cuh).
-__device__ __noinline__ float3 wrap_exact(float4 a, float4 b, const LawParams* __restrict__ P)
+// wrap_component (irr_law.cuh) without branches: both shifted forms are
+// formed and the one the sign of d calls for is selected.
+__device__ __forceinline__ float wrap_select(float a, float b, float d, float half, float shi,
+                                             float slo)
 {
-    const LawParams L = *P;
-    return make_float3(wrap_component(a.x, b.x, __fsub_rn(a.x, b.x), L),
-                       wrap_component(a.y, b.y, __fsub_rn(a.y, b.y), L),
-                       wrap_component(a.z, b.z, __fsub_rn(a.z, b.z), L));
+    const float up = __fsub_rn(__fsub_rn(__fsub_rn(a, shi), b), slo);  // d > half
+    const float dn = __fadd_rn(__fsub_rn(a, __fsub_rn(b, shi)), slo);  // d < -half
+    return d > half ? up : (d < -half ? dn : d);
 }
 
 template <bool PERIODIC>
@@ -183,11 +184,6 @@ __device__ __forceinline__ float rcp_approx(float x)
     return r;
 }
 
-__device__ __forceinline__ float rd_of(float dx, float dy, float dz)
-{
-    return fmaf(dx, dx, fmaf(dy, dy, __fmul_rn(dz, dz)));
-}
-
 // The rare cases of an entry pair: a pair past half the box (periodic) is
 // re-wrapped exactly, and a pair whose rd lies within `band` of the cutoff
 // takes the reference's FP64 decision.  Updates d, rd and the in-flags.
@@ -197,22 +193,16 @@ __device__ __forceinline__ void rare_pair(float4 a, float4 b0, float4 b1, const 
                                           float2& dy, float2& dz, float2& rd, bool& in0, bool& in1)
 {
     if (PERIODIC && fmaxf(rd.x, rd.y) > H.half2) {
-        const LawParams* P = cold;
-        const float half = P->half;
-        if (fabsf(dx.x) > half || fabsf(dy.x) > half || fabsf(dz.x) > half) {
-            const float3 w = wrap_exact(a, b0, P);
-            dx.x = w.x;
-            dy.x = w.y;
-            dz.x = w.z;
-            rd.x = rd_of(w.x, w.y, w.z);
-        }
-        if (fabsf(dx.y) > half || fabsf(dy.y) > half || fabsf(dz.y) > half) {
-            const float3 w = wrap_exact(a, b1, P);
-            dx.y = w.x;
-            dy.y = w.y;
-            dz.y = w.z;
-            rd.y = rd_of(w.x, w.y, w.z);
-        }
+        // every component of both slots through wrap_select (a component
+        // within half the box comes back unchanged, bit for bit)
+        const float half = cold->half, shi = cold->side_hi, slo = cold->side_lo;
+        dx.x = wrap_select(a.x, b0.x, dx.x, half, shi, slo);
+        dy.x = wrap_select(a.y, b0.y, dy.x, half, shi, slo);
+        dz.x = wrap_select(a.z, b0.z, dz.x, half, shi, slo);
+        dx.y = wrap_select(a.x, b1.x, dx.y, half, shi, slo);
+        dy.y = wrap_select(a.y, b1.y, dy.y, half, shi, slo);
+        dz.y = wrap_select(a.z, b1.z, dz.y, half, shi, slo);
+        rd = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
         in0 = rd.x < H.rc2;
         in1 = rd.y < H.rc2;
     }
