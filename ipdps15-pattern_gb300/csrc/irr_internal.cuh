@@ -96,7 +96,10 @@ void make_work_items(const uint32_t* row_off, int64_t n, int inst, int max_rows,
 // cut at multiples of kConsumerSlices slices where that fits.
 void make_sliced_items(const Sliced& sl, int64_t n, int inst, int max_rows, int staged,
                        std::vector<WorkItem>& out);
-constexpr int kConsumerSlices = 8;  // consumer warps of the tiled kernel
+#ifndef IRR_CONSUMER_WARPS
+#define IRR_CONSUMER_WARPS 8
+#endif
+constexpr int kConsumerSlices = IRR_CONSUMER_WARPS;  // consumer warps of the tiled kernel
 // One instance's items for `shape`: sliced items if sl was built for
 // shape.lanes_per_row, else CSR items from the host row offsets.
 void make_instance_items(const uint32_t* host_row_off, const Sliced& sl, int64_t n, int inst,
