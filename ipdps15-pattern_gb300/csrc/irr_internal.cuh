@@ -157,6 +157,12 @@ cudaError_t build_partition(const float4* pos_user, int64_t n, const int2* edges
 // Half neighbour list (irr_neighbor.cu); *d_edges is cudaMalloc'd.
 cudaError_t build_neighbor_list(const float4* pos, int64_t n, float box, float cut2,
                                 int2** d_edges, int64_t* num_edges, cudaStream_t s);
+// Sorts each row of a CSR (row_off[n + 1], col) ascending; every row must
+// hold at most kRowSortMax entries.
+constexpr int kRowSortMax = 1024;
+cudaError_t launch_row_sort(const uint32_t* row_off, int64_t n, int32_t* col, cudaStream_t s);
+// The longest row of a CSR (synchronises s).
+cudaError_t max_row_len(const uint32_t* row_off, int64_t n, uint32_t* result, cudaStream_t s);
 // Stable LSD radix sort of (key, value) pairs on key bits [0, key_bits).
 // Sorted data ends in (keys, vals); tmp arrays have n entries each.
 cudaError_t radix_sort_pairs(uint32_t* keys, int32_t* vals, uint32_t* keys_tmp,

@@ -8,7 +8,8 @@
 //      each cell's start;
 //   3. one thread per node (in cell order, so a warp shares cells) scans the
 //      27 surrounding cells for partners j > i with r2 <= cut2, first counting,
-//      then -- after a scan of the counts -- writing them, sorted by j.
+//      then -- after a scan of the counts -- writing them; a warp per row then
+//      sorts each row by j in shared memory.
 // The pair rule is shared bit for bit with the CPU oracle: d = x_i - x_j in
 // float, wrapped once by +-box when |d| > box/2 (periodic), r2 = ((dx*dx +
 // dy*dy) + dz*dz) with every operation rounded.  Output: pairs (i, j), i < j,
@@ -73,11 +74,13 @@ __global__ void cell_keys_kernel(const float4* pos, int64_t n, Grid g, uint32_t*
 }
 
 // WRITE == false: counts partners; WRITE == true: writes them at row_off[i]
-// and sorts the row by j.
+// (and, with sort_here, sorts the row by j in place: only for rows too long
+// for the shared row sort that otherwise follows).
 template <bool WRITE>
 __global__ void pairs_kernel(const float4* __restrict__ pos, const int32_t* __restrict__ sorted,
                              const uint32_t* __restrict__ cell_start, int64_t n, Grid g,
-                             uint32_t* count, const uint32_t* __restrict__ row_off, int32_t* nbr)
+                             uint32_t* count, const uint32_t* __restrict__ row_off, int32_t* nbr,
+                             int sort_here)
 {
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
          t += (int64_t)gridDim.x * blockDim.x) {
@@ -112,8 +115,8 @@ __global__ void pairs_kernel(const float4* __restrict__ pos, const int32_t* __re
         }
         if (!WRITE) {
             count[i] = m;
-        } else {
-            // insertion sort of the row (rows are short: tens of entries)
+        } else if (sort_here) {
+            // insertion sort of the row in place
             for (uint32_t u = 1; u < m; u++) {
                 const int32_t v = nbr[base + u];
                 uint32_t w = u;
@@ -211,7 +214,7 @@ cudaError_t build_neighbor_list(const float4* pos, int64_t n, float box, float c
     IRR_CUDA_TRY(radix_sort_pairs(keys, sorted, keys_tmp, vals_tmp, n, bits, s));
     IRR_CUDA_TRY(scan_exclusive_u32(cell_start, cell_start, ncell + 1, nullptr, s));
     pairs_kernel<false><<<grid_of(n), 256, 0, s>>>(pos, sorted, cell_start, n, g, cnt, nullptr,
-                                                   nullptr);
+                                                   nullptr, 0);
     IRR_CUDA_TRY(cudaGetLastError());
     IRR_CUDA_TRY(cudaMemsetAsync(cnt + n, 0, sizeof(uint32_t), s));
     uint32_t* d_total = keys_tmp;  // reuse as the total's slot
@@ -222,10 +225,14 @@ cudaError_t build_neighbor_list(const float4* pos, int64_t n, float box, float c
     if ((int64_t)total > 0x7fffffffLL) return cudaErrorInvalidValue;
     int2* edges = nullptr;
     if (total > 0) {
+        uint32_t longest = 0;
+        IRR_CUDA_TRY(max_row_len(cnt, n, &longest, s));
+        const int sort_here = longest > (uint32_t)kRowSortMax;
         IRR_CUDA_TRY(cudaMallocAsync((void**)&nbr, sizeof(int32_t) * total, s));
         pairs_kernel<true><<<grid_of(n), 256, 0, s>>>(pos, sorted, cell_start, n, g, nullptr, cnt,
-                                                      nbr);
+                                                      nbr, sort_here);
         IRR_CUDA_TRY(cudaGetLastError());
+        if (!sort_here) IRR_CUDA_TRY(launch_row_sort(cnt, n, nbr, s));
         IRR_CUDA_TRY(cudaMalloc((void**)&edges, sizeof(int2) * total));
         expand_pairs_kernel<<<grid_of(n), 256, 0, s>>>(cnt, nbr, n, edges);
         IRR_CUDA_TRY(cudaGetLastError());

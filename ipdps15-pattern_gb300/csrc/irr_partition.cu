@@ -10,9 +10,11 @@
 //      box frame (float ops, each rounded), bits interleaved;
 //   2. stable LSD radix sort of (key, node) -> perm[new] = old, inv[old] = new;
 //   3. every half edge (i, j) at list position t becomes the directed entries
-//      (inv[i] <- inv[j]) and (inv[j] <- inv[i]); stable radix sorts by
-//      column, then by row, put them in (row, col) order, and a degree
-//      count + scan gives the row offsets.
+//      (inv[i] <- inv[j]) and (inv[j] <- inv[i]), laid out in (row, col)
+//      order: a degree count + scan gives the row offsets, the entries are
+//      filled at per-row cursors and each row is sorted by one warp in shared
+//      memory (rows up to kRowSortMax entries); a graph with a longer row is
+//      put in order by stable radix sorts by column, then by row.
 // Node blocks are then consecutive ranges of rows.  Every output is an
 // integer function of the inputs, reproduced bit for bit by the CPU oracle.
 // 4. Optionally the sliced layout (struct Sliced): the same entries regrouped
@@ -154,6 +156,77 @@ __global__ void __launch_bounds__(kSortThreads) radix_scatter_kernel(
     }
 }
 
+// ------------------------------------------------------------ row sort
+// Each row of a CSR (row_off[n + 1], col) sorted ascending: one warp per row,
+// the row padded to a power of two in a shared-memory buffer and sorted by a
+// bitonic network.  Rows must hold at most kRowSortMax entries.
+constexpr int kRowSortWarps = 8;
+
+__global__ void __launch_bounds__(kRowSortWarps * 32) row_sort_kernel(const uint32_t* __restrict__ row_off,
+                                                                     int64_t n, int32_t* col)
+{
+    __shared__ int32_t buf[kRowSortWarps][kRowSortMax];
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    int32_t* b = buf[warp];
+    for (int64_t r = (int64_t)blockIdx.x * kRowSortWarps + warp; r < n;
+         r += (int64_t)gridDim.x * kRowSortWarps) {
+        const uint32_t beg = row_off[r];
+        const uint32_t len = row_off[r + 1] - beg;
+        if (len < 2) continue;
+        uint32_t P = 2;
+        while (P < len) P <<= 1;  // len <= kRowSortMax, so P <= kRowSortMax
+        for (uint32_t k = lane; k < P; k += 32) b[k] = k < len ? col[beg + k] : 0x7fffffff;
+        __syncwarp();
+        for (uint32_t size = 2; size <= P; size <<= 1) {
+            for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+                for (uint32_t k = lane; k < P; k += 32) {
+                    const uint32_t o = k ^ stride;
+                    if (o > k) {
+                        const int32_t x = b[k], y = b[o];
+                        if ((x > y) == ((k & size) == 0)) {
+                            b[k] = y;
+                            b[o] = x;
+                        }
+                    }
+                }
+                __syncwarp();
+            }
+        }
+        for (uint32_t k = lane; k < len; k += 32) col[beg + k] = b[k];
+        __syncwarp();
+    }
+}
+
+// *out = max over rows of row_off[r + 1] - row_off[r] (out must start at 0)
+__global__ void max_row_len_kernel(const uint32_t* __restrict__ row_off, int64_t n, uint32_t* out)
+{
+    uint32_t m = 0;
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n;
+         r += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t len = row_off[r + 1] - row_off[r];
+        m = len > m ? len : m;
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        const uint32_t o = __shfl_xor_sync(0xffffffffu, m, off);
+        m = o > m ? o : m;
+    }
+    if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+// *out = max of deg[0, n) (out must start at 0)
+__global__ void max_u32_kernel(const uint32_t* __restrict__ a, int64_t n, uint32_t* out)
+{
+    uint32_t m = 0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        m = a[i] > m ? a[i] : m;
+    for (int off = 16; off > 0; off >>= 1) {
+        const uint32_t o = __shfl_xor_sync(0xffffffffu, m, off);
+        m = o > m ? o : m;
+    }
+    if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
 namespace {
 
 // --------------------------------------------------------------- bbox
@@ -250,6 +323,31 @@ __global__ void entries_kernel(const int2* edges, int64_t e, const int32_t* inv,
         cols[2 * t + 1] = a;
         atomicAdd(deg + a, 1u);
         atomicAdd(deg + b, 1u);
+    }
+}
+
+// Degrees of the directed entries (both endpoints of every half edge).
+__global__ void degree_kernel(const int2* edges, int64_t e, const int32_t* inv, uint32_t* deg)
+{
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < e;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int2 ed = edges[t];
+        atomicAdd(deg + inv[ed.x], 1u);
+        atomicAdd(deg + inv[ed.y], 1u);
+    }
+}
+
+// Directed entries into their rows at per-row cursors (order within a row
+// arbitrary until the row sort).
+__global__ void fill_rows_kernel(const int2* edges, int64_t e, const int32_t* inv,
+                                 uint32_t* cursor, int32_t* col)
+{
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < e;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int2 ed = edges[t];
+        const int32_t a = inv[ed.x], b = inv[ed.y];
+        col[atomicAdd(cursor + a, 1u)] = b;
+        col[atomicAdd(cursor + b, 1u)] = a;
     }
 }
 
@@ -467,6 +565,29 @@ cudaError_t bbox_frame(const float4* pos, int64_t n, float lo[3], float scale[3]
     return cudaSuccess;
 }
 
+cudaError_t launch_row_sort(const uint32_t* row_off, int64_t n, int32_t* col, cudaStream_t s)
+{
+    if (n <= 0) return cudaSuccess;
+    int64_t blocks = (n + kRowSortWarps - 1) / kRowSortWarps;
+    if (blocks > 65536) blocks = 65536;
+    row_sort_kernel<<<(unsigned)blocks, kRowSortWarps * 32, 0, s>>>(row_off, n, col);
+    return cudaGetLastError();
+}
+
+cudaError_t max_row_len(const uint32_t* row_off, int64_t n, uint32_t* result, cudaStream_t s)
+{
+    *result = 0;
+    if (n <= 0) return cudaSuccess;
+    uint32_t* d_max = nullptr;
+    IRR_CUDA_TRY(alloc_async(&d_max, 1, s));
+    IRR_CUDA_TRY(cudaMemsetAsync(d_max, 0, sizeof(uint32_t), s));
+    max_row_len_kernel<<<grid_for(n), 256, 0, s>>>(row_off, n, d_max);
+    IRR_CUDA_TRY(cudaGetLastError());
+    IRR_CUDA_TRY(cudaMemcpyAsync(result, d_max, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    IRR_CUDA_TRY(cudaFreeAsync(d_max, s));
+    return cudaStreamSynchronize(s);
+}
+
 cudaError_t build_partition(const float4* pos_user, int64_t n, const int2* edges, int64_t e,
                             int reorder, PartitionOut* out, cudaStream_t s)
 {
@@ -506,6 +627,35 @@ cudaError_t build_partition(const float4* pos_user, int64_t n, const int2* edges
     // directed entries, binned by row
     uint32_t* deg = out->row_off;  // counted in place, then scanned
     IRR_CUDA_TRY(cudaMemsetAsync(deg, 0, sizeof(uint32_t) * (size_t)(n + 1), s));
+    if (e > 0 && n > 0) {
+        // rows of at most kRowSortMax entries (every MD list): count, scan,
+        // fill at per-row cursors, sort each row -- the same (row, col) layout
+        // as the sorts below, in about a third of the passes
+        degree_kernel<<<grid_for(e), 256, 0, s>>>(edges, e, out->inv, deg);
+        IRR_CUDA_TRY(cudaGetLastError());
+        uint32_t* d_max = nullptr;
+        IRR_CUDA_TRY(alloc_async(&d_max, 1, s));
+        IRR_CUDA_TRY(cudaMemsetAsync(d_max, 0, sizeof(uint32_t), s));
+        max_u32_kernel<<<grid_for(n), 256, 0, s>>>(deg, n, d_max);
+        IRR_CUDA_TRY(cudaGetLastError());
+        uint32_t max_deg = 0;
+        IRR_CUDA_TRY(cudaMemcpyAsync(&max_deg, d_max, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+        IRR_CUDA_TRY(cudaFreeAsync(d_max, s));
+        IRR_CUDA_TRY(cudaStreamSynchronize(s));
+        if (max_deg <= (uint32_t)kRowSortMax) {
+            IRR_CUDA_TRY(scan_exclusive_u32(deg, out->row_off, n + 1, nullptr, s));
+            uint32_t* cursor = nullptr;
+            IRR_CUDA_TRY(alloc_async(&cursor, n, s));
+            IRR_CUDA_TRY(cudaMemcpyAsync(cursor, out->row_off, sizeof(uint32_t) * (size_t)n,
+                                         cudaMemcpyDeviceToDevice, s));
+            fill_rows_kernel<<<grid_for(e), 256, 0, s>>>(edges, e, out->inv, cursor, out->col);
+            IRR_CUDA_TRY(cudaGetLastError());
+            IRR_CUDA_TRY(cudaFreeAsync(cursor, s));
+            IRR_CUDA_TRY(launch_row_sort(out->row_off, n, out->col, s));
+            return cudaSuccess;
+        }
+        IRR_CUDA_TRY(cudaMemsetAsync(deg, 0, sizeof(uint32_t) * (size_t)(n + 1), s));
+    }
     if (e > 0) {
         const int64_t m = 2 * e;
         uint32_t *rows = nullptr, *rows_tmp = nullptr;
