@@ -49,9 +49,16 @@ int grid_of(int64_t n)
     return (int)(g < 1 ? 1 : (g > 8192 ? 8192 : g));
 }
 
+// x into [0, L).  An atom moves much less than a box per step, so one shift
+// of +-L covers the step (FP64 division is slow here); the floor form is the
+// fallback and gives the same value for x in [-L, 2L).
 __device__ __forceinline__ double wrap_box(double x, double L)
 {
-    x -= L * floor(x / L);
+    if (x >= L) {
+        x = x < 2.0 * L ? x - L : x - L * floor(x / L);
+    } else if (x < 0.0) {
+        x = x >= -L ? x + L : x - L * floor(x / L);
+    }
     if (x >= L) x -= L;  // x = -tiny rounds up to L
     if (x < 0.0) x = 0.0;
     return x;
