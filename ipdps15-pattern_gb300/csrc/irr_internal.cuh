@@ -73,15 +73,20 @@ struct TiledShape {
 #ifndef IRR_STAGES
 #define IRR_STAGES 2
 #endif
+// 5104 entries: 2 stages of (5104 + kColPad) words, the barriers and the
+// per-CTA reserve keep 4 CTAs inside the 164 KB shared-memory carveout, so
+// the SM keeps ~92 KB of L1 for the position gathers (at 5120 the next
+// carveout, 196 KB, leaves ~60 KB: measured 2 % slower).  8 slices of the MD
+// workloads (~4800 words) still fit one stage.
 #ifndef IRR_STAGE_ENTRIES
-#define IRR_STAGE_ENTRIES 5120
+#define IRR_STAGE_ENTRIES 5104
 #endif
 #ifndef IRR_CTAS_PER_SM
 #define IRR_CTAS_PER_SM 4
 #endif
 constexpr int kTiledThreads = 256;
 constexpr int kStages = IRR_STAGES;              // shared-memory ring depth
-constexpr int kStageEntries = IRR_STAGE_ENTRIES; // entries per stage (20 KB at 5120)
+constexpr int kStageEntries = IRR_STAGE_ENTRIES; // entries per stage (~20 KB)
 constexpr int kColPad = 4;                       // entries allocated past the end of col
 constexpr int kCtasPerSm = IRR_CTAS_PER_SM;      // resident CTAs per SM (registers, ring)
 
