@@ -116,7 +116,8 @@ void make_instance_items(const uint32_t* host_row_off, const Sliced& sl, int64_t
 // cudaErrorInvalidValue if the layout would exceed 2^32 - 1 words.
 cudaError_t build_sliced(const uint32_t* row_off, const int32_t* col, int64_t n, int G,
                          Sliced* sl, cudaStream_t s);
-void free_sliced(Sliced* sl);
+// s != nullptr: stream-ordered frees on s (the arrays come from cudaMallocAsync).
+void free_sliced(Sliced* sl, cudaStream_t s = nullptr);
 // The automatic choice: sliced when padding adds at most half the entries.
 inline bool sliced_pays(const Sliced& sl, int64_t entries)
 {
@@ -159,9 +160,11 @@ cudaError_t bbox_frame(const float4* pos, int64_t n, float lo[3], float scale[3]
 // cudaMallocAsync on s (caller frees).  reorder == 0 keeps the identity order.
 cudaError_t build_partition(const float4* pos_user, int64_t n, const int2* edges, int64_t e,
                             int reorder, PartitionOut* out, cudaStream_t s);
-// Half neighbour list (irr_neighbor.cu); *d_edges is cudaMalloc'd.
+// Half neighbour list (irr_neighbor.cu); *d_edges is cudaMalloc'd, or, with
+// stream_ordered, cudaMallocAsync'd on s (free it with cudaFreeAsync).
 cudaError_t build_neighbor_list(const float4* pos, int64_t n, float box, float cut2,
-                                int2** d_edges, int64_t* num_edges, cudaStream_t s);
+                                int2** d_edges, int64_t* num_edges, cudaStream_t s,
+                                bool stream_ordered = false);
 // Sorts each row of a CSR (row_off[n + 1], col) ascending; every row must
 // hold at most kRowSortMax entries.
 constexpr int kRowSortMax = 1024;

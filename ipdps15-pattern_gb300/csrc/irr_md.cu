@@ -236,15 +236,18 @@ __global__ void potential_kernel(const float4* __restrict__ pos, const uint32_t*
     }
 }
 
-void free_part(irr_md* m)
+// Stream-ordered frees (on s): no device-wide synchronisation, so the set-up
+// of several systems can overlap (the serving loop rebuilds them on their
+// own streams from several host threads).
+void free_part(irr_md* m, cudaStream_t s)
 {
-    if (m->part.perm) cudaFree(m->part.perm);
-    if (m->part.inv) cudaFree(m->part.inv);
-    if (m->part.row_off) cudaFree(m->part.row_off);
-    if (m->part.col) cudaFree(m->part.col);
+    if (m->part.perm) cudaFreeAsync(m->part.perm, s);
+    if (m->part.inv) cudaFreeAsync(m->part.inv, s);
+    if (m->part.row_off) cudaFreeAsync(m->part.row_off, s);
+    if (m->part.col) cudaFreeAsync(m->part.col, s);
     m->part = PartitionOut{};
-    free_sliced(&m->sl);
-    if (m->d_items) cudaFree(m->d_items);
+    free_sliced(&m->sl, s);
+    if (m->d_items) cudaFreeAsync(m->d_items, s);
     m->d_items = nullptr;
     m->num_items = 0;
 }
@@ -260,12 +263,13 @@ int md_rebuild(irr_md* m)
     const double lc = m->cfg.cutforce + m->cfg.skin;
     int2* d_edges = nullptr;
     int64_t e = 0;
-    MD_CUDA(m, build_neighbor_list(m->pos4, m->n, (float)m->cfg.side, (float)(lc * lc), &d_edges, &e, s),
+    MD_CUDA(m, build_neighbor_list(m->pos4, m->n, (float)m->cfg.side, (float)(lc * lc), &d_edges, &e, s,
+                                   true),
             "neighbour build");
-    free_part(m);
+    free_part(m, s);
     PartitionOut p;
     cudaError_t pe = build_partition(m->pos4, m->n, d_edges, e, 1, &p, s);
-    if (d_edges) cudaFree(d_edges);
+    if (d_edges) cudaFreeAsync(d_edges, s);
     m->part = p;
     if (pe != cudaSuccess) return md_fail(m, IRR_ERR_CUDA, "partition", pe);
     // state into the new order
@@ -284,14 +288,15 @@ int md_rebuild(irr_md* m)
     MD_CUDA(m, cudaStreamSynchronize(s), "row offsets");
     if (build_sliced(m->part.row_off, m->part.col, m->n, m->shape.lanes_per_row, &m->sl, s) != cudaSuccess) {
         cudaGetLastError();
-        free_sliced(&m->sl);  // CSR
+        free_sliced(&m->sl, s);  // CSR
     } else if (!sliced_pays(m->sl, 2 * e)) {
-        free_sliced(&m->sl);
+        free_sliced(&m->sl, s);
     }
     std::vector<WorkItem> items;
     make_instance_items(ro.data(), m->sl, m->n, 0, m->shape, items);
     m->num_items = (int)items.size();
-    MD_CUDA(m, cudaMalloc(&m->d_items, sizeof(WorkItem) * (items.empty() ? 1 : items.size())), "work items");
+    MD_CUDA(m, cudaMallocAsync(&m->d_items, sizeof(WorkItem) * (items.empty() ? 1 : items.size()), s),
+            "work items");
     if (!items.empty())
         MD_CUDA(m, cudaMemcpyAsync(m->d_items, items.data(), sizeof(WorkItem) * items.size(),
                                    cudaMemcpyHostToDevice, s), "work items");
@@ -413,17 +418,19 @@ int irr_md_create(const irr_md_config* cfg, const double* pos, const double* vel
     m->shape.periodic = 1;
     const size_t b3 = sizeof(double) * 3 * (size_t)n;
     cudaError_t e = cudaSuccess;
-    if (e == cudaSuccess) e = cudaMalloc(&m->x, b3);
-    if (e == cudaSuccess) e = cudaMalloc(&m->v, b3);
-    if (e == cudaSuccess) e = cudaMalloc(&m->tmp, b3);
-    if (e == cudaSuccess) e = cudaMalloc(&m->pos4, sizeof(float4) * n);
-    if (e == cudaSuccess) e = cudaMalloc(&m->force, sizeof(float4) * n);
-    if (e == cudaSuccess) e = cudaMalloc(&m->ids, sizeof(int32_t) * n);
-    if (e == cudaSuccess) e = cudaMalloc(&m->ids_tmp, sizeof(int32_t) * n);
-    if (e == cudaSuccess) e = cudaMalloc(&m->d_inst, sizeof(InstDesc));
-    if (e == cudaSuccess) e = cudaMalloc(&m->d_queue, sizeof(int));
-    if (e == cudaSuccess) e = cudaMalloc(&m->d_status, sizeof(int));
-    if (e == cudaSuccess) e = cudaMalloc(&m->d_acc, (4 + 3 * kEnergyBlocks) * sizeof(double));
+    // stream-ordered (no device-wide synchronisation; see free_part)
+    cudaStream_t os = m->own_stream;
+    if (e == cudaSuccess) e = cudaMallocAsync(&m->x, b3, os);
+    if (e == cudaSuccess) e = cudaMallocAsync(&m->v, b3, os);
+    if (e == cudaSuccess) e = cudaMallocAsync(&m->tmp, b3, os);
+    if (e == cudaSuccess) e = cudaMallocAsync(&m->pos4, sizeof(float4) * n, os);
+    if (e == cudaSuccess) e = cudaMallocAsync(&m->force, sizeof(float4) * n, os);
+    if (e == cudaSuccess) e = cudaMallocAsync(&m->ids, sizeof(int32_t) * n, os);
+    if (e == cudaSuccess) e = cudaMallocAsync(&m->ids_tmp, sizeof(int32_t) * n, os);
+    if (e == cudaSuccess) e = cudaMallocAsync(&m->d_inst, sizeof(InstDesc), os);
+    if (e == cudaSuccess) e = cudaMallocAsync(&m->d_queue, sizeof(int), os);
+    if (e == cudaSuccess) e = cudaMallocAsync(&m->d_status, sizeof(int), os);
+    if (e == cudaSuccess) e = cudaMallocAsync(&m->d_acc, (4 + 3 * kEnergyBlocks) * sizeof(double), os);
     if (e == cudaSuccess) e = cudaMemsetAsync(m->d_status, 0, sizeof(int), m->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(m->x, pos, b3, cudaMemcpyHostToDevice, m->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(m->v, vel, b3, cudaMemcpyHostToDevice, m->stream);
@@ -459,12 +466,15 @@ int irr_md_destroy(irr_md* m)
     if (!m) return IRR_ERR_ARG;
     cudaSetDevice(m->device);
     if (m->stream) cudaStreamSynchronize(m->stream);
-    free_part(m);
-    void* ptrs[] = {m->x, m->v, m->tmp, m->pos4, m->force, m->ids, m->ids_tmp,
-                    m->d_inst, m->d_queue, m->d_status, m->d_acc};
-    for (void* p : ptrs)
-        if (p) cudaFree(p);
-    if (m->own_stream) cudaStreamDestroy(m->own_stream);
+    if (m->own_stream) {
+        free_part(m, m->own_stream);
+        void* ptrs[] = {m->x, m->v, m->tmp, m->pos4, m->force, m->ids, m->ids_tmp,
+                        m->d_inst, m->d_queue, m->d_status, m->d_acc};
+        for (void* p : ptrs)
+            if (p) cudaFreeAsync(p, m->own_stream);
+        cudaStreamSynchronize(m->own_stream);
+        cudaStreamDestroy(m->own_stream);
+    }
     delete m;
     return IRR_OK;
 }

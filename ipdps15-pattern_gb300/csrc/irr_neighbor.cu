@@ -146,9 +146,11 @@ int grid_of(int64_t n)
 
 }  // namespace
 
-// Builds the list; *d_edges is cudaMalloc'd (2 * *num_edges int32).
+// Builds the list; *d_edges is cudaMalloc'd, or cudaMallocAsync'd on s when
+// stream_ordered (2 * *num_edges int32).
 cudaError_t build_neighbor_list(const float4* pos, int64_t n, float box, float cut2,
-                                int2** d_edges, int64_t* num_edges, cudaStream_t s)
+                                int2** d_edges, int64_t* num_edges, cudaStream_t s,
+                                bool stream_ordered)
 {
     *d_edges = nullptr;
     *num_edges = 0;
@@ -233,7 +235,10 @@ cudaError_t build_neighbor_list(const float4* pos, int64_t n, float box, float c
                                                       nbr, sort_here);
         IRR_CUDA_TRY(cudaGetLastError());
         if (!sort_here) IRR_CUDA_TRY(launch_row_sort(cnt, n, nbr, s));
-        IRR_CUDA_TRY(cudaMalloc((void**)&edges, sizeof(int2) * total));
+        if (stream_ordered)
+            IRR_CUDA_TRY(cudaMallocAsync((void**)&edges, sizeof(int2) * total, s));
+        else
+            IRR_CUDA_TRY(cudaMalloc((void**)&edges, sizeof(int2) * total));
         expand_pairs_kernel<<<grid_of(n), 256, 0, s>>>(cnt, nbr, n, edges);
         IRR_CUDA_TRY(cudaGetLastError());
         IRR_CUDA_TRY(cudaFreeAsync(nbr, s));

@@ -733,10 +733,15 @@ cudaError_t build_sliced(const uint32_t* row_off, const int32_t* col, int64_t n,
     return cudaSuccess;
 }
 
-void free_sliced(Sliced* sl)
+void free_sliced(Sliced* sl, cudaStream_t s)
 {
-    if (sl->slice_off) cudaFree(sl->slice_off);
-    if (sl->col) cudaFree(sl->col);
+    if (s) {
+        if (sl->slice_off) cudaFreeAsync(sl->slice_off, s);
+        if (sl->col) cudaFreeAsync(sl->col, s);
+    } else {
+        if (sl->slice_off) cudaFree(sl->slice_off);
+        if (sl->col) cudaFree(sl->col);
+    }
     sl->slice_off = nullptr;
     sl->col = nullptr;
     sl->slices = sl->words = 0;

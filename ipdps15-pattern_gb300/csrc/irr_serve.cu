@@ -14,6 +14,7 @@
 // Serial mode runs the same jobs one at a time for comparison.  Each job's
 // initial state arrives with the request: it is made before the clock starts.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -44,6 +45,27 @@ struct Live {
     double admit_s;
     double pair_evals;
 };
+
+// Runs f(0..count-1) on up to `workers` host threads (count small: inline).
+// Each call issues work on its own job's stream, so the GPU overlaps the
+// jobs' set-up kernels while each thread waits only for its own.
+template <class F>
+void run_parallel(size_t count, unsigned workers, int device, F f)
+{
+    if (count <= 1 || workers <= 1) {
+        for (size_t i = 0; i < count; i++) f(i);
+        return;
+    }
+    std::atomic<size_t> next{0};
+    std::vector<std::thread> pool;
+    const unsigned nth = (unsigned)std::min<size_t>(count, workers);
+    for (unsigned t = 0; t < nth; t++)
+        pool.emplace_back([&]() {
+            cudaSetDevice(device);
+            for (size_t i = next++; i < count; i = next++) f(i);
+        });
+    for (auto& th : pool) th.join();
+}
 
 uint64_t mix64(uint64_t x)
 {
@@ -233,7 +255,12 @@ int irr_serve_run(const irr_serve_config* cfg, irr_serve_stats* st, irr_serve_jo
     }
     const auto t0 = std::chrono::steady_clock::now();
     auto now = [&]() { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); };
-    std::vector<double> hpos, hvel;
+    std::vector<int> admit;
+    const unsigned workers = cfg->mode == IRR_SERVE_SERIAL
+                                 ? 1u
+                                 : std::max(1u, std::min(std::thread::hardware_concurrency(), 16u));
+    cudaEvent_t ev_kd = nullptr;
+    cudaEventCreateWithFlags(&ev_kd, cudaEventDisableTiming);
     while (rc == IRR_OK && (next < order.size() || !live.empty())) {
         // admission, in arrival order, within the budget and the slot limit
         while (next < order.size()) {
@@ -250,27 +277,44 @@ int irr_serve_run(const irr_serve_config* cfg, irr_serve_stats* st, irr_serve_jo
                 next++;
                 continue;
             }
-            if ((int)live.size() >= max_res || used + (double)j.est_bytes > cfg->budget_bytes) break;
-            irr_md_config mc;
-            irr_md_config_default(&mc);
-            mc.device = cfg->device;
-            mc.dt = cfg->dt;
-            mc.cutforce = cfg->cutforce;
-            mc.skin = cfg->skin;
-            mc.side = j.side;
-            mc.rebuild_every = cfg->rebuild_every;
-            irr_md* m = nullptr;
-            rc = irr_md_create(&mc, req_pos[order[next]].data(), req_vel[order[next]].data(), j.atoms, &m);
-            std::vector<double>().swap(req_pos[order[next]]);  // uploaded: release the host copy
-            std::vector<double>().swap(req_vel[order[next]]);
-            if (rc) break;
-            cudaStreamSynchronize(m->stream);
-            m->stream = s;
-            live.push_back(Live{order[next], m, 0, now(), 0.0});
+            if ((int)(live.size() + admit.size()) >= max_res ||
+                used + (double)j.est_bytes > cfg->budget_bytes)
+                break;
+            admit.push_back(order[next]);
             used += (double)j.est_bytes;
             peak = std::max(peak, used);
-            st->max_resident = std::max<int64_t>(st->max_resident, (int64_t)live.size());
             next++;
+        }
+        if (!admit.empty()) {
+            // the admitted jobs' set-up (upload + first neighbour build and
+            // partition) runs concurrently, each on its own stream
+            std::vector<irr_md*> made(admit.size(), nullptr);
+            std::vector<int> made_rc(admit.size(), IRR_OK);
+            run_parallel(admit.size(), workers, cfg->device, [&](size_t i) {
+                const int id = admit[i];
+                const JobSpec& j = jobs[id];
+                irr_md_config mc;
+                irr_md_config_default(&mc);
+                mc.device = cfg->device;
+                mc.dt = cfg->dt;
+                mc.cutforce = cfg->cutforce;
+                mc.skin = cfg->skin;
+                mc.side = j.side;
+                mc.rebuild_every = cfg->rebuild_every;
+                made_rc[i] = irr_md_create(&mc, req_pos[id].data(), req_vel[id].data(), j.atoms, &made[i]);
+                std::vector<double>().swap(req_pos[id]);  // uploaded: release the host copy
+                std::vector<double>().swap(req_vel[id]);
+            });
+            for (size_t i = 0; i < admit.size(); i++) {
+                if (made_rc[i] != IRR_OK) {
+                    if (rc == IRR_OK) rc = made_rc[i];
+                    continue;
+                }
+                made[i]->stream = s;
+                live.push_back(Live{admit[i], made[i], 0, now(), 0.0});
+            }
+            st->max_resident = std::max<int64_t>(st->max_resident, (int64_t)live.size());
+            admit.clear();
         }
         if (rc) break;
         if (live.empty()) {
@@ -283,14 +327,32 @@ int irr_serve_run(const irr_serve_config* cfg, irr_serve_stats* st, irr_serve_jo
         // one tick: every resident job advances one step
         std::vector<InstDesc> insts;
         std::vector<WorkItem> items;
+        std::vector<size_t> due;
         for (size_t k = 0; k < live.size() && rc == IRR_OK; k++) {
             irr_md* m = live[k].md;
             rc = md_kick_drift(m);
-            if (!rc && m->since_rebuild >= m->cfg.rebuild_every) {
-                rc = md_rebuild(m);
+            if (!rc && m->since_rebuild >= m->cfg.rebuild_every) due.push_back(k);
+        }
+        if (rc) break;
+        if (!due.empty()) {
+            // rebuilds that are due run concurrently, each on its job's own
+            // stream after this tick's kick-drift; md_rebuild returns once its
+            // stream is done, so the force launch below sees the new layouts
+            cudaEventRecord(ev_kd, s);
+            std::vector<int> due_rc(due.size(), IRR_OK);
+            run_parallel(due.size(), workers, cfg->device, [&](size_t i) {
+                irr_md* m = live[due[i]].md;
+                m->stream = m->own_stream;
+                cudaStreamWaitEvent(m->stream, ev_kd, 0);
+                due_rc[i] = md_rebuild(m);
                 m->stream = s;
-            }
+            });
+            for (int r : due_rc)
+                if (r != IRR_OK && rc == IRR_OK) rc = r;
             if (rc) break;
+        }
+        for (size_t k = 0; k < live.size() && rc == IRR_OK; k++) {
+            irr_md* m = live[k].md;
             insts.push_back(md_instance(m));
             for (WorkItem w : m->host_items) {
                 w.inst = (int)k;
@@ -324,38 +386,49 @@ int irr_serve_run(const irr_serve_config* cfg, irr_serve_stats* st, irr_serve_jo
         if (rc) break;
         // the host copies of the tables are reused next tick: wait for this one
         if (cudaStreamSynchronize(s) != cudaSuccess) { rc = IRR_ERR_CUDA; break; }
-        // retire finished jobs
-        for (size_t k = 0; k < live.size();) {
-            if (live[k].steps < cfg->steps_per_job) { k++; continue; }
-            Live L = live[k];
-            const JobSpec& j = jobs[L.id];
+        // retire finished jobs: their results (final state hash, energy) are
+        // read back and their memory freed concurrently, each on its own stream
+        std::vector<size_t> fin;
+        for (size_t k = 0; k < live.size(); k++)
+            if (live[k].steps >= cfg->steps_per_job) fin.push_back(k);
+        if (!fin.empty()) {
             const double done = now();
-            latency.push_back(done - j.arrival);
-            pair_evals += L.pair_evals;
-            if (out) {
-                irr_serve_job r{};
-                r.atoms = j.atoms;
-                r.edges = L.md->edges;
-                r.arrival_s = j.arrival;
-                r.admit_s = L.admit_s;
-                r.done_s = done;
-                hpos.resize(3 * j.atoms);
-                irr_md_get_state(L.md, hpos.data(), nullptr);
-                r.state_hash = fnv1a(hpos.data(), sizeof(double) * hpos.size());
-                double ke = 0, pe = 0;
-                irr_md_energy(L.md, &ke, &pe, nullptr);
-                r.energy = ke + pe;
-                r.status = IRR_OK;
-                out[L.id] = r;
+            run_parallel(fin.size(), workers, cfg->device, [&](size_t i) {
+                const Live& L = live[fin[i]];
+                const JobSpec& j = jobs[L.id];
+                L.md->stream = L.md->own_stream;
+                if (out) {
+                    irr_serve_job r{};
+                    r.atoms = j.atoms;
+                    r.edges = L.md->edges;
+                    r.arrival_s = j.arrival;
+                    r.admit_s = L.admit_s;
+                    r.done_s = done;
+                    std::vector<double> state(3 * (size_t)j.atoms);
+                    irr_md_get_state(L.md, state.data(), nullptr);
+                    r.state_hash = fnv1a(state.data(), sizeof(double) * state.size());
+                    double ke = 0, pe = 0;
+                    irr_md_energy(L.md, &ke, &pe, nullptr);
+                    r.energy = ke + pe;
+                    r.status = IRR_OK;
+                    out[L.id] = r;
+                }
+                irr_md_destroy(L.md);
+            });
+            for (size_t i = fin.size(); i-- > 0;) {
+                const Live& L = live[fin[i]];
+                const JobSpec& j = jobs[L.id];
+                latency.push_back(done - j.arrival);
+                pair_evals += L.pair_evals;
+                used -= (double)j.est_bytes;
+                live.erase(live.begin() + fin[i]);
+                st->jobs_done++;
             }
-            irr_md_destroy(L.md);
-            used -= (double)j.est_bytes;
-            live.erase(live.begin() + k);
-            st->jobs_done++;
         }
     }
     const double makespan = now();
     for (auto& L : live) irr_md_destroy(L.md);
+    if (ev_kd) cudaEventDestroy(ev_kd);
     int dev_status = 0;
     cudaMemcpy(&dev_status, d_status, sizeof(int), cudaMemcpyDeviceToHost);
     if (d_insts) cudaFree(d_insts);
