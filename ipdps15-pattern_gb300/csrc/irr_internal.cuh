@@ -162,9 +162,11 @@ cudaError_t build_partition(const float4* pos_user, int64_t n, const int2* edges
                             int reorder, PartitionOut* out, cudaStream_t s);
 // Half neighbour list (irr_neighbor.cu); *d_edges is cudaMalloc'd, or, with
 // stream_ordered, cudaMallocAsync'd on s (free it with cudaFreeAsync).
+// sort_rows == false leaves each row's partners in cell-scan order (for a
+// caller that re-sorts them anyway, like the partitioner).
 cudaError_t build_neighbor_list(const float4* pos, int64_t n, float box, float cut2,
                                 int2** d_edges, int64_t* num_edges, cudaStream_t s,
-                                bool stream_ordered = false);
+                                bool stream_ordered = false, bool sort_rows = true);
 // Sorts each row of a CSR (row_off[n + 1], col) ascending; every row must
 // hold at most kRowSortMax entries.
 constexpr int kRowSortMax = 1024;

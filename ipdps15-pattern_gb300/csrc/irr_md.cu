@@ -263,8 +263,10 @@ int md_rebuild(irr_md* m)
     const double lc = m->cfg.cutforce + m->cfg.skin;
     int2* d_edges = nullptr;
     int64_t e = 0;
+    // the partition lays the entries out in (row, col) order itself: the
+    // half list's rows need no sort here
     MD_CUDA(m, build_neighbor_list(m->pos4, m->n, (float)m->cfg.side, (float)(lc * lc), &d_edges, &e, s,
-                                   true),
+                                   true, false),
             "neighbour build");
     free_part(m, s);
     PartitionOut p;

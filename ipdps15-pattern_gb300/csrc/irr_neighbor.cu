@@ -150,7 +150,7 @@ int grid_of(int64_t n)
 // stream_ordered (2 * *num_edges int32).
 cudaError_t build_neighbor_list(const float4* pos, int64_t n, float box, float cut2,
                                 int2** d_edges, int64_t* num_edges, cudaStream_t s,
-                                bool stream_ordered)
+                                bool stream_ordered, bool sort_rows)
 {
     *d_edges = nullptr;
     *num_edges = 0;
@@ -228,13 +228,13 @@ cudaError_t build_neighbor_list(const float4* pos, int64_t n, float box, float c
     int2* edges = nullptr;
     if (total > 0) {
         uint32_t longest = 0;
-        IRR_CUDA_TRY(max_row_len(cnt, n, &longest, s));
+        if (sort_rows) IRR_CUDA_TRY(max_row_len(cnt, n, &longest, s));
         const int sort_here = longest > (uint32_t)kRowSortMax;
         IRR_CUDA_TRY(cudaMallocAsync((void**)&nbr, sizeof(int32_t) * total, s));
         pairs_kernel<true><<<grid_of(n), 256, 0, s>>>(pos, sorted, cell_start, n, g, nullptr, cnt,
                                                       nbr, sort_here);
         IRR_CUDA_TRY(cudaGetLastError());
-        if (!sort_here) IRR_CUDA_TRY(launch_row_sort(cnt, n, nbr, s));
+        if (sort_rows && !sort_here) IRR_CUDA_TRY(launch_row_sort(cnt, n, nbr, s));
         if (stream_ordered)
             IRR_CUDA_TRY(cudaMallocAsync((void**)&edges, sizeof(int2) * total, s));
         else
