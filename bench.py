@@ -348,7 +348,7 @@ def run_ours(args, rank, world, local):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded uniform-random positions; edge list built on the GPU)",
         "config": {"workload": workload_name(n), "nodes": n, "edges": E,
-                   "exec": "partitioned (Morton blocks, owner-computes tiled kernel)",
+                   "exec": "partitioned (Hilbert-ordered node blocks, sliced entries, owner-computes tiled kernel)",
                    "lanes_per_row": info.lanes_per_row, "stage_smem": info.stage_smem,
                    "l2": "inputs larger than L2 (1.07 GB entry stream read every step)",
                    "parallelism": f"replicas x{world}"},

@@ -73,11 +73,21 @@ enum irr_exec {
      * contributions added with global float4 atomics.  The straightforward
      * GPU form of compute_gpu (moldyn/irregular/gpu_kernel.cu:21-103). */
     IRR_EXEC_PLAIN = 0,
-    /* GPU partitioner (Morton order, shared-memory-sized node blocks, edges
+    /* GPU partitioner (Hilbert or Morton order, shared-memory-sized node blocks, edges
      * binned by owning block) and the tiled owner-computes kernel.  Each node
      * sums its own contributions in registers with compensated (two-sum)
      * partials; no atomics; results are bitwise reproducible. */
     IRR_EXEC_PARTITIONED = 1
+};
+
+/* Partitioned: the curve that orders the nodes (both quantise each axis of
+ * the bounding box to 10 bits; ties keep the caller's order). */
+enum irr_order {
+    /* Hilbert curve (default): consecutive nodes are always face-adjacent
+     * cells, so a block's neighbourhood touches fewer cache lines. */
+    IRR_ORDER_HILBERT = 0,
+    /* Morton (Z-order) curve: the order irr_morton_order_static returns. */
+    IRR_ORDER_MORTON = 1
 };
 
 /* Partitioned: how each node block's directed entries are laid out. */
@@ -117,13 +127,14 @@ typedef struct irr_config {
                           0 = tuned default                                          */
     int lanes_per_row; /* partitioned: lanes summing one node's row (1, 2, 4, 8, 16,
                           32); 0 = tuned default                                     */
-    int reorder;       /* partitioned: 1 = Morton order (default), 0 = keep the
+    int reorder;       /* partitioned: 1 = curve order (default, see order), 0 = keep the
                           caller's order (blocks are then cut from it)              */
     int stage_smem;    /* partitioned: 1 = copy each block's entries (neighbour ids)
                           into a shared-memory ring with a bulk (TMA) copy, 0 = read
                           them from global memory; -1 = tuned default               */
     int layout;        /* partitioned: enum irr_layout                               */
-    int reserved[7];
+    int order;         /* partitioned with reorder: enum irr_order                   */
+    int reserved[6];
 } irr_config;
 
 typedef struct irr_handle irr_handle;
@@ -140,7 +151,7 @@ typedef struct irr_info {
     int32_t stage_smem;
     int32_t exec;
     int32_t layout;          /* enum irr_layout in use (CSR or SLICED)              */
-    int32_t reserved;
+    int32_t order;           /* enum irr_order of the node order                    */
     int64_t num_slots;       /* entry slots stored: num_entries plus padding        */
 } irr_info;
 
@@ -409,7 +420,7 @@ IRR_API int irr_serve_run(const irr_serve_config *cfg, irr_serve_stats *stats,
 /* ------------------------------------------------ allocation-free ordering
  * No counterpart in the reference.  The partitioner's Morton node ordering
  * (perm[new] = old node id, bit for bit the perm that irr_get_partition
- * returns for reorder = 1) for callers that cannot allocate device memory --
+ * returns for reorder = 1, order = IRR_ORDER_MORTON) for callers that cannot allocate device memory --
  * an application that has already reserved the GPU's memory for its own
  * pool, or a latency-bound loop where cudaMalloc/cudaFree (which may
  * synchronise the device) are not acceptable.  It calls no allocator: its

@@ -314,6 +314,7 @@ int irr_create(const irr_config* cfg, irr_handle** out)
     if (c.block_nodes != 0 && (c.block_nodes < 64 || c.block_nodes > 4096 || (c.block_nodes & (c.block_nodes - 1))))
         return IRR_ERR_ARG;
     if (c.layout < IRR_LAYOUT_AUTO || c.layout > IRR_LAYOUT_SLICED) return IRR_ERR_ARG;
+    if (c.order != IRR_ORDER_HILBERT && c.order != IRR_ORDER_MORTON) return IRR_ERR_ARG;
     if (c.lanes_per_row != 0 && c.lanes_per_row != 1 && c.lanes_per_row != 2 && c.lanes_per_row != 4 &&
         c.lanes_per_row != 8 && c.lanes_per_row != 16 && c.lanes_per_row != 32)
         return IRR_ERR_ARG;
@@ -475,7 +476,7 @@ int irr_init(irr_handle* h)
     // partitioned: positions in the caller's order feed the partitioner
     H_CUDA(h, launch_load_nodes(h->d_raw, h->raw_elm, nullptr, n, h->d_pos, s), "load node data");
     PartitionOut p;
-    cudaError_t pe = build_partition(h->d_pos, n, h->d_edges, e, h->cfg.reorder, &p, s);
+    cudaError_t pe = build_partition(h->d_pos, n, h->d_edges, e, h->cfg.reorder, &p, s, h->cfg.order);
     h->part = p;
     if (pe != cudaSuccess) {
         free_layout(h);
@@ -575,6 +576,7 @@ int irr_get_info(const irr_handle* h, irr_info* info)
     info->stage_smem = h->shape.stage_smem;
     info->exec = h->cfg.exec;
     info->layout = h->sl.lanes ? IRR_LAYOUT_SLICED : IRR_LAYOUT_CSR;
+    info->order = h->cfg.order;
     info->num_slots = h->sl.lanes ? h->sl.words : info->num_entries;
     return IRR_OK;
 }

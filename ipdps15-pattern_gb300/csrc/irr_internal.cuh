@@ -158,8 +158,9 @@ cudaError_t bbox_frame(const float4* pos, int64_t n, float lo[3], float scale[3]
                        cudaStream_t s);
 // Full partition of n nodes and e half edges.  Allocates out's arrays with
 // cudaMallocAsync on s (caller frees).  reorder == 0 keeps the identity order.
+// curve: 0 = Hilbert (IRR_ORDER_HILBERT), 1 = Morton.
 cudaError_t build_partition(const float4* pos_user, int64_t n, const int2* edges, int64_t e,
-                            int reorder, PartitionOut* out, cudaStream_t s);
+                            int reorder, PartitionOut* out, cudaStream_t s, int curve = 0);
 // Half neighbour list (irr_neighbor.cu); *d_edges is cudaMalloc'd, or, with
 // stream_ordered, cudaMallocAsync'd on s (free it with cudaFreeAsync).
 // sort_rows == false leaves each row's partners in cell-scan order (for a

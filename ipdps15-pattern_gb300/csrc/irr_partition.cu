@@ -6,8 +6,9 @@
 // every edge into the part of each endpoint with std::vector push_back
 // (partitioner.cpp:142-297), then part_index (:490-499).  Here the whole pass
 // runs on the GPU and is deterministic:
-//   1. Morton key per node: each axis quantised to 10 bits in the bounding
-//      box frame (float ops, each rounded), bits interleaved;
+//   1. a curve key per node: each axis quantised to 10 bits in the bounding
+//      box frame (float ops, each rounded), then the cell's Hilbert index
+//      (default) or Morton index (bits interleaved);
 //   2. stable LSD radix sort of (key, node) -> perm[new] = old, inv[old] = new;
 //   3. every half edge (i, j) at list position t becomes the directed entries
 //      (inv[i] <- inv[j]) and (inv[j] <- inv[i]), laid out in (row, col)
@@ -283,15 +284,51 @@ __device__ __forceinline__ uint32_t quant10(float x, float lo, float scale)
     return __float2uint_rz(t);
 }
 
-__global__ void morton_kernel(const float4* pos, int64_t n, float3 lo, float3 scale,
-                              uint32_t* keys, int32_t* vals)
+// Hilbert index of a cell on the 2^10-per-axis grid: Skilling's transform
+// (J. Skilling, "Programming the Hilbert curve", AIP Conf. Proc. 707, 2004)
+// from axes to the transposed index, whose bits are then interleaved, axis 0
+// in the high bit of each 3-bit group.  The oracle restates it bit for bit.
+__device__ __forceinline__ uint32_t hilbert10(uint32_t x0, uint32_t x1, uint32_t x2)
+{
+    uint32_t X[3] = {x0, x1, x2};
+    for (uint32_t Q = 1u << 9; Q > 1; Q >>= 1) {
+        const uint32_t P = Q - 1;
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            if (X[i] & Q) {
+                X[0] ^= P;  // invert
+            } else {
+                const uint32_t t = (X[0] ^ X[i]) & P;  // exchange
+                X[0] ^= t;
+                X[i] ^= t;
+            }
+        }
+    }
+    X[1] ^= X[0];  // Gray encode
+    X[2] ^= X[1];
+    uint32_t t = 0;
+    for (uint32_t Q = 1u << 9; Q > 1; Q >>= 1)
+        if (X[2] & Q) t ^= Q - 1;
+    X[0] ^= t;
+    X[1] ^= t;
+    X[2] ^= t;
+    uint32_t key = 0;
+    for (int b = 9; b >= 0; b--)
+        key = (key << 3) | (((X[0] >> b) & 1u) << 2) | (((X[1] >> b) & 1u) << 1) | ((X[2] >> b) & 1u);
+    return key;
+}
+
+// Curve key of each node (curve 0: Hilbert, 1: Morton) on the 10-bit grid.
+__global__ void curve_key_kernel(const float4* pos, int64_t n, float3 lo, float3 scale, int curve,
+                                 uint32_t* keys, int32_t* vals)
 {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x) {
         const float4 p = pos[i];
-        keys[i] = spread3(quant10(p.x, lo.x, scale.x)) |
-                  (spread3(quant10(p.y, lo.y, scale.y)) << 1) |
-                  (spread3(quant10(p.z, lo.z, scale.z)) << 2);
+        const uint32_t qx = quant10(p.x, lo.x, scale.x), qy = quant10(p.y, lo.y, scale.y),
+                       qz = quant10(p.z, lo.z, scale.z);
+        keys[i] = curve == 0 ? hilbert10(qx, qy, qz)
+                             : (spread3(qx) | (spread3(qy) << 1) | (spread3(qz) << 2));
         vals[i] = (int32_t)i;
     }
 }
@@ -589,7 +626,7 @@ cudaError_t max_row_len(const uint32_t* row_off, int64_t n, uint32_t* result, cu
 }
 
 cudaError_t build_partition(const float4* pos_user, int64_t n, const int2* edges, int64_t e,
-                            int reorder, PartitionOut* out, cudaStream_t s)
+                            int reorder, PartitionOut* out, cudaStream_t s, int curve)
 {
     if (n < 0 || e < 0 || n > 0x7fffffffLL || 2 * e > 0xffffffffLL) return cudaErrorInvalidValue;
     *out = PartitionOut{};
@@ -609,8 +646,9 @@ cudaError_t build_partition(const float4* pos_user, int64_t n, const int2* edges
         IRR_CUDA_TRY(alloc_async(&keys, n, s));
         IRR_CUDA_TRY(alloc_async(&keys_tmp, n, s));
         IRR_CUDA_TRY(alloc_async(&vals_tmp, n, s));
-        morton_kernel<<<g, 256, 0, s>>>(pos_user, n, make_float3(lo[0], lo[1], lo[2]),
-                                        make_float3(scale[0], scale[1], scale[2]), keys, out->perm);
+        curve_key_kernel<<<g, 256, 0, s>>>(pos_user, n, make_float3(lo[0], lo[1], lo[2]),
+                                           make_float3(scale[0], scale[1], scale[2]), curve, keys,
+                                           out->perm);
         IRR_CUDA_TRY(cudaGetLastError());
         IRR_CUDA_TRY(radix_sort_pairs(keys, out->perm, keys_tmp, vals_tmp, n, 30, s));
         IRR_CUDA_TRY(cudaFreeAsync(keys, s));

@@ -25,7 +25,7 @@
 //   of a warp start at unrelated offsets, so its reads of the stage collide
 //   in shared-memory banks.  Slices (consume_sliced, struct Sliced): the
 //   rows of a warp are interleaved and padded, so each step of the warp is
-//   one contiguous 256-byte read and the trip count is uniform; with Morton-
+//   one contiguous 256-byte read and the trip count is uniform; with curve-
 //   ordered rows whose columns ascend, the lanes of one gather also land on
 //   few cache lines.
 #include <algorithm>

@@ -36,6 +36,8 @@ IRR_MAP_LJ_MINIMD_PBC = 2
 IRR_REDUCE_SUM = 0
 IRR_EXEC_PLAIN = 0
 IRR_EXEC_PARTITIONED = 1
+IRR_ORDER_HILBERT = 0
+IRR_ORDER_MORTON = 1
 IRR_LAYOUT_AUTO = 0
 IRR_LAYOUT_CSR = 1
 IRR_LAYOUT_SLICED = 2
@@ -51,7 +53,7 @@ class Config(C.Structure):
     _fields_ = [("device", C.c_int), ("exec", C.c_int), ("map_idx", C.c_int),
                 ("reduce_idx", C.c_int), ("block_nodes", C.c_int), ("lanes_per_row", C.c_int),
                 ("reorder", C.c_int), ("stage_smem", C.c_int), ("layout", C.c_int),
-                ("reserved", C.c_int * 7)]
+                ("order", C.c_int), ("reserved", C.c_int * 6)]
 
 
 class Info(C.Structure):
@@ -59,7 +61,7 @@ class Info(C.Structure):
                 ("num_blocks", C.c_int64), ("device_bytes", C.c_int64),
                 ("block_nodes", C.c_int32), ("lanes_per_row", C.c_int32),
                 ("stage_smem", C.c_int32), ("exec", C.c_int32), ("layout", C.c_int32),
-                ("reserved", C.c_int32), ("num_slots", C.c_int64)]
+                ("order", C.c_int32), ("num_slots", C.c_int64)]
 
 
 class MDConfig(C.Structure):

@@ -589,14 +589,65 @@ void orc_morton_keys(int64_t n, const float *pos, const float lo[3], const float
     }
 }
 
+/* Hilbert index of a cell on the 2^10-per-axis grid: Skilling's transform
+ * (J. Skilling, "Programming the Hilbert curve", AIP Conf. Proc. 707, 2004)
+ * from axes to the transposed index, whose bits are then interleaved with
+ * axis 0 in the highest position of each 3-bit group. */
+static uint32_t hilbert10(uint32_t x0, uint32_t x1, uint32_t x2)
+{
+    uint32_t X[3] = {x0, x1, x2};
+    for (uint32_t Q = 1u << 9; Q > 1; Q >>= 1) {
+        const uint32_t P = Q - 1;
+        for (int i = 0; i < 3; i++) {
+            if (X[i] & Q) {
+                X[0] ^= P;  /* invert */
+            } else {
+                const uint32_t t = (X[0] ^ X[i]) & P;  /* exchange */
+                X[0] ^= t;
+                X[i] ^= t;
+            }
+        }
+    }
+    X[1] ^= X[0]; /* Gray encode */
+    X[2] ^= X[1];
+    uint32_t t = 0;
+    for (uint32_t Q = 1u << 9; Q > 1; Q >>= 1)
+        if (X[2] & Q) t ^= Q - 1;
+    X[0] ^= t;
+    X[1] ^= t;
+    X[2] ^= t;
+    uint32_t key = 0;
+    for (int b = 9; b >= 0; b--)
+        key = (key << 3) | (((X[0] >> b) & 1u) << 2) | (((X[1] >> b) & 1u) << 1) | ((X[2] >> b) & 1u);
+    return key;
+}
+
+void orc_hilbert_keys(int64_t n, const float *pos, const float lo[3], const float scale[3],
+                      uint32_t *keys)
+{
+    for (int64_t i = 0; i < n; i++)
+        keys[i] = hilbert10(quant10(pos[3 * i], lo[0], scale[0]), quant10(pos[3 * i + 1], lo[1], scale[1]),
+                            quant10(pos[3 * i + 2], lo[2], scale[2]));
+}
+
 int orc_partition(int64_t n, const float *pos, const float lo[3], const float scale[3],
                   int64_t e, const int32_t *edges, int32_t *perm, int32_t *inv,
                   int64_t *row_off, int32_t *col)
 {
+    return orc_partition_curve(n, pos, lo, scale, 1, e, edges, perm, inv, row_off, col);
+}
+
+int orc_partition_curve(int64_t n, const float *pos, const float lo[3], const float scale[3],
+                        int curve, int64_t e, const int32_t *edges, int32_t *perm, int32_t *inv,
+                        int64_t *row_off, int32_t *col)
+{
     if (n < 0 || e < 0) return -1;
     uint32_t *keys = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)(n > 0 ? n : 1));
     if (!keys) return -1;
-    orc_morton_keys(n, pos, lo, scale, keys);
+    if (curve == 0)
+        orc_hilbert_keys(n, pos, lo, scale, keys);
+    else
+        orc_morton_keys(n, pos, lo, scale, keys);
     /* Stable counting sort on the 30-bit key, 3 passes of 10 bits. */
     int32_t *a = (int32_t *)malloc(sizeof(int32_t) * (size_t)(n > 0 ? n : 1));
     int32_t *b = (int32_t *)malloc(sizeof(int32_t) * (size_t)(n > 0 ? n : 1));

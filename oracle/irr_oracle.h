@@ -126,6 +126,14 @@ void orc_morton_keys(int64_t n, const float *pos, const float lo[3], const float
 int orc_partition(int64_t n, const float *pos, const float lo[3], const float scale[3],
                   int64_t e, const int32_t *edges, int32_t *perm, int32_t *inv,
                   int64_t *row_off, int32_t *col);
+/* Hilbert keys on the same 10-bit grid (Skilling's transposed index, axis 0
+ * in the high bit of each 3-bit group), and the partition ordered by either
+ * curve: curve 0 = Hilbert, 1 = Morton (orc_partition). */
+void orc_hilbert_keys(int64_t n, const float *pos, const float lo[3], const float scale[3],
+                      uint32_t *keys);
+int orc_partition_curve(int64_t n, const float *pos, const float lo[3], const float scale[3],
+                        int curve, int64_t e, const int32_t *edges, int32_t *perm, int32_t *inv,
+                        int64_t *row_off, int32_t *col);
 
 #ifdef __cplusplus
 }

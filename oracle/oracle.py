@@ -67,6 +67,9 @@ def lib():
         L.orc_morton_keys.argtypes = [i64, P, P, P, P]
         L.orc_partition.argtypes = [i64, P, P, P, i64, P, P, P, P, P]
         L.orc_partition.restype = C.c_int
+        L.orc_hilbert_keys.argtypes = [i64, P, P, P, P]
+        L.orc_partition_curve.argtypes = [i64, P, P, P, C.c_int, i64, P, P, P, P, P]
+        L.orc_partition_curve.restype = C.c_int
         _lib = L
     return _lib
 
@@ -228,8 +231,18 @@ def morton_keys(pos32, lo, scale) -> np.ndarray:
     return keys
 
 
-def partition(pos32, lo, scale, edges):
-    """Returns (perm, inv, row_off, col) of the bit-exact partition oracle."""
+def hilbert_keys(pos32, lo, scale) -> np.ndarray:
+    pos32 = np.ascontiguousarray(pos32, np.float32).reshape(-1, 3)
+    lo = np.ascontiguousarray(lo, np.float32)
+    scale = np.ascontiguousarray(scale, np.float32)
+    keys = np.zeros(pos32.shape[0], np.uint32)
+    lib().orc_hilbert_keys(pos32.shape[0], _p(pos32), _p(lo), _p(scale), _p(keys))
+    return keys
+
+
+def partition(pos32, lo, scale, edges, curve: str = "morton"):
+    """Returns (perm, inv, row_off, col) of the bit-exact partition oracle;
+    nodes ordered along the Morton or the Hilbert curve."""
     pos32 = np.ascontiguousarray(pos32, np.float32).reshape(-1, 3)
     edges = _edges(edges)
     n = pos32.shape[0]
@@ -240,8 +253,8 @@ def partition(pos32, lo, scale, edges):
     inv = np.zeros(n, np.int32)
     row_off = np.zeros(n + 1, np.int64)
     col = np.zeros(max(2 * e, 1), np.int32)
-    rc = lib().orc_partition(n, _p(pos32), _p(lo), _p(scale), e, _p(edges), _p(perm), _p(inv),
-                             _p(row_off), _p(col))
+    rc = lib().orc_partition_curve(n, _p(pos32), _p(lo), _p(scale), 0 if curve == "hilbert" else 1,
+                                   e, _p(edges), _p(perm), _p(inv), _p(row_off), _p(col))
     if rc != 0:
         raise ValueError(f"orc_partition failed ({rc})")
     return perm, inv, row_off, col[: 2 * e]

@@ -65,12 +65,13 @@ def test_parity_golden(built_lib, oracle_lib, name, shape):
 
 
 @pytest.mark.parametrize("name", golden_names())
-@pytest.mark.parametrize("reorder", [1, 0])
-def test_partition_bit_exact(built_lib, oracle_lib, name, reorder):
+@pytest.mark.parametrize("reorder,curve", [(1, "hilbert"), (1, "morton"), (0, "morton")])
+def test_partition_bit_exact(built_lib, oracle_lib, name, reorder, curve):
     import irregular_gb300 as irr
     O = oracle_lib
     c = load_golden(name)
-    h = irr.Handle(irr.default_config(map_idx=map_idx_of(c), exec=1, reorder=reorder))
+    order = irr.IRR_ORDER_HILBERT if curve == "hilbert" else irr.IRR_ORDER_MORTON
+    h = irr.Handle(irr.default_config(map_idx=map_idx_of(c), exec=1, reorder=reorder, order=order))
     h.set_params(c["param"])
     h.set_edges(c["edges"])
     h.set_nodes(c["pos"], 24)
@@ -81,7 +82,8 @@ def test_partition_bit_exact(built_lib, oracle_lib, name, reorder):
         lo, scale = O.morton_frame(pos32)
     else:
         lo, scale = np.zeros(3, np.float32), np.zeros(3, np.float32)  # all keys 0: identity
-    operm, oinv, orow, ocol = O.partition(pos32, lo, scale, c["edges"])
+    operm, oinv, orow, ocol = O.partition(pos32, lo, scale, c["edges"], curve=curve)
+    assert h.info().order == order
     assert np.array_equal(perm, operm)
     assert np.array_equal(row_off, orow)
     assert np.array_equal(col, ocol)

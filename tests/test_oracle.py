@@ -125,3 +125,23 @@ def test_partition_oracle_properties(oracle_lib):
     shuf[flip] = shuf[flip][:, ::-1]
     _, _, row_off2, col2 = O.partition(pos32, lo, scale, shuf)
     assert np.array_equal(row_off2, row_off) and np.array_equal(col2, col)
+
+
+def test_hilbert_keys_walk_the_grid(oracle_lib):
+    """The partition's Hilbert key: the first 8^4 keys fill the 16^3 corner
+    cube, each key's cell is face-adjacent to the next one's, and distinct
+    cells get distinct keys."""
+    O = oracle_lib
+    g = np.arange(16, dtype=np.float32)
+    cells = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3) + np.float32(0.5)
+    lo = np.zeros(3, np.float32)
+    scale = np.ones(3, np.float32)  # quantisation: cell (i, j, k) -> (i, j, k)
+    keys = O.hilbert_keys(cells, lo, scale)
+    assert np.array_equal(np.sort(keys), np.arange(16 ** 3, dtype=np.uint32))
+    path = cells[np.argsort(keys)]
+    assert np.all(np.abs(np.diff(path, axis=0)).sum(axis=1) == 1)
+    rng = np.random.default_rng(3)
+    far = rng.integers(0, 1024, size=(1024, 3)).astype(np.float32) + np.float32(0.5)
+    far = np.unique(far, axis=0)
+    assert np.unique(O.hilbert_keys(far, lo, scale)).size == far.shape[0]
+

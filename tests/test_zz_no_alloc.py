@@ -21,7 +21,7 @@ pytestmark = pytest.mark.gpu
 def partitioner_perm(irr, pos32):
     """The existing path: a partitioned handle's Morton permutation."""
     h = irr.Handle(irr.default_config(map_idx=irr.IRR_MAP_LJ_MOLDYN, exec=irr.IRR_EXEC_PARTITIONED,
-                                      reorder=1))
+                                      reorder=1, order=irr.IRR_ORDER_MORTON))
     h.set_params(irr.moldyn_params(1000.0, 2.5))
     h.set_edges(np.zeros((0, 2), np.int32))
     h.set_nodes(pos32, 12)
