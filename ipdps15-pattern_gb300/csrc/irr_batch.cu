@@ -145,7 +145,7 @@ std::string tune_key(int device, int64_t instances, int64_t nodes, int64_t entri
     cudaGetDeviceProperties(&prop, device);
     const double per_inst = instances > 0 ? (double)nodes / instances : 0.0;
     const double per_row = nodes > 0 ? (double)entries / nodes : 0.0;
-    char buf[256];
+    char buf[512];
     snprintf(buf, sizeof(buf), "%s|sm%d|inst2^%d|nodes2^%d|deg2^%d|p%d", prop.name, prop.multiProcessorCount,
              (int)std::lround(std::log2((double)std::max<int64_t>(instances, 1))),
              (int)std::lround(std::log2(std::max(per_inst, 1.0))),

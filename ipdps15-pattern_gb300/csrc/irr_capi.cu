@@ -132,6 +132,7 @@ int upload_inst(irr_handle* h)
     d.scol = h->sl.lanes ? h->sl.col : nullptr;
     d.law = h->law;
     d.n = h->n;
+    h->inst = d;
     H_CUDA(h, cudaMemcpyAsync(h->d_inst, &d, sizeof(d), cudaMemcpyHostToDevice, h->stream),
            "upload instance descriptor");
     H_CUDA(h, cudaStreamSynchronize(h->stream), "upload instance descriptor");
@@ -520,7 +521,7 @@ int irr_step(irr_handle* h)
     }
     H_CUDA(h, cudaMemsetAsync(h->d_queue, 0, sizeof(int), h->stream), "clear work queue");
     H_CUDA(h, launch_tiled(h->shape, h->d_inst, h->d_items, h->num_items, h->d_queue,
-                           h->sms * kCtasPerSm, h->d_status, h->stream),
+                           h->sms * kCtasPerSm, h->d_status, h->stream, &h->inst),
            "tiled kernel");
     return IRR_OK;
 }

@@ -43,6 +43,7 @@ struct irr_handle {
     std::vector<uint32_t> host_row_off;  // host copy of part.row_off (cuts work items)
     irr::Sliced sl{};                    // sliced layout, when in use
     InstDesc* d_inst = nullptr;
+    InstDesc inst{};             // host copy of *d_inst (the single-instance launch parameter)
     WorkItem* d_items = nullptr;
     int num_items = 0;
     int* d_status = nullptr;

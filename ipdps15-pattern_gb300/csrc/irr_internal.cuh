@@ -127,11 +127,13 @@ inline bool sliced_pays(const Sliced& sl, int64_t entries)
 // -- reduction kernels (irr_reduce.cu) --
 cudaError_t launch_plain(const float4* pos, const int2* edges, int64_t e, float4* force,
                          const LawParams& law, cudaStream_t s);
-// queue == nullptr: one CTA per work item.  Otherwise a persistent grid of
-// `grid` CTAs draws items from *queue (which must be 0 at launch).
+// A persistent grid of `grid` CTAs draws items from *queue (which must be 0
+// at launch).  `one` (host copy of d_insts[0]) may be given when every item
+// belongs to instance 0: the kernel then takes the descriptor as a launch
+// parameter and keeps no instance fields in registers.
 cudaError_t launch_tiled(const TiledShape& shape, const InstDesc* d_insts,
                          const WorkItem* d_items, int num_items, int* d_queue, int grid,
-                         int* d_status, cudaStream_t s);
+                         int* d_status, cudaStream_t s, const InstDesc* one = nullptr);
 
 // -- data movement (irr_partition.cu) --
 // Raw node records (12/16/24 bytes) -> float4, optionally gathered: dst[k] =

@@ -311,6 +311,7 @@ int md_rebuild(irr_md* m)
     d.scol = m->sl.lanes ? m->sl.col : nullptr;
     d.law = m->law;
     d.n = m->n;
+    m->inst = d;
     MD_CUDA(m, cudaMemcpyAsync(m->d_inst, &d, sizeof(d), cudaMemcpyHostToDevice, s), "instance");
     MD_CUDA(m, cudaStreamSynchronize(s), "rebuild");
     m->edges = e;
@@ -324,7 +325,7 @@ int md_forces(irr_md* m)
 {
     MD_CUDA(m, cudaMemsetAsync(m->d_queue, 0, sizeof(int), m->stream), "queue");
     MD_CUDA(m, launch_tiled(m->shape, m->d_inst, m->d_items, m->num_items, m->d_queue,
-                            m->sms * kCtasPerSm, m->d_status, m->stream), "force kernel");
+                            m->sms * kCtasPerSm, m->d_status, m->stream, &m->inst), "force kernel");
     return IRR_OK;
 }
 

@@ -32,6 +32,7 @@ struct irr_md {
     PartitionOut part{};
     irr::Sliced sl{};          // sliced entry layout (when it pays)
     InstDesc* d_inst = nullptr;
+    InstDesc inst{};           // host copy of *d_inst (the force launch's parameter)
     WorkItem* d_items = nullptr;
     int num_items = 0;
     int* d_queue = nullptr;

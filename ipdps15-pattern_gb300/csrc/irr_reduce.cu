@@ -145,9 +145,8 @@ struct InstHot {
     HotLaw H;
 };
 
-__device__ __forceinline__ InstHot load_hot(const InstDesc* __restrict__ insts, int inst)
+__device__ __forceinline__ InstHot load_hot(const InstDesc* __restrict__ I)
 {
-    const InstDesc* __restrict__ I = insts + inst;
     InstHot h;
     h.pos = I->pos;
     h.row_off = I->row_off;
@@ -409,10 +408,15 @@ __device__ __forceinline__ void consume_sliced(const WorkItem& w, const InstHot&
 // suspend the thread until the phase completes (mbar_try_wait).  Every
 // wait is bounded; a wait that gives up sets kStatusWaitTimeout, waits once
 // more (bounded) for a copy that may be in flight, and leaves.
-template <bool PERIODIC, int G>
+//
+// ONE: every item belongs to instance 0, whose descriptor is the launch
+// parameter `one` (constant bank): its fields are read as operands where
+// they are used instead of being held in registers across items (at the
+// 56-register bound of 4 CTAs x 288 threads this removes the spills).
+template <bool PERIODIC, int G, bool ONE>
 __global__ void __launch_bounds__(kPipeThreads, kCtasPerSm) tiled_kernel(
     const InstDesc* __restrict__ insts, const WorkItem* __restrict__ items, int num_items,
-    int* queue, int* status, int use_stages)
+    int* queue, int* status, int use_stages, const __grid_constant__ InstDesc one)
 {
     extern __shared__ int4 smem_raw[];
     int32_t* stage_base = reinterpret_cast<int32_t*>(smem_raw);
@@ -458,8 +462,8 @@ __global__ void __launch_bounds__(kPipeThreads, kCtasPerSm) tiled_kernel(
                     s_smem[s] = 1;
                     const uint32_t a0 = w.ent0 & ~3u;
                     const uint32_t words = ((w.ent0 + w.nent - a0) + 3u) & ~3u;
-                    const int32_t* src =
-                        (w.flags & kItemSliced) ? insts[w.inst].scol : insts[w.inst].col;
+                    const InstDesc* I = ONE ? &one : insts + w.inst;
+                    const int32_t* src = (w.flags & kItemSliced) ? I->scol : I->col;
                     bulk_load(stage_base + s * kStageInts, src + a0, words * 4u, &full[s]);
                 }
             }
@@ -483,8 +487,11 @@ __global__ void __launch_bounds__(kPipeThreads, kCtasPerSm) tiled_kernel(
         const int it = s_item[s];
         if (it >= num_items) return;
         const WorkItem w = items[it];
-        if (w.inst != cur) {
-            hot = load_hot(insts, w.inst);
+        const InstDesc* I = ONE ? &one : insts + w.inst;
+        if (ONE) {
+            hot = load_hot(&one);
+        } else if (w.inst != cur) {
+            hot = load_hot(I);
             cur = w.inst;
         }
         if (w.flags & kItemSliced) {
@@ -492,23 +499,23 @@ __global__ void __launch_bounds__(kPipeThreads, kCtasPerSm) tiled_kernel(
                 consume_sliced<PERIODIC, G, true>(w, hot, stage_base + s * kStageInts, w.ent0, warp,
                                                   lane);
             else
-                consume_sliced<PERIODIC, G, false>(w, hot, insts[w.inst].scol, 0u, warp, lane);
+                consume_sliced<PERIODIC, G, false>(w, hot, I->scol, 0u, warp, lane);
         } else if (s_smem[s]) {
             consume_item<PERIODIC, G>(w, hot, stage_base + s * kStageInts, w.ent0 & ~3u, warp, lane);
         } else {
-            consume_item<PERIODIC, G>(w, hot, insts[w.inst].col, 0u, warp, lane);
+            consume_item<PERIODIC, G>(w, hot, I->col, 0u, warp, lane);
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(&empty[s]);
     }
 }
 
-template <bool PERIODIC, int G>
-cudaError_t launch_tiled_g(const TiledShape& shape, const InstDesc* d_insts,
-                           const WorkItem* d_items, int num_items, int* d_queue, int grid,
-                           int* d_status, cudaStream_t s)
+template <bool PERIODIC, int G, bool ONE>
+cudaError_t launch_tiled_one(const TiledShape& shape, const InstDesc* d_insts,
+                             const WorkItem* d_items, int num_items, int* d_queue, int grid,
+                             int* d_status, cudaStream_t s, const InstDesc& one)
 {
-    auto kern = tiled_kernel<PERIODIC, G>;
+    auto kern = tiled_kernel<PERIODIC, G, ONE>;
     const size_t smem =
         shape.stage_smem ? (size_t)kStages * (kStageEntries + kColPad) * sizeof(int32_t) : 0;
     if (smem > 48 * 1024)
@@ -516,21 +523,33 @@ cudaError_t launch_tiled_g(const TiledShape& shape, const InstDesc* d_insts,
                                           (int)smem));
     if (grid <= 0 || num_items <= 0) return cudaSuccess;
     kern<<<grid, kPipeThreads, smem, s>>>(d_insts, d_items, num_items, d_queue, d_status,
-                                          shape.stage_smem);
+                                          shape.stage_smem, one);
     return cudaGetLastError();
+}
+
+template <bool PERIODIC, int G>
+cudaError_t launch_tiled_g(const TiledShape& shape, const InstDesc* d_insts,
+                           const WorkItem* d_items, int num_items, int* d_queue, int grid,
+                           int* d_status, cudaStream_t s, const InstDesc* one)
+{
+    if (one)
+        return launch_tiled_one<PERIODIC, G, true>(shape, d_insts, d_items, num_items, d_queue,
+                                                   grid, d_status, s, *one);
+    return launch_tiled_one<PERIODIC, G, false>(shape, d_insts, d_items, num_items, d_queue, grid,
+                                                d_status, s, InstDesc{});
 }
 
 template <bool PERIODIC>
 cudaError_t launch_tiled_p(const TiledShape& sh, const InstDesc* a, const WorkItem* b, int n,
-                           int* q, int grid, int* st, cudaStream_t s)
+                           int* q, int grid, int* st, cudaStream_t s, const InstDesc* one)
 {
     switch (sh.lanes_per_row) {
-    case 1: return launch_tiled_g<PERIODIC, 1>(sh, a, b, n, q, grid, st, s);
-    case 2: return launch_tiled_g<PERIODIC, 2>(sh, a, b, n, q, grid, st, s);
-    case 4: return launch_tiled_g<PERIODIC, 4>(sh, a, b, n, q, grid, st, s);
-    case 8: return launch_tiled_g<PERIODIC, 8>(sh, a, b, n, q, grid, st, s);
-    case 16: return launch_tiled_g<PERIODIC, 16>(sh, a, b, n, q, grid, st, s);
-    case 32: return launch_tiled_g<PERIODIC, 32>(sh, a, b, n, q, grid, st, s);
+    case 1: return launch_tiled_g<PERIODIC, 1>(sh, a, b, n, q, grid, st, s, one);
+    case 2: return launch_tiled_g<PERIODIC, 2>(sh, a, b, n, q, grid, st, s, one);
+    case 4: return launch_tiled_g<PERIODIC, 4>(sh, a, b, n, q, grid, st, s, one);
+    case 8: return launch_tiled_g<PERIODIC, 8>(sh, a, b, n, q, grid, st, s, one);
+    case 16: return launch_tiled_g<PERIODIC, 16>(sh, a, b, n, q, grid, st, s, one);
+    case 32: return launch_tiled_g<PERIODIC, 32>(sh, a, b, n, q, grid, st, s, one);
     default: return cudaErrorInvalidValue;
     }
 }
@@ -555,12 +574,13 @@ cudaError_t launch_plain(const float4* pos, const int2* edges, int64_t e, float4
 
 cudaError_t launch_tiled(const TiledShape& shape, const InstDesc* d_insts,
                          const WorkItem* d_items, int num_items, int* d_queue, int grid,
-                         int* d_status, cudaStream_t s)
+                         int* d_status, cudaStream_t s, const InstDesc* one)
 {
     if (!d_queue) return cudaErrorInvalidValue;
-    return shape.periodic
-               ? launch_tiled_p<true>(shape, d_insts, d_items, num_items, d_queue, grid, d_status, s)
-               : launch_tiled_p<false>(shape, d_insts, d_items, num_items, d_queue, grid, d_status, s);
+    return shape.periodic ? launch_tiled_p<true>(shape, d_insts, d_items, num_items, d_queue, grid,
+                                                 d_status, s, one)
+                          : launch_tiled_p<false>(shape, d_insts, d_items, num_items, d_queue,
+                                                  grid, d_status, s, one);
 }
 
 void make_work_items(const uint32_t* row_off, int64_t n, int inst, int max_rows, int staged,
