@@ -249,30 +249,46 @@ __device__ __forceinline__ void lj_pair(float4 a, float4 b0, float4 b1, bool v0,
 
 // The row's result from its G lanes' packed partials: the two halves of each
 // lane joined by TwoSum, then the G lanes by a TwoSum butterfly.
+//
+// The x and y components run as one FP32x2 pair, z as a scalar; every
+// operation rounds as its scalar form (a - b is fma(b, -1, a), one rounding),
+// so the result is bitwise the scalar TwoSum chain's.
+__device__ __forceinline__ float2 sub2(float2 a, float2 b)
+{
+    return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a);
+}
+
+__device__ __forceinline__ void two_sum2(float2 a, float2 b, float2& s, float2& e)
+{
+    s = __fadd2_rn(a, b);
+    const float2 bb = sub2(s, a);
+    e = __fadd2_rn(sub2(a, sub2(s, bb)), sub2(b, bb));
+}
+
 template <int G>
 __device__ __forceinline__ float3 join_partials(float2 ax, float2 ay, float2 az)
 {
-    float hx, hy, hz, cx, cy, cz;
-    two_sum(ax.x, ax.y, hx, cx);
-    two_sum(ay.x, ay.y, hy, cy);
+    float2 h, c;  // (x, y) sums and their carried errors
+    float hz, cz;
+    two_sum2(make_float2(ax.x, ay.x), make_float2(ax.y, ay.y), h, c);
     two_sum(az.x, az.y, hz, cz);
 #pragma unroll
     for (int off = G / 2; off > 0; off >>= 1) {
-        const float ox = __shfl_xor_sync(0xffffffffu, hx, off, G);
-        const float oy = __shfl_xor_sync(0xffffffffu, hy, off, G);
+        const float2 o = make_float2(__shfl_xor_sync(0xffffffffu, h.x, off, G),
+                                     __shfl_xor_sync(0xffffffffu, h.y, off, G));
         const float oz = __shfl_xor_sync(0xffffffffu, hz, off, G);
-        const float ocx = __shfl_xor_sync(0xffffffffu, cx, off, G);
-        const float ocy = __shfl_xor_sync(0xffffffffu, cy, off, G);
+        const float2 oc = make_float2(__shfl_xor_sync(0xffffffffu, c.x, off, G),
+                                      __shfl_xor_sync(0xffffffffu, c.y, off, G));
         const float ocz = __shfl_xor_sync(0xffffffffu, cz, off, G);
-        float e;
-        two_sum(hx, ox, hx, e);
-        cx = __fadd_rn(__fadd_rn(cx, ocx), e);
-        two_sum(hy, oy, hy, e);
-        cy = __fadd_rn(__fadd_rn(cy, ocy), e);
-        two_sum(hz, oz, hz, e);
-        cz = __fadd_rn(__fadd_rn(cz, ocz), e);
+        float2 e;
+        two_sum2(h, o, h, e);
+        c = __fadd2_rn(__fadd2_rn(c, oc), e);
+        float ez;
+        two_sum(hz, oz, hz, ez);
+        cz = __fadd_rn(__fadd_rn(cz, ocz), ez);
     }
-    return make_float3(__fadd_rn(hx, cx), __fadd_rn(hy, cy), __fadd_rn(hz, cz));
+    const float2 r = __fadd2_rn(h, c);
+    return make_float3(r.x, r.y, __fadd_rn(hz, cz));
 }
 
 // One row: G lanes; each lane takes entry pairs (k, k + G) with stride 2G.
