@@ -6,10 +6,14 @@
 //   1. each node gets a cell key (cells at least as wide as the list cutoff);
 //   2. a stable radix sort by key orders nodes by cell; a count + scan gives
 //      each cell's start;
-//   3. one thread per node (in cell order, so a warp shares cells) scans the
+//   3. positions are copied into cell order, so a cell's candidates are
+//      contiguous and each is one load, not an id load and then a dependent
+//      position load;
+//   4. one thread per node (in cell order, so a warp shares cells) scans the
 //      27 surrounding cells for partners j > i with r2 <= cut2, first counting,
 //      then -- after a scan of the counts -- writing them; a warp per row then
-//      sorts each row by j in shared memory.
+//      sorts each row by j (rows in any order are written straight as
+//      pairs when the caller re-sorts them anyway).
 // The pair rule is shared bit for bit with the CPU oracle: d = x_i - x_j in
 // float, wrapped once by +-box when |d| > box/2 (periodic), r2 = ((dx*dx +
 // dy*dy) + dz*dz) with every operation rounded.  Output: pairs (i, j), i < j,
@@ -58,7 +62,7 @@ __device__ __forceinline__ int cell_coord(float x, int axis, const Grid& g)
     return (int)k;
 }
 
-__global__ void cell_keys_kernel(const float4* pos, int64_t n, Grid g, uint32_t* keys,
+__global__ void cell_keys_kernel(const float4* pos, int64_t n, const __grid_constant__ Grid g, uint32_t* keys,
                                  int32_t* vals, uint32_t* cell_count)
 {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
@@ -73,19 +77,30 @@ __global__ void cell_keys_kernel(const float4* pos, int64_t n, Grid g, uint32_t*
     }
 }
 
-// WRITE == false: counts partners; WRITE == true: writes them at row_off[i]
-// (and, with sort_here, sorts the row by j in place: only for rows too long
-// for the shared row sort that otherwise follows).
+// pos_c[q] = pos[sorted[q]]: positions in cell order
+__global__ void cell_order_kernel(const float4* __restrict__ pos, const int32_t* __restrict__ sorted,
+                                  int64_t n, float4* __restrict__ pos_c)
+{
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n;
+         q += (int64_t)gridDim.x * blockDim.x)
+        pos_c[q] = pos[sorted[q]];
+}
+
+// WRITE == false: counts partners; WRITE == true: writes them from row_off[i],
+// as neighbour ids into nbr (with sort_here, sorting the row by j in place:
+// only for rows too long for the row sort that otherwise follows) or, when
+// pairs != nullptr, as the pairs (i, j) themselves.
 template <bool WRITE>
-__global__ void pairs_kernel(const float4* __restrict__ pos, const int32_t* __restrict__ sorted,
-                             const uint32_t* __restrict__ cell_start, int64_t n, Grid g,
+__global__ void pairs_kernel(const float4* __restrict__ pos_c, const int32_t* __restrict__ sorted,
+                             const uint32_t* __restrict__ cell_start, int64_t n,
+                             const __grid_constant__ Grid g,
                              uint32_t* count, const uint32_t* __restrict__ row_off, int32_t* nbr,
-                             int sort_here)
+                             int2* pairs, int sort_here)
 {
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
          t += (int64_t)gridDim.x * blockDim.x) {
         const int32_t i = sorted[t];
-        const float4 a = pos[i];
+        const float4 a = pos_c[t];
         const int cx = cell_coord(a.x, 0, g), cy = cell_coord(a.y, 1, g), cz = cell_coord(a.z, 2, g);
         uint32_t m = 0;
         const uint32_t base = WRITE ? row_off[i] : 0;
@@ -102,11 +117,18 @@ __global__ void pairs_kernel(const float4* __restrict__ pos, const int32_t* __re
                     if (g.periodic) x = (x + g.nc[0]) % g.nc[0];
                     else if (x < 0 || x >= g.nc[0]) continue;
                     const uint32_t c = ((uint32_t)z * g.nc[1] + y) * g.nc[0] + x;
-                    for (uint32_t q = cell_start[c]; q < cell_start[c + 1]; q++) {
+                    const uint32_t q1 = cell_start[c + 1];
+                    for (uint32_t q = cell_start[c]; q < q1; q++) {
                         const int32_t j = sorted[q];
+                        const float4 b = pos_c[q];
                         if (j <= i) continue;
-                        if (list_pair(a, pos[j], g)) {
-                            if (WRITE) nbr[base + m] = j;
+                        if (list_pair(a, b, g)) {
+                            if (WRITE) {
+                                if (pairs)
+                                    pairs[base + m] = make_int2(i, j);
+                                else
+                                    nbr[base + m] = j;
+                            }
                             m++;
                         }
                     }
@@ -115,7 +137,7 @@ __global__ void pairs_kernel(const float4* __restrict__ pos, const int32_t* __re
         }
         if (!WRITE) {
             count[i] = m;
-        } else if (sort_here) {
+        } else if (sort_here && !pairs) {
             // insertion sort of the row in place
             for (uint32_t u = 1; u < m; u++) {
                 const int32_t v = nbr[base + u];
@@ -215,8 +237,12 @@ cudaError_t build_neighbor_list(const float4* pos, int64_t n, float box, float c
     while (bits < 32 && ((int64_t)1 << bits) < ncell) bits++;
     IRR_CUDA_TRY(radix_sort_pairs(keys, sorted, keys_tmp, vals_tmp, n, bits, s));
     IRR_CUDA_TRY(scan_exclusive_u32(cell_start, cell_start, ncell + 1, nullptr, s));
-    pairs_kernel<false><<<grid_of(n), 256, 0, s>>>(pos, sorted, cell_start, n, g, cnt, nullptr,
-                                                   nullptr, 0);
+    float4* pos_c = nullptr;
+    IRR_CUDA_TRY(cudaMallocAsync((void**)&pos_c, sizeof(float4) * n, s));
+    cell_order_kernel<<<grid_of(n), 256, 0, s>>>(pos, sorted, n, pos_c);
+    IRR_CUDA_TRY(cudaGetLastError());
+    pairs_kernel<false><<<grid_of(n), 256, 0, s>>>(pos_c, sorted, cell_start, n, g, cnt, nullptr,
+                                                   nullptr, nullptr, 0);
     IRR_CUDA_TRY(cudaGetLastError());
     IRR_CUDA_TRY(cudaMemsetAsync(cnt + n, 0, sizeof(uint32_t), s));
     uint32_t* d_total = keys_tmp;  // reuse as the total's slot
@@ -224,24 +250,34 @@ cudaError_t build_neighbor_list(const float4* pos, int64_t n, float box, float c
     uint32_t total = 0;
     IRR_CUDA_TRY(cudaMemcpyAsync(&total, d_total, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
     IRR_CUDA_TRY(cudaStreamSynchronize(s));
-    if ((int64_t)total > 0x7fffffffLL) return cudaErrorInvalidValue;
+    if ((int64_t)total > 0x7fffffffLL) {
+        void* tmp[] = {keys, keys_tmp, sorted, vals_tmp, cell_start, cnt, pos_c};
+        for (void* q : tmp) cudaFreeAsync(q, s);
+        return cudaErrorInvalidValue;
+    }
     int2* edges = nullptr;
     if (total > 0) {
-        uint32_t longest = 0;
-        if (sort_rows) IRR_CUDA_TRY(max_row_len(cnt, n, &longest, s));
-        const int sort_here = longest > (uint32_t)kRowSortMax;
-        IRR_CUDA_TRY(cudaMallocAsync((void**)&nbr, sizeof(int32_t) * total, s));
-        pairs_kernel<true><<<grid_of(n), 256, 0, s>>>(pos, sorted, cell_start, n, g, nullptr, cnt,
-                                                      nbr, sort_here);
-        IRR_CUDA_TRY(cudaGetLastError());
-        if (sort_rows && !sort_here) IRR_CUDA_TRY(launch_row_sort(cnt, n, nbr, s));
         if (stream_ordered)
             IRR_CUDA_TRY(cudaMallocAsync((void**)&edges, sizeof(int2) * total, s));
         else
             IRR_CUDA_TRY(cudaMalloc((void**)&edges, sizeof(int2) * total));
-        expand_pairs_kernel<<<grid_of(n), 256, 0, s>>>(cnt, nbr, n, edges);
-        IRR_CUDA_TRY(cudaGetLastError());
-        IRR_CUDA_TRY(cudaFreeAsync(nbr, s));
+        if (sort_rows) {
+            uint32_t longest = 0;
+            IRR_CUDA_TRY(max_row_len(cnt, n, &longest, s));
+            const int sort_here = longest > (uint32_t)kRowSortMax;
+            IRR_CUDA_TRY(cudaMallocAsync((void**)&nbr, sizeof(int32_t) * total, s));
+            pairs_kernel<true><<<grid_of(n), 256, 0, s>>>(pos_c, sorted, cell_start, n, g, nullptr,
+                                                          cnt, nbr, nullptr, sort_here);
+            IRR_CUDA_TRY(cudaGetLastError());
+            if (!sort_here) IRR_CUDA_TRY(launch_row_sort(cnt, n, nbr, s));
+            expand_pairs_kernel<<<grid_of(n), 256, 0, s>>>(cnt, nbr, n, edges);
+            IRR_CUDA_TRY(cudaGetLastError());
+            IRR_CUDA_TRY(cudaFreeAsync(nbr, s));
+        } else {
+            pairs_kernel<true><<<grid_of(n), 256, 0, s>>>(pos_c, sorted, cell_start, n, g, nullptr,
+                                                          cnt, nullptr, edges, 0);
+            IRR_CUDA_TRY(cudaGetLastError());
+        }
     }
     IRR_CUDA_TRY(cudaFreeAsync(keys, s));
     IRR_CUDA_TRY(cudaFreeAsync(keys_tmp, s));
@@ -249,6 +285,7 @@ cudaError_t build_neighbor_list(const float4* pos, int64_t n, float box, float c
     IRR_CUDA_TRY(cudaFreeAsync(vals_tmp, s));
     IRR_CUDA_TRY(cudaFreeAsync(cell_start, s));
     IRR_CUDA_TRY(cudaFreeAsync(cnt, s));
+    IRR_CUDA_TRY(cudaFreeAsync(pos_c, s));
     IRR_CUDA_TRY(cudaStreamSynchronize(s));
     *d_edges = edges;
     *num_edges = total;

@@ -158,10 +158,54 @@ __global__ void __launch_bounds__(kSortThreads) radix_scatter_kernel(
 }
 
 // ------------------------------------------------------------ row sort
-// Each row of a CSR (row_off[n + 1], col) sorted ascending: one warp per row,
-// the row padded to a power of two in a shared-memory buffer and sorted by a
-// bitonic network.  Rows must hold at most kRowSortMax entries.
+// Each row of a CSR (row_off[n + 1], col) sorted ascending, one warp per row,
+// by a bitonic network over the row padded to a power of two.  Rows of up to
+// 256 entries stay in registers (entry k at lane k % 32, slot k / 32):
+// exchanges across lanes are shuffles, within a lane min/max pairs.  Longer
+// rows, up to kRowSortMax entries, go through a shared-memory buffer.
 constexpr int kRowSortWarps = 8;
+
+template <int E>
+__device__ __forceinline__ void sort_row_in_registers(int32_t* col, uint32_t beg, uint32_t len,
+                                                      int lane)
+{
+    int32_t v[E];
+#pragma unroll
+    for (int r = 0; r < E; r++) {
+        const uint32_t k = (uint32_t)(r * 32 + lane);
+        v[r] = k < len ? col[beg + k] : 0x7fffffff;
+    }
+#pragma unroll
+    for (int size = 2; size <= 32 * E; size <<= 1) {
+#pragma unroll
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            if (stride >= 32) {  // partner in the same lane, slot r ^ (stride / 32)
+#pragma unroll
+                for (int r = 0; r < E; r++) {
+                    const int r2 = r ^ (stride / 32);
+                    if (r2 < r) continue;
+                    const bool up = ((r * 32) & size) == 0;  // size >= 64: the lane bits do not reach it
+                    const int32_t lo = min(v[r], v[r2]), hi = max(v[r], v[r2]);
+                    v[r] = up ? lo : hi;
+                    v[r2] = up ? hi : lo;
+                }
+            } else {
+#pragma unroll
+                for (int r = 0; r < E; r++) {
+                    const int32_t o = __shfl_xor_sync(0xffffffffu, v[r], stride);
+                    const bool up = ((r * 32 + lane) & size) == 0;
+                    const bool lower = (lane & stride) == 0;
+                    v[r] = up == lower ? min(v[r], o) : max(v[r], o);
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < E; r++) {
+        const uint32_t k = (uint32_t)(r * 32 + lane);
+        if (k < len) col[beg + k] = v[r];
+    }
+}
 
 __global__ void __launch_bounds__(kRowSortWarps * 32) row_sort_kernel(const uint32_t* __restrict__ row_off,
                                                                      int64_t n, int32_t* col)
@@ -174,6 +218,22 @@ __global__ void __launch_bounds__(kRowSortWarps * 32) row_sort_kernel(const uint
         const uint32_t beg = row_off[r];
         const uint32_t len = row_off[r + 1] - beg;
         if (len < 2) continue;
+        if (len <= 32) {
+            sort_row_in_registers<1>(col, beg, len, lane);
+            continue;
+        }
+        if (len <= 64) {
+            sort_row_in_registers<2>(col, beg, len, lane);
+            continue;
+        }
+        if (len <= 128) {
+            sort_row_in_registers<4>(col, beg, len, lane);
+            continue;
+        }
+        if (len <= 256) {
+            sort_row_in_registers<8>(col, beg, len, lane);
+            continue;
+        }
         uint32_t P = 2;
         while (P < len) P <<= 1;  // len <= kRowSortMax, so P <= kRowSortMax
         for (uint32_t k = lane; k < P; k += 32) b[k] = k < len ? col[beg + k] : 0x7fffffff;
