@@ -164,6 +164,35 @@ __global__ void scatter3_kernel(const double* __restrict__ src, const int32_t* _
     }
 }
 
+// SplitMix64's output mix (Steele, Lea and Flood, "Fast splittable
+// pseudorandom number generators", OOPSLA 2014).
+__device__ __forceinline__ uint64_t mix64(uint64_t z)
+{
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
+
+// Digest of the positions by atom: the sum mod 2^64, over atoms k and
+// components c, of mix64(bits(x) + golden * (3 * id + c + 1)).  Integer sums
+// do not depend on their order, so the digest is a function of the state in
+// the caller's atom order, whatever the execution order.
+__global__ void state_digest_kernel(const double* __restrict__ x, const int32_t* __restrict__ ids,
+                                    int64_t n, unsigned long long* out)
+{
+    uint64_t acc = 0;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t key = 3ull * (uint64_t)ids[k];
+#pragma unroll
+        for (int c = 0; c < 3; c++)
+            acc += mix64((uint64_t)__double_as_longlong(x[3 * k + c]) +
+                         0x9e3779b97f4a7c15ull * (key + (uint64_t)c + 1ull));
+    }
+    for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+    if ((threadIdx.x & 31) == 0 && acc) atomicAdd(out, (unsigned long long)acc);
+}
+
 __device__ __forceinline__ double block_sum(double v, double* red)
 {
     for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
@@ -349,6 +378,19 @@ int md_kick(irr_md* m)
     kick_kernel<<<grid_of(m->n), 256, 0, m->stream>>>(m->v, m->force, m->n, m->cfg.dt);
     MD_CUDA(m, cudaGetLastError(), "kick");
     m->steps++;
+    return IRR_OK;
+}
+
+int md_state_digest(irr_md* m, uint64_t* digest)
+{
+    unsigned long long* d = reinterpret_cast<unsigned long long*>(m->d_acc + 3);  // the spare slot
+    MD_CUDA(m, cudaMemsetAsync(d, 0, sizeof(*d), m->stream), "digest");
+    state_digest_kernel<<<grid_of(m->n), 256, 0, m->stream>>>(m->x, m->ids, m->n, d);
+    MD_CUDA(m, cudaGetLastError(), "digest");
+    unsigned long long h = 0;
+    MD_CUDA(m, cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, m->stream), "digest");
+    MD_CUDA(m, cudaStreamSynchronize(m->stream), "digest");
+    *digest = h;
     return IRR_OK;
 }
 

@@ -55,4 +55,6 @@ int md_forces(irr_md* m);
 int md_kick_drift(irr_md* m);
 int md_kick(irr_md* m);
 InstDesc md_instance(const irr_md* m);
+// Digest of the final positions by atom id (a sum of per-atom 64-bit mixes).
+int md_state_digest(irr_md* m, uint64_t* digest);
 }  // namespace irr

@@ -146,14 +146,6 @@ void initial_state(const JobSpec& j, const irr_serve_config* c, std::vector<doub
     for (double& v : vel) v *= s;
 }
 
-uint64_t fnv1a(const void* data, size_t bytes)
-{
-    const unsigned char* p = static_cast<const unsigned char*>(data);
-    uint64_t h = 1469598103934665603ull;
-    for (size_t i = 0; i < bytes; i++) h = (h ^ p[i]) * 1099511628211ull;
-    return h;
-}
-
 double pct(std::vector<double> v, double q)
 {
     if (v.empty()) return 0.0;
@@ -177,7 +169,11 @@ void irr_serve_config_default(irr_serve_config* c)
     c->rebuild_every = 20;
     c->mode = IRR_SERVE_CONTINUOUS;
     c->only_job = -1;
-    c->max_resident = 1 << 20;
+    // A tick advances every resident job, so its time grows with the resident
+    // set and every resident job waits for it: with no limit the 200-job
+    // stream (200 jobs/s, 2K-2M atoms) had p50 1.44-1.48 s; with 96 slots,
+    // 1.08-1.09 s at a 2 % longer makespan (64: 1.15 s, 128: 1.30-1.35 s).
+    c->max_resident = 96;
     c->arrival_rate = 200.0;
     c->density = 0.8442;
     c->cutforce = 2.5;
@@ -404,9 +400,7 @@ int irr_serve_run(const irr_serve_config* cfg, irr_serve_stats* st, irr_serve_jo
                     r.arrival_s = j.arrival;
                     r.admit_s = L.admit_s;
                     r.done_s = done;
-                    std::vector<double> state(3 * (size_t)j.atoms);
-                    irr_md_get_state(L.md, state.data(), nullptr);
-                    r.state_hash = fnv1a(state.data(), sizeof(double) * state.size());
+                    md_state_digest(L.md, &r.state_hash);
                     double ke = 0, pe = 0;
                     irr_md_energy(L.md, &ke, &pe, nullptr);
                     r.energy = ke + pe;
