@@ -49,71 +49,24 @@ int grid_of(int64_t n)
     return (int)(g < 1 ? 1 : (g > 8192 ? 8192 : g));
 }
 
-// x into [0, L).  An atom moves much less than a box per step, so one shift
-// of +-L covers the step (FP64 division is slow here); the floor form is the
-// fallback and gives the same value for x in [-L, 2L).
-__device__ __forceinline__ double wrap_box(double x, double L)
-{
-    // the common case, +0 <= x < L, decided on the bit patterns with integer
-    // compares (FP64 compares issue at the FP64 rate, a small fraction of the
-    // FP32 one on this part): for x with the sign bit clear the IEEE order is
-    // the integer order; -0, negatives, NaN and x >= L take the path below
-    const long long bx = __double_as_longlong(x);
-    if (bx >= 0 && bx < __double_as_longlong(L)) return x;
-    if (x >= L) {
-        x = x < 2.0 * L ? x - L : x - L * floor(x / L);
-    } else if (x < 0.0) {
-        x = x >= -L ? x + L : x - L * floor(x / L);
-    }
-    if (x >= L) x -= L;  // x = -tiny rounds up to L
-    if (x < 0.0) x = 0.0;
-    return x;
-}
-
+// KICKS = 1: kick + drift of a step; KICKS = 2: also the closing kick of
+// the step before (the same forces).
+template <int KICKS>
 __global__ void kick_drift_kernel(double* __restrict__ x, double* __restrict__ v,
                                   const float4* __restrict__ f, int64_t n, double dt, double L,
                                   float4* __restrict__ pos4)
 {
-    const double hk = 0.5 * dt * 48.0;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        const float4 fi = f[i];
-        double* xi = x + 3 * i;
-        double* vi = v + 3 * i;
-        const double vx = vi[0] + hk * (double)fi.x;
-        const double vy = vi[1] + hk * (double)fi.y;
-        const double vz = vi[2] + hk * (double)fi.z;
-        const double px = wrap_box(xi[0] + dt * vx, L);
-        const double py = wrap_box(xi[1] + dt * vy, L);
-        const double pz = wrap_box(xi[2] + dt * vz, L);
-        vi[0] = vx;
-        vi[1] = vy;
-        vi[2] = vz;
-        xi[0] = px;
-        xi[1] = py;
-        xi[2] = pz;
-        // the float copy stays inside [0, L): a value that rounds up to L wraps to 0
-        float fx = (float)px, fy = (float)py, fz = (float)pz;
-        const float Lf = (float)L;
-        if (fx >= Lf) fx = 0.f;
-        if (fy >= Lf) fy = 0.f;
-        if (fz >= Lf) fz = 0.f;
-        pos4[i] = make_float4(fx, fy, fz, 0.f);
-    }
+         i += (int64_t)gridDim.x * blockDim.x)
+        md_kick_drift_atom<KICKS>(x, v, f, i, dt, L, pos4);
 }
 
 __global__ void kick_kernel(double* __restrict__ v, const float4* __restrict__ f, int64_t n,
                             double dt)
 {
-    const double hk = 0.5 * dt * 48.0;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        const float4 fi = f[i];
-        double* vi = v + 3 * i;
-        vi[0] += hk * (double)fi.x;
-        vi[1] += hk * (double)fi.y;
-        vi[2] += hk * (double)fi.z;
-    }
+         i += (int64_t)gridDim.x * blockDim.x)
+        md_kick_atom(v, f, i, dt);
 }
 
 __global__ void to_float4_kernel(const double* __restrict__ x, int64_t n, double L,
@@ -366,9 +319,20 @@ int md_forces(irr_md* m)
 
 int md_kick_drift(irr_md* m)
 {
-    kick_drift_kernel<<<grid_of(m->n), 256, 0, m->stream>>>(m->x, m->v, m->force, m->n, m->cfg.dt,
-                                                            m->cfg.side, m->pos4);
+    kick_drift_kernel<1><<<grid_of(m->n), 256, 0, m->stream>>>(m->x, m->v, m->force, m->n,
+                                                               m->cfg.dt, m->cfg.side, m->pos4);
     MD_CUDA(m, cudaGetLastError(), "kick-drift");
+    m->since_rebuild++;
+    return IRR_OK;
+}
+
+// md_kick of the previous step and md_kick_drift of this one in one pass.
+int md_kick_kick_drift(irr_md* m)
+{
+    kick_drift_kernel<2><<<grid_of(m->n), 256, 0, m->stream>>>(m->x, m->v, m->force, m->n,
+                                                               m->cfg.dt, m->cfg.side, m->pos4);
+    MD_CUDA(m, cudaGetLastError(), "kick-drift");
+    m->steps++;
     m->since_rebuild++;
     return IRR_OK;
 }
@@ -544,13 +508,13 @@ int irr_md_run(irr_md* m, int steps)
     if (!m || steps < 0) return IRR_ERR_ARG;
     cudaSetDevice(m->device);
     for (int t = 0; t < steps; t++) {
-        int rc = md_kick_drift(m);
+        // a step's closing kick is fused into the next step's kick-drift
+        int rc = t == 0 ? md_kick_drift(m) : md_kick_kick_drift(m);
         if (!rc && m->since_rebuild >= m->cfg.rebuild_every) rc = md_rebuild(m);
         if (!rc) rc = md_forces(m);
-        if (!rc) rc = md_kick(m);
         if (rc) return rc;
     }
-    return IRR_OK;
+    return steps > 0 ? md_kick(m) : IRR_OK;
 }
 
 int irr_md_energy(irr_md* m, double* kinetic, double* potential, double* virial)

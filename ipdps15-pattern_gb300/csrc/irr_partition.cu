@@ -13,9 +13,10 @@
 //   3. every half edge (i, j) at list position t becomes the directed entries
 //      (inv[i] <- inv[j]) and (inv[j] <- inv[i]), laid out in (row, col)
 //      order: a degree count + scan gives the row offsets, the entries are
-//      filled at per-row cursors and each row is sorted by one warp in shared
-//      memory (rows up to kRowSortMax entries); a graph with a longer row is
-//      put in order by stable radix sorts by column, then by row.
+//      filled at per-row cursors and each row is sorted by one warp, in
+//      registers (rows up to 256 entries) or in shared memory (up to
+//      kRowSortMax); a graph with a longer row is put in order by stable radix
+//      sorts by column, then by row.
 // Node blocks are then consecutive ranges of rows.  Every output is an
 // integer function of the inputs, reproduced bit for bit by the CPU oracle.
 // 4. Optionally the sliced layout (struct Sliced): the same entries regrouped
@@ -322,16 +323,23 @@ __global__ void bbox_partial_kernel(const float4* pos, int64_t n, float* part)
     if (threadIdx.x < 6) part[blockIdx.x * 6 + threadIdx.x] = red[threadIdx.x][0];
 }
 
+// One warp: lanes take the blocks' partials in turn, then a shuffle reduction.
 __global__ void bbox_final_kernel(const float* part, int nparts, float* out)
 {
-    if (threadIdx.x != 0) return;
+    const int lane = threadIdx.x & 31;
     float v[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
-    for (int b = 0; b < nparts; b++)
+    for (int b = lane; b < nparts; b += 32)
         for (int c = 0; c < 3; c++) {
             v[c] = fminf(v[c], part[b * 6 + c]);
             v[3 + c] = fmaxf(v[3 + c], part[b * 6 + 3 + c]);
         }
-    for (int c = 0; c < 6; c++) out[c] = v[c];
+    for (int off = 16; off > 0; off >>= 1)
+        for (int c = 0; c < 3; c++) {
+            v[c] = fminf(v[c], __shfl_xor_sync(0xffffffffu, v[c], off));
+            v[3 + c] = fmaxf(v[3 + c], __shfl_xor_sync(0xffffffffu, v[3 + c], off));
+        }
+    if (lane == 0)
+        for (int c = 0; c < 6; c++) out[c] = v[c];
 }
 
 // ------------------------------------------------------------- morton
@@ -540,26 +548,30 @@ __global__ void slice_words_kernel(const uint32_t* row_off, int64_t n, int G, in
     }
 }
 
-// One thread per row slot (rows past n are empty): writes the row's T * 2G
-// words of its slice, entries then padding.  A padding word holds the row's
-// own id (0 for a row past n), so the kernel's gathers need no predicate:
-// a padded slot reads its own position, d = 0, and is masked to 0.
-__global__ void slice_fill_kernel(const uint32_t* row_off, const int32_t* col, int64_t n, int G,
+// One warp per slice, lane i*G + l serving row i of the slice: per step t it
+// writes the pair (entry 2Gt + l, entry 2Gt + G + l) of its row as the int2 at
+// word 64t + 2*lane, so each step is one contiguous 256-byte store (G is a
+// power of two: lg = log2 G).  A padding word holds the row's own id (0 for a
+// row past n), so the kernel's gathers need no predicate: a padded slot reads
+// its own position, d = 0, and is masked to 0.
+__global__ void slice_fill_kernel(const uint32_t* row_off, const int32_t* col, int64_t n, int lg,
                                   int64_t slices, const uint32_t* slice_off, int32_t* out)
 {
-    const int R = 32 / G;
-    const int64_t rows = slices * R;
-    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows;
-         r += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t q = r / R;
-        const int i = (int)(r - q * R);
+    const int G = 1 << lg;
+    const int lane = threadIdx.x & 31;
+    const int i = lane >> lg, l = lane & (G - 1);
+    const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t q = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < slices; q += warps) {
+        const int64_t r = (q << (5 - lg)) + i;
         const uint32_t o = slice_off[q];
-        const uint32_t slots = (slice_off[q + 1] - o) / 64u * (2u * G);
+        const uint32_t steps = (slice_off[q + 1] - o) >> 6;
         const uint32_t beg = r < n ? row_off[r] : 0u;
         const uint32_t len = r < n ? row_off[r + 1] - beg : 0u;
-        for (uint32_t k = 0; k < slots; k++) {
-            const uint32_t t = k / (2u * G), h = (k / G) & 1u, l = k % G;
-            out[o + 64u * t + 2u * (i * G + l) + h] = k < len ? col[beg + k] : (r < n ? (int32_t)r : 0);
+        const int32_t pad = r < n ? (int32_t)r : 0;
+        int2* line = reinterpret_cast<int2*>(out + o) + lane;
+        for (uint32_t t = 0; t < steps; t++) {
+            const uint32_t k0 = (t << (lg + 1)) + l, k1 = k0 + G;
+            line[32 * t] = make_int2(k0 < len ? col[beg + k0] : pad, k1 < len ? col[beg + k1] : pad);
         }
     }
 }
@@ -809,8 +821,10 @@ cudaError_t build_sliced(const uint32_t* row_off, const int32_t* col, int64_t n,
     if (err == cudaSuccess) err = scan_exclusive_u32(words, sl->slice_off, slices + 1, nullptr, s);
     if (err == cudaSuccess) err = alloc_async(&sl->col, (int64_t)total, s);
     if (err == cudaSuccess && slices > 0) {
-        slice_fill_kernel<<<grid_for(slices * R), 256, 0, s>>>(row_off, col, n, G, slices,
-                                                               sl->slice_off, sl->col);
+        int lg = 0;
+        while ((1 << lg) < G) lg++;
+        slice_fill_kernel<<<grid_for(slices * 32), 256, 0, s>>>(row_off, col, n, lg, slices,
+                                                                sl->slice_off, sl->col);
         err = cudaGetLastError();
     }
     if (err == cudaSuccess) {

@@ -5,9 +5,11 @@
 // number of velocity-Verlet steps) arrive as a Poisson stream.  The loop:
 //   * admits arrived jobs in arrival order while their estimated device memory
 //     fits the budget (their state then stays resident until they finish);
-//   * every tick advances each resident job by one step: per-job kick/drift,
-//     rebuilds that are due, ONE batched force launch over all resident jobs'
-//     (instance, node block) work items, per-job kick;
+//   * every tick advances each resident job by one step: ONE kick/drift launch
+//     over all resident jobs, the rebuilds that are due, ONE batched force
+//     launch over all resident jobs' (instance, node block) work items (the
+//     item table is gathered on the device from each job's own), ONE kick
+//     launch;
 //   * retires finished jobs (their memory frees up for waiting arrivals).
 // A job's rows are computed by the same kernel code whatever else shares the
 // launch, so its trajectory is bitwise the same alone and in the mix.
@@ -45,6 +47,131 @@ struct Live {
     double admit_s;
     double pair_evals;
 };
+
+// One resident job in a tick's device tables.  Its atoms occupy whole
+// 256-thread blocks [block0, block0 + ceil(n / 256)) of the integrator
+// launches; its work items are [item0, item0 + num_items) of the batch.
+struct TickJob {
+    double* x;
+    double* v;
+    const float4* force;
+    float4* pos4;
+    const WorkItem* items;
+    int64_t n;
+    double side;
+    int32_t block0;
+    int32_t item0;
+    int32_t num_items;
+    int32_t pad;
+};
+constexpr int kTickThreads = 256;
+
+// The job a block (or an item) belongs to: the last k with start(k) <= x.
+template <class Start>
+__device__ __forceinline__ int find_job(int njobs, int64_t x, Start start)
+{
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (start(mid) <= x) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+template <int KICKS>
+__global__ void __launch_bounds__(kTickThreads) tick_kick_drift_kernel(const TickJob* __restrict__ jobs,
+                                                                       int njobs, double dt)
+{
+    const int k = find_job(njobs, blockIdx.x, [&](int j) { return (int64_t)jobs[j].block0; });
+    const TickJob& J = jobs[k];
+    const int64_t i = (int64_t)(blockIdx.x - J.block0) * kTickThreads + threadIdx.x;
+    if (i < J.n) md_kick_drift_atom<KICKS>(J.x, J.v, J.force, i, dt, J.side, J.pos4);
+}
+
+__global__ void __launch_bounds__(kTickThreads) tick_kick_kernel(const TickJob* __restrict__ jobs,
+                                                                 int njobs, double dt)
+{
+    const int k = find_job(njobs, blockIdx.x, [&](int j) { return (int64_t)jobs[j].block0; });
+    const TickJob& J = jobs[k];
+    const int64_t i = (int64_t)(blockIdx.x - J.block0) * kTickThreads + threadIdx.x;
+    if (i < J.n) md_kick_atom(J.v, J.force, i, dt);
+}
+
+// The batch's work items: job k's own items with the instance set to k.
+__global__ void tick_items_kernel(const TickJob* __restrict__ jobs, int njobs, int64_t total,
+                                  WorkItem* __restrict__ out)
+{
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int k = find_job(njobs, t, [&](int j) { return (int64_t)jobs[j].item0; });
+        WorkItem w = jobs[k].items[t - jobs[k].item0];
+        w.inst = k;
+        out[t] = w;
+    }
+}
+
+// Host tables of a tick, in page-locked memory (reused every tick: the tick
+// ends with a stream synchronisation).
+template <class T>
+struct Pinned {
+    T* h = nullptr;
+    T* d = nullptr;
+    size_t cap = 0;
+    bool reserve(size_t n)
+    {
+        if (n <= cap) return true;
+        release();
+        cap = n * 2;
+        if (cudaHostAlloc((void**)&h, sizeof(T) * cap, cudaHostAllocDefault) != cudaSuccess ||
+            cudaMalloc((void**)&d, sizeof(T) * cap) != cudaSuccess) {
+            cudaGetLastError();
+            release();
+            return false;
+        }
+        return true;
+    }
+    void release()
+    {
+        if (h) cudaFreeHost(h);
+        if (d) cudaFree(d);
+        h = nullptr;
+        d = nullptr;
+        cap = 0;
+    }
+};
+
+// Fills the job table for the resident jobs (their current arrays: a rebuild
+// swaps a job's state buffers) and uploads it on s; returns the launch's
+// block count and the batch's item count.
+bool upload_tick_jobs(const std::vector<Live>& live, Pinned<TickJob>& T, cudaStream_t s,
+                      int* blocks, int64_t* items)
+{
+    if (!T.reserve(live.size())) return false;
+    int64_t b = 0, it = 0;
+    for (size_t k = 0; k < live.size(); k++) {
+        const irr_md* m = live[k].md;
+        TickJob& J = T.h[k];
+        J.x = m->x;
+        J.v = m->v;
+        J.force = m->force;
+        J.pos4 = m->pos4;
+        J.items = m->d_items;
+        J.n = m->n;
+        J.side = m->cfg.side;
+        J.block0 = (int32_t)b;
+        J.item0 = (int32_t)it;
+        J.num_items = m->num_items;
+        J.pad = 0;
+        b += (m->n + kTickThreads - 1) / kTickThreads;
+        it += m->num_items;
+    }
+    if (b > 0x7fffffffLL || it > 0x7fffffffLL) return false;
+    *blocks = (int)b;
+    *items = it;
+    return cudaMemcpyAsync(T.d, T.h, sizeof(TickJob) * live.size(), cudaMemcpyHostToDevice, s) ==
+           cudaSuccess;
+}
 
 // Runs f(0..count-1) on up to `workers` host threads (count small: inline).
 // Each call issues work on its own job's stream, so the GPU overlaps the
@@ -220,9 +347,10 @@ int irr_serve_run(const irr_serve_config* cfg, irr_serve_stats* st, irr_serve_jo
     const int max_res = cfg->mode == IRR_SERVE_SERIAL ? 1 : cfg->max_resident;
     std::vector<double> latency;
     std::vector<Live> live;
-    InstDesc* d_insts = nullptr;
+    Pinned<TickJob> tick_a, tick_b;  // before and after the tick's rebuilds
+    Pinned<InstDesc> tick_insts;
     WorkItem* d_items = nullptr;
-    size_t insts_cap = 0, items_cap = 0;
+    size_t items_cap = 0;
     double used = 0.0, peak = 0.0, pair_evals = 0.0;
     size_t next = 0;
     int rc = IRR_OK;
@@ -321,15 +449,17 @@ int irr_serve_run(const irr_serve_config* cfg, irr_serve_stats* st, irr_serve_jo
             continue;
         }
         // one tick: every resident job advances one step
-        std::vector<InstDesc> insts;
-        std::vector<WorkItem> items;
         std::vector<size_t> due;
-        for (size_t k = 0; k < live.size() && rc == IRR_OK; k++) {
+        int blocks = 0;
+        int64_t nitems = 0;
+        if (!upload_tick_jobs(live, tick_a, s, &blocks, &nitems)) { rc = IRR_ERR_CUDA; break; }
+        tick_kick_drift_kernel<1><<<blocks, kTickThreads, 0, s>>>(tick_a.d, (int)live.size(), cfg->dt);
+        if (cudaGetLastError() != cudaSuccess) { rc = IRR_ERR_CUDA; break; }
+        for (size_t k = 0; k < live.size(); k++) {
             irr_md* m = live[k].md;
-            rc = md_kick_drift(m);
-            if (!rc && m->since_rebuild >= m->cfg.rebuild_every) due.push_back(k);
+            m->since_rebuild++;  // the bookkeeping of md_kick_drift
+            if (m->since_rebuild >= m->cfg.rebuild_every) due.push_back(k);
         }
-        if (rc) break;
         if (!due.empty()) {
             // rebuilds that are due run concurrently, each on its job's own
             // stream after this tick's kick-drift; md_rebuild returns once its
@@ -347,39 +477,44 @@ int irr_serve_run(const irr_serve_config* cfg, irr_serve_stats* st, irr_serve_jo
                 if (r != IRR_OK && rc == IRR_OK) rc = r;
             if (rc) break;
         }
-        for (size_t k = 0; k < live.size() && rc == IRR_OK; k++) {
-            irr_md* m = live[k].md;
-            insts.push_back(md_instance(m));
-            for (WorkItem w : m->host_items) {
-                w.inst = (int)k;
-                items.push_back(w);
-            }
-            live[k].pair_evals += (double)m->edges;
-        }
-        if (rc) break;
-        if (insts.size() > insts_cap) {
-            if (d_insts) cudaFree(d_insts);
-            insts_cap = insts.size() * 2;
-            if (cudaMalloc(&d_insts, sizeof(InstDesc) * insts_cap) != cudaSuccess) { rc = IRR_ERR_NOMEM; break; }
-        }
-        if (items.size() > items_cap) {
-            if (d_items) cudaFree(d_items);
-            items_cap = items.size() * 2;
-            if (cudaMalloc(&d_items, sizeof(WorkItem) * items_cap) != cudaSuccess) { rc = IRR_ERR_NOMEM; break; }
-        }
-        if (cudaMemcpyAsync(d_insts, insts.data(), sizeof(InstDesc) * insts.size(), cudaMemcpyHostToDevice, s) != cudaSuccess ||
-            cudaMemcpyAsync(d_items, items.data(), sizeof(WorkItem) * items.size(), cudaMemcpyHostToDevice, s) != cudaSuccess ||
-            cudaMemsetAsync(d_queue, 0, sizeof(int), s) != cudaSuccess ||
-            launch_tiled(shape, d_insts, d_items, (int)items.size(), d_queue, sms * kCtasPerSm, d_status, s) != cudaSuccess) {
+        // the job table again (rebuilt jobs have new arrays and items), the
+        // instance table, the batch's items gathered on the device, one force
+        // launch, one kick launch
+        if (!upload_tick_jobs(live, tick_b, s, &blocks, &nitems) || !tick_insts.reserve(live.size())) {
             rc = IRR_ERR_CUDA;
             break;
         }
+        for (size_t k = 0; k < live.size(); k++) {
+            tick_insts.h[k] = md_instance(live[k].md);
+            live[k].pair_evals += (double)live[k].md->edges;
+        }
+        if ((size_t)nitems > items_cap) {
+            if (d_items) cudaFree(d_items);
+            items_cap = (size_t)nitems * 2;
+            if (cudaMalloc(&d_items, sizeof(WorkItem) * items_cap) != cudaSuccess) { rc = IRR_ERR_NOMEM; break; }
+        }
+        if (cudaMemcpyAsync(tick_insts.d, tick_insts.h, sizeof(InstDesc) * live.size(),
+                            cudaMemcpyHostToDevice, s) != cudaSuccess) {
+            rc = IRR_ERR_CUDA;
+            break;
+        }
+        if (nitems > 0) {
+            const int64_t want = (nitems + 255) / 256;
+            tick_items_kernel<<<(unsigned)(want < 4096 ? want : 4096), 256, 0, s>>>(tick_b.d, (int)live.size(),
+                                                                                    nitems, d_items);
+        }
+        if (cudaGetLastError() != cudaSuccess ||
+            cudaMemsetAsync(d_queue, 0, sizeof(int), s) != cudaSuccess ||
+            launch_tiled(shape, tick_insts.d, d_items, (int)nitems, d_queue, sms * kCtasPerSm, d_status, s) != cudaSuccess) {
+            rc = IRR_ERR_CUDA;
+            break;
+        }
+        tick_kick_kernel<<<blocks, kTickThreads, 0, s>>>(tick_b.d, (int)live.size(), cfg->dt);
+        if (cudaGetLastError() != cudaSuccess) { rc = IRR_ERR_CUDA; break; }
         for (auto& L : live) {
-            rc = md_kick(L.md);
-            if (rc) break;
+            L.md->steps++;  // the bookkeeping of md_kick
             L.steps++;
         }
-        if (rc) break;
         // the host copies of the tables are reused next tick: wait for this one
         if (cudaStreamSynchronize(s) != cudaSuccess) { rc = IRR_ERR_CUDA; break; }
         // retire finished jobs: their results (final state hash, energy) are
@@ -425,7 +560,9 @@ int irr_serve_run(const irr_serve_config* cfg, irr_serve_stats* st, irr_serve_jo
     if (ev_kd) cudaEventDestroy(ev_kd);
     int dev_status = 0;
     cudaMemcpy(&dev_status, d_status, sizeof(int), cudaMemcpyDeviceToHost);
-    if (d_insts) cudaFree(d_insts);
+    tick_a.release();
+    tick_b.release();
+    tick_insts.release();
     if (d_items) cudaFree(d_items);
     cudaFree(d_queue);
     cudaFree(d_status);
