@@ -165,8 +165,9 @@ cudaError_t build_partition(const float4* pos_user, int64_t n, const int2* edges
                             int reorder, PartitionOut* out, cudaStream_t s, int curve = 0);
 // Half neighbour list (irr_neighbor.cu); *d_edges is cudaMalloc'd, or, with
 // stream_ordered, cudaMallocAsync'd on s (free it with cudaFreeAsync).
-// sort_rows == false leaves each row's partners in cell-scan order (for a
-// caller that re-sorts them anyway, like the partitioner).
+// sort_rows == false returns the same pairs (i < j) in no particular order,
+// for a caller that re-sorts them anyway, like the partitioner (found by a
+// half-stencil search when the box has at least 3 cells per axis).
 cudaError_t build_neighbor_list(const float4* pos, int64_t n, float box, float cut2,
                                 int2** d_edges, int64_t* num_edges, cudaStream_t s,
                                 bool stream_ordered = false, bool sort_rows = true);

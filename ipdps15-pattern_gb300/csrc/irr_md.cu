@@ -5,7 +5,7 @@
 // and call IrregularStart once per step.  Here the whole loop stays on the GPU:
 //   kick + drift   v += dt/2 * F/m, x += dt * v, x wrapped into [0, L)   (FP64)
 //   rebuild        every `rebuild_every` steps: GPU neighbour list at
-//                  cutforce + skin, GPU partition (Morton order), state
+//                  cutforce + skin, GPU partition (Hilbert order), state
 //                  permuted into the new order
 //   force          the owner-computes reduction (FP32 per edge, compensated)
 //   kick           v += dt/2 * F/m                                       (FP64)
@@ -272,15 +272,21 @@ int md_rebuild(irr_md* m)
     std::swap(m->ids, m->ids_tmp);
     to_float4_kernel<<<g, 256, 0, s>>>(m->x, m->n, m->cfg.side, m->pos4);
     MD_CUDA(m, cudaGetLastError(), "permute state");
-    std::vector<uint32_t> ro((size_t)m->n + 1);
-    MD_CUDA(m, cudaMemcpyAsync(ro.data(), m->part.row_off, sizeof(uint32_t) * (m->n + 1),
-                               cudaMemcpyDeviceToHost, s), "row offsets");
-    MD_CUDA(m, cudaStreamSynchronize(s), "row offsets");
+    // the sliced layout's work items are cut from its slice offsets (which
+    // build_sliced brings to the host); only the CSR fallback needs the row
+    // offsets on the host
     if (build_sliced(m->part.row_off, m->part.col, m->n, m->shape.lanes_per_row, &m->sl, s) != cudaSuccess) {
         cudaGetLastError();
         free_sliced(&m->sl, s);  // CSR
     } else if (!sliced_pays(m->sl, 2 * e)) {
         free_sliced(&m->sl, s);
+    }
+    std::vector<uint32_t> ro;
+    if (!m->sl.lanes) {
+        ro.resize((size_t)m->n + 1);
+        MD_CUDA(m, cudaMemcpyAsync(ro.data(), m->part.row_off, sizeof(uint32_t) * (m->n + 1),
+                                   cudaMemcpyDeviceToHost, s), "row offsets");
+        MD_CUDA(m, cudaStreamSynchronize(s), "row offsets");
     }
     std::vector<WorkItem> items;
     make_instance_items(ro.data(), m->sl, m->n, 0, m->shape, items);
@@ -305,7 +311,6 @@ int md_rebuild(irr_md* m)
     m->edges = e;
     m->rebuilds++;
     m->since_rebuild = 0;
-    m->host_items = std::move(items);
     return IRR_OK;
 }
 

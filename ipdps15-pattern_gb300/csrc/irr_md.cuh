@@ -117,7 +117,6 @@ struct irr_md {
     int64_t steps = 0;
     int64_t rebuilds = 0;
     int64_t since_rebuild = 0;
-    std::vector<WorkItem> host_items;  // this system's node blocks (for batched launches)
 };
 
 

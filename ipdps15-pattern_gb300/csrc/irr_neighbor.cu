@@ -12,8 +12,9 @@
 //   4. one thread per node (in cell order, so a warp shares cells) scans the
 //      27 surrounding cells for partners j > i with r2 <= cut2, first counting,
 //      then -- after a scan of the counts -- writing them; a warp per row then
-//      sorts each row by j (rows in any order are written straight as
-//      pairs when the caller re-sorts them anyway).
+//      sorts each row by j.  A caller that re-sorts the pairs anyway gets
+//      them in no particular order, from a half stencil (pairs_half_kernel:
+//      each pair found once, from one end), written straight as pairs.
 // The pair rule is shared bit for bit with the CPU oracle: d = x_i - x_j in
 // float, wrapped once by +-box when |d| > box/2 (periodic), r2 = ((dx*dx +
 // dy*dy) + dz*dz) with every operation rounded.  Output: pairs (i, j), i < j,
@@ -152,6 +153,53 @@ __global__ void pairs_kernel(const float4* __restrict__ pos_c, const int32_t* __
     }
 }
 
+// The same pairs from a half stencil, for callers that take the pairs in any
+// order (with at least 3 cells per axis, so no cell is its own neighbour):
+// node t (in cell order) pairs with the later nodes of its own cell and with
+// the nodes of the 13 neighbour cells whose offset (dz, dy, dx) comes after
+// (0, 0, 0) in lexicographic order.  Each pair is found once and written as
+// (min id, max id).
+template <bool WRITE>
+__global__ void pairs_half_kernel(const float4* __restrict__ pos_c, const int32_t* __restrict__ sorted,
+                                  const uint32_t* __restrict__ cell_start, int64_t n,
+                                  const __grid_constant__ Grid g, uint32_t* count,
+                                  const uint32_t* __restrict__ row_off, int2* pairs)
+{
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t i = sorted[t];
+        const float4 a = pos_c[t];
+        const int cx = cell_coord(a.x, 0, g), cy = cell_coord(a.y, 1, g), cz = cell_coord(a.z, 2, g);
+        uint32_t m = 0;
+        const uint32_t base = WRITE ? row_off[i] : 0;
+        for (int o = 0; o < 14; o++) {
+            // o = 0: the own cell (later nodes only); o = 1..13: forward offsets
+            const int k = o == 0 ? 13 : 13 + o;  // (dz+1)*9 + (dy+1)*3 + (dx+1)
+            int z = cz + k / 9 - 1, y = cy + (k / 3) % 3 - 1, x = cx + k % 3 - 1;
+            if (g.periodic) {
+                z = z < 0 ? z + g.nc[2] : (z >= g.nc[2] ? z - g.nc[2] : z);
+                y = y < 0 ? y + g.nc[1] : (y >= g.nc[1] ? y - g.nc[1] : y);
+                x = x < 0 ? x + g.nc[0] : (x >= g.nc[0] ? x - g.nc[0] : x);
+            } else if (z < 0 || z >= g.nc[2] || y < 0 || y >= g.nc[1] || x < 0 || x >= g.nc[0]) {
+                continue;
+            }
+            const uint32_t c = ((uint32_t)z * g.nc[1] + y) * g.nc[0] + x;
+            const uint32_t q1 = cell_start[c + 1];
+            for (uint32_t q = o == 0 ? (uint32_t)t + 1 : cell_start[c]; q < q1; q++) {
+                const float4 b = pos_c[q];
+                if (list_pair(a, b, g)) {
+                    if (WRITE) {
+                        const int32_t j = sorted[q];
+                        pairs[base + m] = i < j ? make_int2(i, j) : make_int2(j, i);
+                    }
+                    m++;
+                }
+            }
+        }
+        if (!WRITE) count[i] = m;
+    }
+}
+
 __global__ void expand_pairs_kernel(const uint32_t* row_off, const int32_t* nbr, int64_t n,
                                     int2* edges)
 {
@@ -241,8 +289,14 @@ cudaError_t build_neighbor_list(const float4* pos, int64_t n, float box, float c
     IRR_CUDA_TRY(cudaMallocAsync((void**)&pos_c, sizeof(float4) * n, s));
     cell_order_kernel<<<grid_of(n), 256, 0, s>>>(pos, sorted, n, pos_c);
     IRR_CUDA_TRY(cudaGetLastError());
-    pairs_kernel<false><<<grid_of(n), 256, 0, s>>>(pos_c, sorted, cell_start, n, g, cnt, nullptr,
-                                                   nullptr, nullptr, 0);
+    // rows in any order are asked for: the half stencil, where the box allows it
+    const bool half = !sort_rows && g.nc[0] >= 3 && g.nc[1] >= 3 && g.nc[2] >= 3;
+    if (half)
+        pairs_half_kernel<false><<<grid_of(n), 256, 0, s>>>(pos_c, sorted, cell_start, n, g, cnt,
+                                                            nullptr, nullptr);
+    else
+        pairs_kernel<false><<<grid_of(n), 256, 0, s>>>(pos_c, sorted, cell_start, n, g, cnt, nullptr,
+                                                       nullptr, nullptr, 0);
     IRR_CUDA_TRY(cudaGetLastError());
     IRR_CUDA_TRY(cudaMemsetAsync(cnt + n, 0, sizeof(uint32_t), s));
     uint32_t* d_total = keys_tmp;  // reuse as the total's slot
@@ -273,6 +327,10 @@ cudaError_t build_neighbor_list(const float4* pos, int64_t n, float box, float c
             expand_pairs_kernel<<<grid_of(n), 256, 0, s>>>(cnt, nbr, n, edges);
             IRR_CUDA_TRY(cudaGetLastError());
             IRR_CUDA_TRY(cudaFreeAsync(nbr, s));
+        } else if (half) {
+            pairs_half_kernel<true><<<grid_of(n), 256, 0, s>>>(pos_c, sorted, cell_start, n, g,
+                                                               nullptr, cnt, edges);
+            IRR_CUDA_TRY(cudaGetLastError());
         } else {
             pairs_kernel<true><<<grid_of(n), 256, 0, s>>>(pos_c, sorted, cell_start, n, g, nullptr,
                                                           cnt, nullptr, edges, 0);
