@@ -432,13 +432,33 @@ __global__ void entries_kernel(const int2* edges, int64_t e, const int32_t* inv,
 }
 
 // Degrees of the directed entries (both endpoints of every half edge).
+// Adds 1 to ctr[key] for every lane of the warp with valid == true, one
+// atomic per distinct key (lanes of a warp often share a row: the edges of a
+// sorted list, or of one node's neighbour search); returns the lane's own
+// slot, the counter's value before it plus its rank among the key's lanes.
+// All 32 lanes must call it together.
+__device__ __forceinline__ uint32_t add_grouped(uint32_t* ctr, int32_t key, bool valid)
+{
+    const uint32_t peers = __match_any_sync(0xffffffffu, valid ? key : -1);
+    const uint32_t rank = (uint32_t)__popc(peers & lanemask_lt());
+    uint32_t base = 0;
+    if (valid && rank == 0) base = atomicAdd(ctr + key, (uint32_t)__popc(peers));
+    base = __shfl_sync(0xffffffffu, base, __ffs(peers) - 1);
+    return base + rank;
+}
+
+// Whole warps walk the edges (t = warp start + lane), so every lane takes
+// part in the grouped adds.
 __global__ void degree_kernel(const int2* edges, int64_t e, const int32_t* inv, uint32_t* deg)
 {
-    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < e;
-         t += (int64_t)gridDim.x * blockDim.x) {
-        const int2 ed = edges[t];
-        atomicAdd(deg + inv[ed.x], 1u);
-        atomicAdd(deg + inv[ed.y], 1u);
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t t0 = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); t0 < e; t0 += stride) {
+        const int64_t t = t0 + (threadIdx.x & 31);
+        const bool v = t < e;
+        const int2 ed = v ? edges[t] : make_int2(0, 0);
+        const int32_t a = v ? inv[ed.x] : 0, b = v ? inv[ed.y] : 0;
+        add_grouped(deg, a, v);
+        add_grouped(deg, b, v);
     }
 }
 
@@ -447,12 +467,18 @@ __global__ void degree_kernel(const int2* edges, int64_t e, const int32_t* inv, 
 __global__ void fill_rows_kernel(const int2* edges, int64_t e, const int32_t* inv,
                                  uint32_t* cursor, int32_t* col)
 {
-    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < e;
-         t += (int64_t)gridDim.x * blockDim.x) {
-        const int2 ed = edges[t];
-        const int32_t a = inv[ed.x], b = inv[ed.y];
-        col[atomicAdd(cursor + a, 1u)] = b;
-        col[atomicAdd(cursor + b, 1u)] = a;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t t0 = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); t0 < e; t0 += stride) {
+        const int64_t t = t0 + (threadIdx.x & 31);
+        const bool v = t < e;
+        const int2 ed = v ? edges[t] : make_int2(0, 0);
+        const int32_t a = v ? inv[ed.x] : 0, b = v ? inv[ed.y] : 0;
+        const uint32_t sa = add_grouped(cursor, a, v);
+        const uint32_t sb = add_grouped(cursor, b, v);
+        if (v) {
+            col[sa] = b;
+            col[sb] = a;
+        }
     }
 }
 
