@@ -14,10 +14,13 @@ def system(cells=6, rho=0.8442, temp=1.44, seed=20260003, jitter=0.03):
     return pos, vel, side
 
 
-def test_initial_forces_match_fp64(built_lib, oracle_lib):
+@pytest.mark.parametrize("cells", [4, 6, 12])
+def test_initial_forces_match_fp64(built_lib, oracle_lib, cells):
+    """cells 4: two list cells per axis (the full-stencil search); 6 and 12:
+    3 and 7 cells per axis (the half stencil, each pair found once)."""
     import irregular_gb300 as irr
     O = oracle_lib
-    pos, vel, side = system()
+    pos, vel, side = system(cells=cells)
     md = irr.MD(pos, vel, side)
     f = md.forces()
     # FP64 forces of the positions the GPU computes with (the float copy of

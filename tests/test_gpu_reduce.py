@@ -89,6 +89,40 @@ def test_partition_bit_exact(built_lib, oracle_lib, name, reorder, curve):
     assert np.array_equal(col, ocol)
 
 
+def test_partition_rows_of_every_sort_path_bit_exact(built_lib, oracle_lib):
+    """Rows of 1..~1000 entries (with duplicate edges) take every row-sort path
+    -- 1, 2, 4 and 8 entries per lane in registers, and shared memory above
+    256 -- and still equal the oracle's partition bit for bit."""
+    import irregular_gb300 as irr
+    O = oracle_lib
+    rng = np.random.default_rng(77)
+    n = 3000
+    pos32, L = random_box(n, 0.8442, 78)
+    edges = [rng.integers(0, n, size=(6000, 2))]
+    for k, d in enumerate([1, 2, 31, 33, 64, 65, 127, 129, 200, 256, 257, 400, 700, 900]):
+        hub = 17 * k + 5
+        others = rng.choice(np.delete(np.arange(n), hub), size=d, replace=False)
+        edges.append(np.stack([np.full(d, hub), others], axis=1))
+    e = np.concatenate(edges).astype(np.int32)
+    e = e[e[:, 0] != e[:, 1]]
+    e = np.concatenate([e, e[rng.choice(e.shape[0], 500)]])  # duplicates
+    e = e[rng.permutation(e.shape[0])]
+    h = irr.Handle(irr.default_config(map_idx=0, exec=1))
+    h.set_params(irr.moldyn_params(float(L), 2.5))
+    h.set_edges(e)
+    h.set_nodes(pos32, 12)
+    h.init()
+    perm, row_off, col = h.partition()
+    deg = np.diff(row_off.astype(np.int64))
+    assert deg.max() <= 1024 and (deg > 256).sum() >= 3 and ((deg > 128) & (deg <= 256)).sum() >= 3
+    lo, scale = O.morton_frame(pos32)
+    operm, _, orow, ocol = O.partition(pos32, lo, scale, e, curve="hilbert")
+    assert np.array_equal(perm, operm)
+    assert np.array_equal(row_off, orow)
+    assert np.array_equal(col, ocol)
+    h.close()
+
+
 @pytest.mark.parametrize("shape", ["part", "part_direct", "part_g32", "part_g1"])
 def test_partitioned_is_bitwise_reproducible(built_lib, shape):
     import irregular_gb300 as irr
