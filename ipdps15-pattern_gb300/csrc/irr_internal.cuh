@@ -84,7 +84,6 @@ struct TiledShape {
 #ifndef IRR_CTAS_PER_SM
 #define IRR_CTAS_PER_SM 4
 #endif
-constexpr int kTiledThreads = 256;
 constexpr int kStages = IRR_STAGES;              // shared-memory ring depth
 constexpr int kStageEntries = IRR_STAGE_ENTRIES; // entries per stage (~20 KB)
 constexpr int kColPad = 4;                       // entries allocated past the end of col
@@ -155,7 +154,8 @@ struct PartitionOut {
 };
 // Per-axis min and max of pos (synchronises s).
 cudaError_t bbox_minmax(const float4* pos, int64_t n, float lo[3], float hi[3], cudaStream_t s);
-// Computes the Morton frame (per-axis min and 1024 / extent) of pos.
+// Computes the curve frame (per-axis min and 1024 / extent) of pos: the
+// 10-bit grid both node orders quantise on.
 cudaError_t bbox_frame(const float4* pos, int64_t n, float lo[3], float scale[3],
                        cudaStream_t s);
 // Full partition of n nodes and e half edges.  Allocates out's arrays with

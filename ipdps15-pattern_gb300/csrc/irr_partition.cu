@@ -805,7 +805,7 @@ cudaError_t build_partition(const float4* pos_user, int64_t n, const int2* edges
         while (bits < 31 && ((int64_t)1 << bits) < n) bits++;
         // (row, col) order: stable by column, then stable by row.  Ascending
         // columns inside a row put the lanes of one gather on fewer cache
-        // lines (the rows of a warp are Morton neighbours and share most of
+        // lines (the rows of a warp are curve neighbours and share most of
         // their neighbourhood), and make the layout independent of the
         // order of the edge list.
         IRR_CUDA_TRY(radix_sort_pairs(reinterpret_cast<uint32_t*>(out->col),

@@ -133,8 +133,10 @@ struct HotLaw {
     float band;    // |rd - rc2| < band: take the reference's FP64 decision
 };
 
-// What the consumers read of an instance, kept in registers across work
-// items of the same instance (items of one instance are consecutive).
+// What the consumers read of an instance.  Batched launches keep it in
+// registers across the work items of one instance (its items are
+// consecutive); single-instance launches rebuild it from the launch
+// parameter for every item, which costs no registers across items.
 struct InstHot {
     const float4* __restrict__ pos;
     const uint32_t* __restrict__ row_off;
