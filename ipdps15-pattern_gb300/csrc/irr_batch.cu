@@ -35,6 +35,7 @@ struct irr_batch {
     TiledShape shape{};
     bool finalized = false;
     InstDesc* d_insts = nullptr;
+    std::vector<InstDesc> host_insts;  // host copy of d_insts (the launch's parameter table)
     WorkItem* d_items = nullptr;
     int num_items = 0;
     int* d_queue = nullptr;
@@ -93,6 +94,7 @@ int upload_insts(irr_batch* b)
         B_CUDA(b, cudaMalloc(&b->d_insts, sizeof(InstDesc) * insts.size()), "instance table");
     B_CUDA(b, cudaMemcpy(b->d_insts, insts.data(), sizeof(InstDesc) * insts.size(), cudaMemcpyHostToDevice),
            "instance table");
+    b->host_insts = std::move(insts);
     return IRR_OK;
 }
 
@@ -131,7 +133,8 @@ int launch_step(irr_batch* b, const TiledShape& shape)
 {
     B_CUDA(b, cudaMemsetAsync(b->d_queue, 0, sizeof(int), b->stream), "queue");
     B_CUDA(b, launch_tiled(shape, b->d_insts, b->d_items, b->num_items, b->d_queue,
-                           b->sms * kCtasPerSm, b->d_status, b->stream), "batched kernel");
+                           b->sms * kCtasPerSm, b->d_status, b->stream, b->host_insts.data(),
+                           (int)b->host_insts.size()), "batched kernel");
     return IRR_OK;
 }
 

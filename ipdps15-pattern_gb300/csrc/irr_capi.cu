@@ -521,7 +521,7 @@ int irr_step(irr_handle* h)
     }
     H_CUDA(h, cudaMemsetAsync(h->d_queue, 0, sizeof(int), h->stream), "clear work queue");
     H_CUDA(h, launch_tiled(h->shape, h->d_inst, h->d_items, h->num_items, h->d_queue,
-                           h->sms * kCtasPerSm, h->d_status, h->stream, &h->inst),
+                           h->sms * kCtasPerSm, h->d_status, h->stream, &h->inst, 1),
            "tiled kernel");
     return IRR_OK;
 }

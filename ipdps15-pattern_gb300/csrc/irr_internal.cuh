@@ -126,13 +126,15 @@ inline bool sliced_pays(const Sliced& sl, int64_t entries)
 // -- reduction kernels (irr_reduce.cu) --
 cudaError_t launch_plain(const float4* pos, const int2* edges, int64_t e, float4* force,
                          const LawParams& law, cudaStream_t s);
-// A persistent grid of `grid` CTAs draws items from *queue (which must be 0
-// at launch).  `one` (host copy of d_insts[0]) may be given when every item
-// belongs to instance 0: the kernel then takes the descriptor as a launch
-// parameter and keeps no instance fields in registers.
+// A persistent grid of `grid` CTAs draws items from *d_queue (which must be
+// 0 at launch).  host_insts (a host copy of the num_insts descriptors of
+// d_insts) may be given: for one instance, or up to 512, the kernel then
+// takes the consumers' instance fields as a launch parameter and keeps none
+// in registers across items.
 cudaError_t launch_tiled(const TiledShape& shape, const InstDesc* d_insts,
                          const WorkItem* d_items, int num_items, int* d_queue, int grid,
-                         int* d_status, cudaStream_t s, const InstDesc* one = nullptr);
+                         int* d_status, cudaStream_t s, const InstDesc* host_insts = nullptr,
+                         int num_insts = 0);
 
 // -- data movement (irr_partition.cu) --
 // Raw node records (12/16/24 bytes) -> float4, optionally gathered: dst[k] =

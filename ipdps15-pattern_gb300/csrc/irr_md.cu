@@ -318,7 +318,7 @@ int md_forces(irr_md* m)
 {
     MD_CUDA(m, cudaMemsetAsync(m->d_queue, 0, sizeof(int), m->stream), "queue");
     MD_CUDA(m, launch_tiled(m->shape, m->d_inst, m->d_items, m->num_items, m->d_queue,
-                            m->sms * kCtasPerSm, m->d_status, m->stream, &m->inst), "force kernel");
+                            m->sms * kCtasPerSm, m->d_status, m->stream, &m->inst, 1), "force kernel");
     return IRR_OK;
 }
 

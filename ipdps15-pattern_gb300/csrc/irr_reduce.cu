@@ -29,6 +29,7 @@
 //   ordered rows whose columns ascend, the lanes of one gather also land on
 //   few cache lines.
 #include <algorithm>
+#include <type_traits>
 #include <vector>
 
 #include "irr_internal.cuh"
@@ -159,6 +160,50 @@ __device__ __forceinline__ InstHot load_hot(const InstDesc* __restrict__ I)
     h.H.half2 = I->law.half2;
     h.H.rc2 = I->law.rc2;
     h.H.band = I->law.band;
+    return h;
+}
+
+// Where a launch's consumers find the instance fields (the kernel's last
+// parameter, in the constant bank: its fields are read as operands where they
+// are used, so they need no registers across items -- at the 56-register
+// bound of 4 CTAs x 288 threads that is what removes the spills):
+//   SrcGlobal: from the descriptor table in global memory (any batch size);
+//   SrcOne:    every item belongs to instance 0, whose descriptor is the
+//              parameter;
+//   SrcTable:  up to kTableInsts instances, the consumers' fields of each in
+//              the parameter (the producer still reads col / scol, and the
+//              rare path the law, from the global table).
+struct SrcGlobal {
+    int unused;
+};
+struct SrcOne {
+    InstDesc d;
+};
+struct HotEntry {
+    const float4* pos;
+    const uint32_t* row_off;
+    const uint32_t* slice_off;
+    float4* force;
+    int64_t n;
+    HotLaw H;
+    float pad;
+};
+constexpr int kTableInsts = 512;  // 512 x 56 B stays inside the 32 KB of kernel parameters
+struct SrcTable {
+    HotEntry h[kTableInsts];
+};
+
+__device__ __forceinline__ InstHot hot_from(const SrcTable& t, const InstDesc* insts, int inst)
+{
+    const HotEntry& e = t.h[inst];
+    InstHot h;
+    h.pos = e.pos;
+    h.row_off = e.row_off;
+    h.slice_off = e.slice_off;
+    h.force = e.force;
+    h.cold = &insts[inst].law;
+    h.n = e.n;
+    h.H = e.H;
     return h;
 }
 
@@ -427,15 +472,14 @@ __device__ __forceinline__ void consume_sliced(const WorkItem& w, const InstHot&
 // wait is bounded; a wait that gives up sets kStatusWaitTimeout, waits once
 // more (bounded) for a copy that may be in flight, and leaves.
 //
-// ONE: every item belongs to instance 0, whose descriptor is the launch
-// parameter `one` (constant bank): its fields are read as operands where
-// they are used instead of being held in registers across items (at the
-// 56-register bound of 4 CTAs x 288 threads this removes the spills).
-template <bool PERIODIC, int G, bool ONE>
+// Src (SrcGlobal, SrcOne, SrcTable): where the instance fields come from.
+template <bool PERIODIC, int G, class Src>
 __global__ void __launch_bounds__(kPipeThreads, kCtasPerSm) tiled_kernel(
     const InstDesc* __restrict__ insts, const WorkItem* __restrict__ items, int num_items,
-    int* queue, int* status, int use_stages, const __grid_constant__ InstDesc one)
+    int* queue, int* status, int use_stages, const __grid_constant__ Src src)
 {
+    constexpr bool ONE = std::is_same<Src, SrcOne>::value;
+    constexpr bool TABLE = std::is_same<Src, SrcTable>::value;
     extern __shared__ int4 smem_raw[];
     int32_t* stage_base = reinterpret_cast<int32_t*>(smem_raw);
     constexpr int kStageInts = kStageEntries + kColPad;
@@ -480,9 +524,11 @@ __global__ void __launch_bounds__(kPipeThreads, kCtasPerSm) tiled_kernel(
                     s_smem[s] = 1;
                     const uint32_t a0 = w.ent0 & ~3u;
                     const uint32_t words = ((w.ent0 + w.nent - a0) + 3u) & ~3u;
-                    const InstDesc* I = ONE ? &one : insts + w.inst;
-                    const int32_t* src = (w.flags & kItemSliced) ? I->scol : I->col;
-                    bulk_load(stage_base + s * kStageInts, src + a0, words * 4u, &full[s]);
+                    const InstDesc* I;
+                    if constexpr (ONE) I = &src.d;
+                    else I = insts + w.inst;
+                    const int32_t* ent = (w.flags & kItemSliced) ? I->scol : I->col;
+                    bulk_load(stage_base + s * kStageInts, ent + a0, words * 4u, &full[s]);
                 }
             }
             if (!issue) {
@@ -505,12 +551,19 @@ __global__ void __launch_bounds__(kPipeThreads, kCtasPerSm) tiled_kernel(
         const int it = s_item[s];
         if (it >= num_items) return;
         const WorkItem w = items[it];
-        const InstDesc* I = ONE ? &one : insts + w.inst;
-        if (ONE) {
-            hot = load_hot(&one);
-        } else if (w.inst != cur) {
+        const InstDesc* I;
+        if constexpr (ONE) {
+            I = &src.d;
             hot = load_hot(I);
-            cur = w.inst;
+        } else if constexpr (TABLE) {
+            I = insts + w.inst;
+            hot = hot_from(src, insts, w.inst);
+        } else {
+            I = insts + w.inst;
+            if (w.inst != cur) {
+                hot = load_hot(I);
+                cur = w.inst;
+            }
         }
         if (w.flags & kItemSliced) {
             if (s_smem[s])
@@ -528,12 +581,12 @@ __global__ void __launch_bounds__(kPipeThreads, kCtasPerSm) tiled_kernel(
     }
 }
 
-template <bool PERIODIC, int G, bool ONE>
-cudaError_t launch_tiled_one(const TiledShape& shape, const InstDesc* d_insts,
+template <bool PERIODIC, int G, class Src>
+cudaError_t launch_tiled_src(const TiledShape& shape, const InstDesc* d_insts,
                              const WorkItem* d_items, int num_items, int* d_queue, int grid,
-                             int* d_status, cudaStream_t s, const InstDesc& one)
+                             int* d_status, cudaStream_t s, const Src& src)
 {
-    auto kern = tiled_kernel<PERIODIC, G, ONE>;
+    auto kern = tiled_kernel<PERIODIC, G, Src>;
     const size_t smem =
         shape.stage_smem ? (size_t)kStages * (kStageEntries + kColPad) * sizeof(int32_t) : 0;
     if (smem > 48 * 1024)
@@ -541,33 +594,44 @@ cudaError_t launch_tiled_one(const TiledShape& shape, const InstDesc* d_insts,
                                           (int)smem));
     if (grid <= 0 || num_items <= 0) return cudaSuccess;
     kern<<<grid, kPipeThreads, smem, s>>>(d_insts, d_items, num_items, d_queue, d_status,
-                                          shape.stage_smem, one);
+                                          shape.stage_smem, src);
     return cudaGetLastError();
 }
 
 template <bool PERIODIC, int G>
 cudaError_t launch_tiled_g(const TiledShape& shape, const InstDesc* d_insts,
                            const WorkItem* d_items, int num_items, int* d_queue, int grid,
-                           int* d_status, cudaStream_t s, const InstDesc* one)
+                           int* d_status, cudaStream_t s, const InstDesc* host_insts,
+                           int num_insts)
 {
-    if (one)
-        return launch_tiled_one<PERIODIC, G, true>(shape, d_insts, d_items, num_items, d_queue,
-                                                   grid, d_status, s, *one);
-    return launch_tiled_one<PERIODIC, G, false>(shape, d_insts, d_items, num_items, d_queue, grid,
-                                                d_status, s, InstDesc{});
+    if (host_insts && num_insts == 1)
+        return launch_tiled_src<PERIODIC, G>(shape, d_insts, d_items, num_items, d_queue, grid,
+                                             d_status, s, SrcOne{host_insts[0]});
+    if (host_insts && num_insts > 1 && num_insts <= kTableInsts) {
+        static thread_local SrcTable t;  // 28 KB: kept off the stack
+        for (int k = 0; k < num_insts; k++) {
+            const InstDesc& d = host_insts[k];
+            t.h[k] = HotEntry{d.pos, d.row_off, d.slice_off, d.force, d.n,
+                              HotLaw{d.law.half2, d.law.rc2, d.law.band}, 0.f};
+        }
+        return launch_tiled_src<PERIODIC, G>(shape, d_insts, d_items, num_items, d_queue, grid,
+                                             d_status, s, t);
+    }
+    return launch_tiled_src<PERIODIC, G>(shape, d_insts, d_items, num_items, d_queue, grid,
+                                         d_status, s, SrcGlobal{0});
 }
 
 template <bool PERIODIC>
 cudaError_t launch_tiled_p(const TiledShape& sh, const InstDesc* a, const WorkItem* b, int n,
-                           int* q, int grid, int* st, cudaStream_t s, const InstDesc* one)
+                           int* q, int grid, int* st, cudaStream_t s, const InstDesc* hi, int ni)
 {
     switch (sh.lanes_per_row) {
-    case 1: return launch_tiled_g<PERIODIC, 1>(sh, a, b, n, q, grid, st, s, one);
-    case 2: return launch_tiled_g<PERIODIC, 2>(sh, a, b, n, q, grid, st, s, one);
-    case 4: return launch_tiled_g<PERIODIC, 4>(sh, a, b, n, q, grid, st, s, one);
-    case 8: return launch_tiled_g<PERIODIC, 8>(sh, a, b, n, q, grid, st, s, one);
-    case 16: return launch_tiled_g<PERIODIC, 16>(sh, a, b, n, q, grid, st, s, one);
-    case 32: return launch_tiled_g<PERIODIC, 32>(sh, a, b, n, q, grid, st, s, one);
+    case 1: return launch_tiled_g<PERIODIC, 1>(sh, a, b, n, q, grid, st, s, hi, ni);
+    case 2: return launch_tiled_g<PERIODIC, 2>(sh, a, b, n, q, grid, st, s, hi, ni);
+    case 4: return launch_tiled_g<PERIODIC, 4>(sh, a, b, n, q, grid, st, s, hi, ni);
+    case 8: return launch_tiled_g<PERIODIC, 8>(sh, a, b, n, q, grid, st, s, hi, ni);
+    case 16: return launch_tiled_g<PERIODIC, 16>(sh, a, b, n, q, grid, st, s, hi, ni);
+    case 32: return launch_tiled_g<PERIODIC, 32>(sh, a, b, n, q, grid, st, s, hi, ni);
     default: return cudaErrorInvalidValue;
     }
 }
@@ -592,13 +656,13 @@ cudaError_t launch_plain(const float4* pos, const int2* edges, int64_t e, float4
 
 cudaError_t launch_tiled(const TiledShape& shape, const InstDesc* d_insts,
                          const WorkItem* d_items, int num_items, int* d_queue, int grid,
-                         int* d_status, cudaStream_t s, const InstDesc* one)
+                         int* d_status, cudaStream_t s, const InstDesc* host_insts, int num_insts)
 {
     if (!d_queue) return cudaErrorInvalidValue;
     return shape.periodic ? launch_tiled_p<true>(shape, d_insts, d_items, num_items, d_queue, grid,
-                                                 d_status, s, one)
+                                                 d_status, s, host_insts, num_insts)
                           : launch_tiled_p<false>(shape, d_insts, d_items, num_items, d_queue,
-                                                  grid, d_status, s, one);
+                                                  grid, d_status, s, host_insts, num_insts);
 }
 
 void make_work_items(const uint32_t* row_off, int64_t n, int inst, int max_rows, int staged,

@@ -505,7 +505,8 @@ int irr_serve_run(const irr_serve_config* cfg, irr_serve_stats* st, irr_serve_jo
         }
         if (cudaGetLastError() != cudaSuccess ||
             cudaMemsetAsync(d_queue, 0, sizeof(int), s) != cudaSuccess ||
-            launch_tiled(shape, tick_insts.d, d_items, (int)nitems, d_queue, sms * kCtasPerSm, d_status, s) != cudaSuccess) {
+            launch_tiled(shape, tick_insts.d, d_items, (int)nitems, d_queue, sms * kCtasPerSm, d_status, s,
+                         tick_insts.h, (int)live.size()) != cudaSuccess) {
             rc = IRR_ERR_CUDA;
             break;
         }
