@@ -6,10 +6,11 @@
 //   * admits arrived jobs in arrival order while their estimated device memory
 //     fits the budget (their state then stays resident until they finish);
 //   * every tick advances each resident job by one step: ONE kick/drift launch
-//     over all resident jobs, the rebuilds that are due, ONE batched force
-//     launch over all resident jobs' (instance, node block) work items (the
-//     item table is gathered on the device from each job's own), ONE kick
-//     launch;
+//     over all resident jobs; the rebuilds that are due start on worker
+//     threads while the other jobs' forces (one batched launch over their
+//     (instance, node block) work items, gathered on the device from each
+//     job's own table) and kicks (one launch) are queued; then the same two
+//     launches for the rebuilt jobs;
 //   * retires finished jobs (their memory frees up for waiting arrivals).
 // A job's rows are computed by the same kernel code whatever else shares the
 // launch, so its trajectory is bitwise the same alone and in the mix.
@@ -20,6 +21,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <memory>
 #include <numeric>
 #include <random>
 #include <thread>
@@ -141,16 +143,16 @@ struct Pinned {
     }
 };
 
-// Fills the job table for the resident jobs (their current arrays: a rebuild
-// swaps a job's state buffers) and uploads it on s; returns the launch's
-// block count and the batch's item count.
-bool upload_tick_jobs(const std::vector<Live>& live, Pinned<TickJob>& T, cudaStream_t s,
+// Fills the job table for the jobs ms (their current arrays: a rebuild swaps a
+// job's state buffers) and uploads it on s; returns the launch's block count
+// and the batch's item count.
+bool upload_tick_jobs(const std::vector<irr_md*>& ms, Pinned<TickJob>& T, cudaStream_t s,
                       int* blocks, int64_t* items)
 {
-    if (!T.reserve(live.size())) return false;
+    if (!T.reserve(ms.size())) return false;
     int64_t b = 0, it = 0;
-    for (size_t k = 0; k < live.size(); k++) {
-        const irr_md* m = live[k].md;
+    for (size_t k = 0; k < ms.size(); k++) {
+        const irr_md* m = ms[k];
         TickJob& J = T.h[k];
         J.x = m->x;
         J.v = m->v;
@@ -169,8 +171,78 @@ bool upload_tick_jobs(const std::vector<Live>& live, Pinned<TickJob>& T, cudaStr
     if (b > 0x7fffffffLL || it > 0x7fffffffLL) return false;
     *blocks = (int)b;
     *items = it;
-    return cudaMemcpyAsync(T.d, T.h, sizeof(TickJob) * live.size(), cudaMemcpyHostToDevice, s) ==
+    return cudaMemcpyAsync(T.d, T.h, sizeof(TickJob) * ms.size(), cudaMemcpyHostToDevice, s) ==
            cudaSuccess;
+}
+
+// The device tables of one force launch of a tick.
+struct ForceBatch {
+    Pinned<TickJob> jobs;
+    Pinned<InstDesc> insts;
+    WorkItem* d_items = nullptr;
+    size_t items_cap = 0;
+    void release()
+    {
+        jobs.release();
+        insts.release();
+        if (d_items) cudaFree(d_items);
+        d_items = nullptr;
+        items_cap = 0;
+    }
+};
+
+// The forces of the jobs ms (one persistent launch over their work items,
+// gathered on the device from each job's own table) and their closing kick
+// (one launch), queued on s.
+int force_and_kick(const std::vector<irr_md*>& ms, ForceBatch& B, const TiledShape& shape,
+                   int* d_queue, int* d_status, int sms, double dt, cudaStream_t s)
+{
+    if (ms.empty()) return IRR_OK;
+    int blocks = 0;
+    int64_t nitems = 0;
+    if (!upload_tick_jobs(ms, B.jobs, s, &blocks, &nitems) || !B.insts.reserve(ms.size()))
+        return IRR_ERR_CUDA;
+    for (size_t k = 0; k < ms.size(); k++) B.insts.h[k] = md_instance(ms[k]);
+    if ((size_t)nitems > B.items_cap) {
+        if (B.d_items) cudaFree(B.d_items);
+        B.items_cap = (size_t)nitems * 2;
+        if (cudaMalloc(&B.d_items, sizeof(WorkItem) * B.items_cap) != cudaSuccess) {
+            B.d_items = nullptr;
+            B.items_cap = 0;
+            return IRR_ERR_NOMEM;
+        }
+    }
+    if (cudaMemcpyAsync(B.insts.d, B.insts.h, sizeof(InstDesc) * ms.size(), cudaMemcpyHostToDevice, s) !=
+        cudaSuccess)
+        return IRR_ERR_CUDA;
+    if (nitems > 0) {
+        const int64_t want = (nitems + 255) / 256;
+        tick_items_kernel<<<(unsigned)(want < 4096 ? want : 4096), 256, 0, s>>>(B.jobs.d, (int)ms.size(),
+                                                                                nitems, B.d_items);
+    }
+    if (cudaGetLastError() != cudaSuccess || cudaMemsetAsync(d_queue, 0, sizeof(int), s) != cudaSuccess ||
+        launch_tiled(shape, B.insts.d, B.d_items, (int)nitems, d_queue, sms * kCtasPerSm, d_status, s,
+                     B.insts.h, (int)ms.size()) != cudaSuccess)
+        return IRR_ERR_CUDA;
+    tick_kick_kernel<<<blocks, kTickThreads, 0, s>>>(B.jobs.d, (int)ms.size(), dt);
+    return cudaGetLastError() == cudaSuccess ? IRR_OK : IRR_ERR_CUDA;
+}
+
+// Starts f(0..count-1) on up to `workers` host threads and returns them
+// (join them before using what f produces).
+template <class F>
+std::vector<std::thread> start_parallel(size_t count, unsigned workers, int device, F f)
+{
+    std::vector<std::thread> pool;
+    if (count == 0) return pool;
+    auto next = std::make_shared<std::atomic<size_t>>(0);
+    const size_t nth = std::min<size_t>(count, std::max(1u, workers));
+    for (size_t t = 0; t < nth; t++)
+        pool.emplace_back([=]() {
+            cudaSetDevice(device);
+            for (size_t i; (i = next->fetch_add(1)) < count;) f(i);
+        });
+    return pool;
 }
 
 // Runs f(0..count-1) on up to `workers` host threads (count small: inline).
@@ -347,10 +419,8 @@ int irr_serve_run(const irr_serve_config* cfg, irr_serve_stats* st, irr_serve_jo
     const int max_res = cfg->mode == IRR_SERVE_SERIAL ? 1 : cfg->max_resident;
     std::vector<double> latency;
     std::vector<Live> live;
-    Pinned<TickJob> tick_a, tick_b;  // before and after the tick's rebuilds
-    Pinned<InstDesc> tick_insts;
-    WorkItem* d_items = nullptr;
-    size_t items_cap = 0;
+    Pinned<TickJob> tick_a;        // every resident job (the kick-drift)
+    ForceBatch keep_b, due_b;      // the jobs without and with a rebuild this tick
     double used = 0.0, peak = 0.0, pair_evals = 0.0;
     size_t next = 0;
     int rc = IRR_OK;
@@ -449,70 +519,41 @@ int irr_serve_run(const irr_serve_config* cfg, irr_serve_stats* st, irr_serve_jo
             continue;
         }
         // one tick: every resident job advances one step
-        std::vector<size_t> due;
+        std::vector<irr_md*> all, keep, due;
+        for (auto& L : live) all.push_back(L.md);
         int blocks = 0;
         int64_t nitems = 0;
-        if (!upload_tick_jobs(live, tick_a, s, &blocks, &nitems)) { rc = IRR_ERR_CUDA; break; }
-        tick_kick_drift_kernel<1><<<blocks, kTickThreads, 0, s>>>(tick_a.d, (int)live.size(), cfg->dt);
+        if (!upload_tick_jobs(all, tick_a, s, &blocks, &nitems)) { rc = IRR_ERR_CUDA; break; }
+        tick_kick_drift_kernel<1><<<blocks, kTickThreads, 0, s>>>(tick_a.d, (int)all.size(), cfg->dt);
         if (cudaGetLastError() != cudaSuccess) { rc = IRR_ERR_CUDA; break; }
         for (size_t k = 0; k < live.size(); k++) {
             irr_md* m = live[k].md;
             m->since_rebuild++;  // the bookkeeping of md_kick_drift
-            if (m->since_rebuild >= m->cfg.rebuild_every) due.push_back(k);
+            (m->since_rebuild >= m->cfg.rebuild_every ? due : keep).push_back(m);
         }
-        if (!due.empty()) {
-            // rebuilds that are due run concurrently, each on its job's own
-            // stream after this tick's kick-drift; md_rebuild returns once its
-            // stream is done, so the force launch below sees the new layouts
-            cudaEventRecord(ev_kd, s);
-            std::vector<int> due_rc(due.size(), IRR_OK);
-            run_parallel(due.size(), workers, cfg->device, [&](size_t i) {
-                irr_md* m = live[due[i]].md;
-                m->stream = m->own_stream;
-                cudaStreamWaitEvent(m->stream, ev_kd, 0);
-                due_rc[i] = md_rebuild(m);
-                m->stream = s;
-            });
-            for (int r : due_rc)
-                if (r != IRR_OK && rc == IRR_OK) rc = r;
-            if (rc) break;
-        }
-        // the job table again (rebuilt jobs have new arrays and items), the
-        // instance table, the batch's items gathered on the device, one force
-        // launch, one kick launch
-        if (!upload_tick_jobs(live, tick_b, s, &blocks, &nitems) || !tick_insts.reserve(live.size())) {
-            rc = IRR_ERR_CUDA;
-            break;
-        }
-        for (size_t k = 0; k < live.size(); k++) {
-            tick_insts.h[k] = md_instance(live[k].md);
-            live[k].pair_evals += (double)live[k].md->edges;
-        }
-        if ((size_t)nitems > items_cap) {
-            if (d_items) cudaFree(d_items);
-            items_cap = (size_t)nitems * 2;
-            if (cudaMalloc(&d_items, sizeof(WorkItem) * items_cap) != cudaSuccess) { rc = IRR_ERR_NOMEM; break; }
-        }
-        if (cudaMemcpyAsync(tick_insts.d, tick_insts.h, sizeof(InstDesc) * live.size(),
-                            cudaMemcpyHostToDevice, s) != cudaSuccess) {
-            rc = IRR_ERR_CUDA;
-            break;
-        }
-        if (nitems > 0) {
-            const int64_t want = (nitems + 255) / 256;
-            tick_items_kernel<<<(unsigned)(want < 4096 ? want : 4096), 256, 0, s>>>(tick_b.d, (int)live.size(),
-                                                                                    nitems, d_items);
-        }
-        if (cudaGetLastError() != cudaSuccess ||
-            cudaMemsetAsync(d_queue, 0, sizeof(int), s) != cudaSuccess ||
-            launch_tiled(shape, tick_insts.d, d_items, (int)nitems, d_queue, sms * kCtasPerSm, d_status, s,
-                         tick_insts.h, (int)live.size()) != cudaSuccess) {
-            rc = IRR_ERR_CUDA;
-            break;
-        }
-        tick_kick_kernel<<<blocks, kTickThreads, 0, s>>>(tick_b.d, (int)live.size(), cfg->dt);
-        if (cudaGetLastError() != cudaSuccess) { rc = IRR_ERR_CUDA; break; }
+        // the rebuilds that are due start on worker threads, each on its
+        // job's own stream after this tick's kick-drift, while this thread
+        // queues the forces and kicks of the other jobs; the rebuilt jobs'
+        // forces and kicks follow once their rebuilds have returned
+        std::vector<int> due_rc(due.size(), IRR_OK);
+        if (!due.empty()) cudaEventRecord(ev_kd, s);
+        std::vector<std::thread> rebuilding = start_parallel(due.size(), workers, cfg->device, [&](size_t i) {
+            irr_md* m = due[i];
+            m->stream = m->own_stream;
+            cudaStreamWaitEvent(m->stream, ev_kd, 0);
+            due_rc[i] = md_rebuild(m);
+            m->stream = s;
+        });
+        const int krc = force_and_kick(keep, keep_b, shape, d_queue, d_status, sms, cfg->dt, s);
+        for (auto& th : rebuilding) th.join();
+        if (krc != IRR_OK) rc = krc;
+        for (int r : due_rc)
+            if (r != IRR_OK && rc == IRR_OK) rc = r;
+        if (rc) break;
+        rc = force_and_kick(due, due_b, shape, d_queue, d_status, sms, cfg->dt, s);
+        if (rc) break;
         for (auto& L : live) {
+            L.pair_evals += (double)L.md->edges;
             L.md->steps++;  // the bookkeeping of md_kick
             L.steps++;
         }
@@ -562,9 +603,8 @@ int irr_serve_run(const irr_serve_config* cfg, irr_serve_stats* st, irr_serve_jo
     int dev_status = 0;
     cudaMemcpy(&dev_status, d_status, sizeof(int), cudaMemcpyDeviceToHost);
     tick_a.release();
-    tick_b.release();
-    tick_insts.release();
-    if (d_items) cudaFree(d_items);
+    keep_b.release();
+    due_b.release();
     cudaFree(d_queue);
     cudaFree(d_status);
     cudaStreamDestroy(s);
