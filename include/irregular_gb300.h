@@ -319,7 +319,9 @@ typedef struct irr_md_config {
     double cutforce;   /* force cutoff (2.5)                                */
     double skin;       /* neighbour skin (0.3)                              */
     double side;       /* periodic box side; > 2 (cutforce + skin)          */
-    int reserved[8];
+    int reorder_every; /* every this many rebuilds the atoms are re-sorted  */
+                       /* along the curve (10; 0 or 1: every rebuild)       */
+    int reserved[7];
 } irr_md_config;
 
 typedef struct irr_md_info {

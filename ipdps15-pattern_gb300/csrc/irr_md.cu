@@ -5,7 +5,8 @@
 // and call IrregularStart once per step.  Here the whole loop stays on the GPU:
 //   kick + drift   v += dt/2 * F/m, x += dt * v, x wrapped into [0, L)   (FP64)
 //   rebuild        every `rebuild_every` steps: GPU neighbour list at
-//                  cutforce + skin, GPU partition (Hilbert order), state
+//                  cutforce + skin, GPU partition (the atoms re-sorted along
+//                  the Hilbert curve every reorder_every-th rebuild), state
 //                  permuted into the new order
 //   force          the owner-computes reduction (FP32 per edge, compensated)
 //   kick           v += dt/2 * F/m                                       (FP64)
@@ -257,21 +258,28 @@ int md_rebuild(irr_md* m)
                                    true, false),
             "neighbour build");
     free_part(m, s);
+    // The node order only decides locality: atoms move a fraction of the skin
+    // between rebuilds, so the curve order of an earlier rebuild stays nearly
+    // as local, and the atoms are re-sorted only every reorder_every-th
+    // rebuild (the first one included); the others keep the execution order.
+    const bool reorder = m->rebuilds % (m->cfg.reorder_every > 1 ? m->cfg.reorder_every : 1) == 0;
     PartitionOut p;
-    cudaError_t pe = build_partition(m->pos4, m->n, d_edges, e, 1, &p, s);
+    cudaError_t pe = build_partition(m->pos4, m->n, d_edges, e, reorder ? 1 : 0, &p, s);
     if (d_edges) cudaFreeAsync(d_edges, s);
     m->part = p;
     if (pe != cudaSuccess) return md_fail(m, IRR_ERR_CUDA, "partition", pe);
-    // state into the new order
-    const int g = grid_of(m->n);
-    gather3_kernel<<<g, 256, 0, s>>>(m->x, m->part.perm, m->n, m->tmp);
-    std::swap(m->x, m->tmp);
-    gather3_kernel<<<g, 256, 0, s>>>(m->v, m->part.perm, m->n, m->tmp);
-    std::swap(m->v, m->tmp);
-    gather_ids_kernel<<<g, 256, 0, s>>>(m->ids, m->part.perm, m->n, m->ids_tmp);
-    std::swap(m->ids, m->ids_tmp);
-    to_float4_kernel<<<g, 256, 0, s>>>(m->x, m->n, m->cfg.side, m->pos4);
-    MD_CUDA(m, cudaGetLastError(), "permute state");
+    if (reorder) {
+        // state into the new order
+        const int g = grid_of(m->n);
+        gather3_kernel<<<g, 256, 0, s>>>(m->x, m->part.perm, m->n, m->tmp);
+        std::swap(m->x, m->tmp);
+        gather3_kernel<<<g, 256, 0, s>>>(m->v, m->part.perm, m->n, m->tmp);
+        std::swap(m->v, m->tmp);
+        gather_ids_kernel<<<g, 256, 0, s>>>(m->ids, m->part.perm, m->n, m->ids_tmp);
+        std::swap(m->ids, m->ids_tmp);
+        to_float4_kernel<<<g, 256, 0, s>>>(m->x, m->n, m->cfg.side, m->pos4);
+        MD_CUDA(m, cudaGetLastError(), "permute state");
+    }
     // the sliced layout's work items are cut from its slice offsets (which
     // build_sliced brings to the host); only the CSR fallback needs the row
     // offsets on the host
@@ -391,6 +399,7 @@ void irr_md_config_default(irr_md_config* c)
     c->skin = 0.3;
     c->side = 0.0;
     c->rebuild_every = 20;
+    c->reorder_every = 10;
 }
 
 int irr_md_create(const irr_md_config* cfg, const double* pos, const double* vel, int64_t n,

@@ -67,7 +67,7 @@ class Info(C.Structure):
 class MDConfig(C.Structure):
     _fields_ = [("device", C.c_int), ("rebuild_every", C.c_int), ("dt", C.c_double),
                 ("cutforce", C.c_double), ("skin", C.c_double), ("side", C.c_double),
-                ("reserved", C.c_int * 8)]
+                ("reorder_every", C.c_int), ("reserved", C.c_int * 7)]
 
 
 class MDInfo(C.Structure):
@@ -518,12 +518,15 @@ class MD:
     """GPU Lennard-Jones MD (irr_md_*): FP64 state and integration, FP32 forces."""
 
     def __init__(self, pos, vel, side: float, dt: float = 0.005, cutforce: float = 2.5,
-                 skin: float = 0.3, rebuild_every: int = 20, device: int = 0):
+                 skin: float = 0.3, rebuild_every: int = 20, device: int = 0,
+                 reorder_every: Optional[int] = None):
         L = load()
         cfg = MDConfig()
         L.irr_md_config_default(C.byref(cfg))
         cfg.device, cfg.dt, cfg.cutforce, cfg.skin = device, dt, cutforce, skin
         cfg.side, cfg.rebuild_every = side, rebuild_every
+        if reorder_every is not None:
+            cfg.reorder_every = reorder_every
         p = np.ascontiguousarray(pos, np.float64).reshape(-1, 3)
         v = np.ascontiguousarray(vel, np.float64).reshape(-1, 3)
         self.n = p.shape[0]

@@ -34,12 +34,15 @@ def test_initial_forces_match_fp64(built_lib, oracle_lib, cells):
     md.close()
 
 
-def test_short_trajectory_matches_fp64_reference(built_lib, oracle_lib):
+@pytest.mark.parametrize("reorder_every", [1, 10])
+def test_short_trajectory_matches_fp64_reference(built_lib, oracle_lib, reorder_every):
+    """reorder_every 1: the second rebuild re-sorts the atoms; 10: it keeps
+    their order (either way the same physics)."""
     import irregular_gb300 as irr
     O = oracle_lib
     pos, vel, side = system()
     steps = 25  # crosses one rebuild (every 20 steps)
-    md = irr.MD(pos, vel, side, dt=0.005, rebuild_every=20)
+    md = irr.MD(pos, vel, side, dt=0.005, rebuild_every=20, reorder_every=reorder_every)
     md.run(steps)
     gp, gv = md.state()
     info = md.info()
