@@ -501,15 +501,20 @@ def run_md(args):
 def run_served(args):
     """Config 5: Poisson arrivals at 200 jobs/s, sizes log-uniform in
     [2,048, 2,097,152] atoms, density 0.8442, cutoff 2.5, 50 velocity-Verlet
-    steps each, 120 GB admission budget; continuous batching vs serial."""
+    steps each, 120 GB admission budget; continuous batching vs serial, both
+    admitting in arrival order, and continuous batching admitting the smallest
+    waiting job first."""
     import irregular_gb300 as irr
 
     out = {"leg": "served", "jobs": args.jobs, "arrival_rate_per_s": 200.0,
            "steps_per_job": 50, "budget_GB": 120.0,
            "data": "synthetic (seeded arrivals and sizes; FCC + jitter, Maxwell velocities)"}
-    for mode, name in ((irr.IRR_SERVE_CONTINUOUS, "continuous"), (irr.IRR_SERVE_SERIAL, "serial")):
-        st, _ = irr.serve(num_jobs=args.jobs, mode=mode, arrival_rate=200.0, steps_per_job=50,
-                          budget_bytes=120e9, seed=SEED + 5)
+    runs = ((irr.IRR_SERVE_CONTINUOUS, irr.IRR_SERVE_FIFO, "continuous"),
+            (irr.IRR_SERVE_SERIAL, irr.IRR_SERVE_FIFO, "serial"),
+            (irr.IRR_SERVE_CONTINUOUS, irr.IRR_SERVE_SJF, "continuous_sjf"))
+    for mode, policy, name in runs:
+        st, _ = irr.serve(num_jobs=args.jobs, mode=mode, policy=policy, arrival_rate=200.0,
+                          steps_per_job=50, budget_bytes=120e9, seed=SEED + 5)
         out[name] = {"p50_ms": st.p50_ms, "p99_ms": st.p99_ms, "mean_ms": st.mean_ms,
                      "max_ms": st.max_ms, "makespan_s": st.makespan_s,
                      "edges_per_s": st.edges_per_s, "jobs_done": int(st.jobs_done),

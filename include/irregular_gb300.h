@@ -364,6 +364,9 @@ IRR_API int irr_md_get_info(const irr_md *m, irr_md_info *info);
  * same jobs one at a time.  A job's trajectory is bitwise the same alone
  * (only_job = its index) and in the mix. */
 enum irr_serve_mode { IRR_SERVE_CONTINUOUS = 0, IRR_SERVE_SERIAL = 1 };
+/* Which waiting job a free slot admits: the earliest arrival, or the smallest
+ * job (shortest-job-first: the lowest mean latency, the largest jobs last). */
+enum irr_serve_policy { IRR_SERVE_FIFO = 0, IRR_SERVE_SJF = 1 };
 
 typedef struct irr_serve_config {
     int device;
@@ -384,7 +387,8 @@ typedef struct irr_serve_config {
     int64_t max_atoms;
     double budget_bytes; /* admission budget of device memory                 */
     uint64_t seed;
-    int reserved[8];
+    int policy;         /* enum irr_serve_policy: admission order (FIFO)      */
+    int reserved[7];
 } irr_serve_config;
 
 typedef struct irr_serve_stats {

@@ -393,6 +393,7 @@ int irr_serve_run(const irr_serve_config* cfg, irr_serve_stats* st, irr_serve_jo
         !(cfg->budget_bytes > 0) || cfg->max_resident < 1)
         return IRR_ERR_ARG;
     if (cfg->only_job >= cfg->num_jobs) return IRR_ERR_ARG;
+    if (cfg->policy != IRR_SERVE_FIFO && cfg->policy != IRR_SERVE_SJF) return IRR_ERR_ARG;
     memset(st, 0, sizeof(*st));
     if (cudaSetDevice(cfg->device) != cudaSuccess) {
         cudaGetLastError();
@@ -455,30 +456,40 @@ int irr_serve_run(const irr_serve_config* cfg, irr_serve_stats* st, irr_serve_jo
                                  : std::max(1u, std::min(std::thread::hardware_concurrency(), 16u));
     cudaEvent_t ev_kd = nullptr;
     cudaEventCreateWithFlags(&ev_kd, cudaEventDisableTiming);
-    while (rc == IRR_OK && (next < order.size() || !live.empty())) {
-        // admission, in arrival order, within the budget and the slot limit
-        while (next < order.size()) {
-            const JobSpec& j = jobs[order[next]];
-            if (j.arrival > now()) break;
-            if ((double)j.est_bytes > cfg->budget_bytes) {  // can never fit: rejected
+    std::vector<int> waiting;  // arrived, not yet admitted, in arrival order
+    while (rc == IRR_OK && (next < order.size() || !waiting.empty() || !live.empty())) {
+        // arrivals (a job larger than the whole budget is rejected)
+        while (next < order.size() && jobs[order[next]].arrival <= now()) {
+            const int k = order[next++];
+            if ((double)jobs[k].est_bytes > cfg->budget_bytes) {
                 if (out) {
-                    out[order[next]] = irr_serve_job{};
-                    out[order[next]].atoms = j.atoms;
-                    out[order[next]].arrival_s = j.arrival;
-                    out[order[next]].status = IRR_ERR_BUDGET;
+                    out[k] = irr_serve_job{};
+                    out[k].atoms = jobs[k].atoms;
+                    out[k].arrival_s = jobs[k].arrival;
+                    out[k].status = IRR_ERR_BUDGET;
                 }
                 st->rejected++;
-                next++;
                 continue;
             }
+            waiting.push_back(k);
+        }
+        // admission within the budget and the slot limit: the earliest
+        // arrival first (FIFO), or the smallest job first (SJF; ties by
+        // arrival) -- in either order, the first job that does not fit stops it
+        if (cfg->policy == IRR_SERVE_SJF)
+            std::stable_sort(waiting.begin(), waiting.end(),
+                             [&](int a, int b) { return jobs[a].atoms < jobs[b].atoms; });
+        size_t taken = 0;
+        while (taken < waiting.size()) {
+            const JobSpec& j = jobs[waiting[taken]];
             if ((int)(live.size() + admit.size()) >= max_res ||
                 used + (double)j.est_bytes > cfg->budget_bytes)
                 break;
-            admit.push_back(order[next]);
+            admit.push_back(waiting[taken++]);
             used += (double)j.est_bytes;
             peak = std::max(peak, used);
-            next++;
         }
+        waiting.erase(waiting.begin(), waiting.begin() + (std::ptrdiff_t)taken);
         if (!admit.empty()) {
             // the admitted jobs' set-up (upload + first neighbour build and
             // partition) runs concurrently, each on its own stream

@@ -88,7 +88,7 @@ class ServeConfig(C.Structure):
                 ("density", C.c_double), ("cutforce", C.c_double), ("skin", C.c_double),
                 ("dt", C.c_double), ("temperature", C.c_double), ("min_atoms", C.c_int64),
                 ("max_atoms", C.c_int64), ("budget_bytes", C.c_double), ("seed", C.c_uint64),
-                ("reserved", C.c_int * 8)]
+                ("policy", C.c_int), ("reserved", C.c_int * 7)]
 
 
 class ServeStats(C.Structure):
@@ -107,6 +107,8 @@ class ServeJob(C.Structure):
 
 IRR_SERVE_CONTINUOUS = 0
 IRR_SERVE_SERIAL = 1
+IRR_SERVE_FIFO = 0
+IRR_SERVE_SJF = 1
 
 
 # name -> (restype, argtypes); every symbol include/irregular_gb300.h declares

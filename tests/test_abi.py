@@ -53,6 +53,25 @@ def test_status_strings_and_defaults(built_lib):
     assert cfg.exec == irr.IRR_EXEC_PARTITIONED and cfg.reorder == 1 and cfg.stage_smem == -1
 
 
+def test_serve_and_md_config_defaults_and_validation(built_lib):
+    """New fields sit in the configs' reserved space with their defaults, and
+    a bad admission policy is refused before any device call."""
+    import ctypes as C
+    import irregular_gb300 as irr
+    L = irr.load()
+    sc = irr.ServeConfig()
+    L.irr_serve_config_default(C.byref(sc))
+    assert sc.policy == irr.IRR_SERVE_FIFO and sc.max_resident == 96
+    mc = irr.MDConfig()
+    L.irr_md_config_default(C.byref(mc))
+    assert mc.reorder_every == 10 and mc.rebuild_every == 20
+    # the sizes the structs had before the new fields took reserved slots
+    assert C.sizeof(irr.ServeConfig) == 144 and C.sizeof(irr.MDConfig) == 72
+    with pytest.raises(irr.IrregularError) as ei:
+        irr.serve(policy=7)
+    assert ei.value.status == irr.IRR_ERR_ARG
+
+
 def test_create_rejects_bad_config_without_crashing(built_lib):
     import irregular_gb300 as irr
     for bad in (dict(exec=7), dict(map_idx=9), dict(block_nodes=100), dict(lanes_per_row=3), dict(lanes_per_row=64)):

@@ -46,3 +46,16 @@ def test_latency_statistics(built_lib):
     assert stats.edges_per_s > 0 and stats.pair_evals > 0
     lat = sorted(1e3 * (j.done_s - j.arrival_s) for j in jobs)
     assert abs(stats.max_ms - lat[-1]) < 1e-6
+
+
+def test_shortest_job_first_admission(built_lib):
+    """One slot, every job waiting from the start: SJF admits them smallest
+    first (FIFO in arrival order), and each job's trajectory is the same."""
+    import irregular_gb300 as irr
+    cfg = dict(SMALL, arrival_rate=1e9, max_resident=1)
+    _, fifo = irr.serve(**cfg)
+    _, sjf = irr.serve(policy=irr.IRR_SERVE_SJF, **cfg)
+    by_admit = sorted(range(len(sjf)), key=lambda k: sjf[k].admit_s)
+    atoms = [sjf[k].atoms for k in by_admit]
+    assert atoms[1:] == sorted(atoms[1:])  # the first admission may precede the last arrival
+    assert [j.state_hash for j in sjf] == [j.state_hash for j in fifo]
