@@ -207,9 +207,12 @@ IRR_API int irr_step(irr_handle *h);
 /* get_reduction_result (irregular_runtime.cu:393-411): the per-node result
  * in the caller's node order, elm_size bytes per node (enum
  * irr_result_format), into host memory.  Synchronises the stream and reports
- * any device-side fault. */
+ * any device-side fault.  Page-locked host memory starting on a 16-byte
+ * boundary is written by the kernel in place (no staging copy); so is the
+ * node data irr_set_nodes reads after irr_init. */
 IRR_API int irr_get_result(irr_handle *h, void *out, int elm_size);
-/* Same, into device memory; enqueued, does not synchronise. */
+/* Same, into device memory (aligned to 4, 16 or 8 bytes for 12-, 16- or
+ * 24-byte records, else IRR_ERR_ARG); enqueued, does not synchronise. */
 IRR_API int irr_get_result_device(irr_handle *h, void *d_out, int elm_size);
 
 /* Waits for the handle's stream and reports any device-side fault. */

@@ -187,6 +187,18 @@ int set_nodes_common(irr_handle* h, const void* src, int elm, int64_t n, cudaMem
     if (!valid_node_elm(elm)) return fail(h, IRR_ERR_ARG, "node elm_size %d: use 12, 16 or 24", elm);
     if (n > 0x7fffffffLL) return fail(h, IRR_ERR_CAPACITY, "more than 2^31-1 nodes");
     if (h->inited && n != h->n) return fail(h, IRR_ERR_STATE, "node count changed after init (%lld -> %lld)", (long long)h->n, (long long)n);
+    if (kind == cudaMemcpyHostToDevice && h->inited && n > 0) {
+        // reset_node_data from page-locked host memory: the kernel reads the
+        // caller's records in order over the host link and scatters them into
+        // execution order (no staging copy, no second pass)
+        if (const void* mapped = host_device_view(src)) {
+            H_CUDA(h, launch_load_nodes_scatter(mapped, elm, h->part.inv, n, h->d_pos, h->stream),
+                   "load node data");
+            h->raw_elm = elm;
+            h->raw_pending = false;
+            return IRR_OK;
+        }
+    }
     int rc = ensure_raw(h, (size_t)(n > 0 ? n : 1) * (size_t)elm);
     if (rc) return rc;
     if (n > 0)
@@ -531,6 +543,10 @@ int irr_get_result_device(irr_handle* h, void* d_out, int elm_size)
     if (!h || !d_out) return fail(h, IRR_ERR_ARG, "null output");
     if (elm_size != 12 && elm_size != 16 && elm_size != 24) return fail(h, IRR_ERR_ARG, "result elm_size %d: use 12, 16 or 24", elm_size);
     if (!h->inited) return fail(h, IRR_ERR_STATE, "no result before irr_step");
+    const uintptr_t align = elm_size == 12 ? 4 : (elm_size == 16 ? 16 : 8);
+    if (reinterpret_cast<uintptr_t>(d_out) % align)
+        return fail(h, IRR_ERR_ARG, "result buffer not aligned to %d bytes for %d-byte records",
+                    (int)align, elm_size);
     cudaSetDevice(h->device);
     H_CUDA(h, launch_store_result(h->d_force, h->part.inv, h->n, elm_size, d_out, h->stream), "store result");
     return IRR_OK;
@@ -542,6 +558,15 @@ int irr_get_result(irr_handle* h, void* out, int elm_size)
     if (elm_size != 12 && elm_size != 16 && elm_size != 24) return fail(h, IRR_ERR_ARG, "result elm_size %d: use 12, 16 or 24", elm_size);
     if (!h->inited) return fail(h, IRR_ERR_STATE, "no result before irr_step");
     cudaSetDevice(h->device);
+    if (h->n > 0) {
+        // into page-locked host memory directly: written in order over the
+        // host link, gathered from execution order on the device
+        if (void* mapped = host_device_view(out)) {
+            H_CUDA(h, launch_store_result(h->d_force, h->part.inv, h->n, elm_size, mapped, h->stream),
+                   "store result");
+            return check_status(h);
+        }
+    }
     const size_t bytes = (size_t)(h->n > 0 ? h->n : 1) * elm_size;
     if (bytes > h->out_cap) {
         dfree(h->d_out);

@@ -141,7 +141,17 @@ cudaError_t launch_tiled(const TiledShape& shape, const InstDesc* d_insts,
 // rec[perm ? perm[k] : k].
 cudaError_t launch_load_nodes(const void* raw, int elm_size, const int32_t* perm, int64_t n,
                               float4* dst, cudaStream_t s);
-// Results: out[i] = force[inv ? inv[i] : i] in the requested format.
+// Records in the caller's order, read in order (rec may be page-locked host
+// memory the device addresses: see host_device_view) and scattered into
+// execution order: dst[inv ? inv[i] : i] = record i.
+cudaError_t launch_load_nodes_scatter(const void* rec, int elm_size, const int32_t* inv, int64_t n,
+                                      float4* dst, cudaStream_t s);
+// p itself when it is page-locked host memory that kernels can read and
+// write at the same address and it starts on a 16-byte boundary, else
+// nullptr (other host memory goes through staging copies).
+void* host_device_view(const void* p);
+// Results: out[i] = force[inv ? inv[i] : i] in the requested format, written
+// in order (out may be device memory or page-locked host memory).
 cudaError_t launch_store_result(const float4* force, const int32_t* inv, int64_t n,
                                 int elm_size, void* out, cudaStream_t s);
 cudaError_t launch_validate_edges(const int2* edges, int64_t e, int64_t n, int* d_status,

@@ -504,10 +504,85 @@ __global__ void load_nodes_kernel(const char* raw, int elm, const int32_t* perm,
     }
 }
 
-__global__ void store_result_kernel(const float4* force, const int32_t* inv, int64_t n, int elm,
-                                    char* out)
+// Node records read in order -- from page-locked host memory the device
+// addresses directly, where the link wants contiguous reads -- and scattered
+// into execution order on the device: dst[inv ? inv[i] : i] = record i.
+// vec12: 12-byte records at a 16-byte aligned base.  A block moves tiles of
+// kMoveThreads * 4 records (3 * kMoveThreads 16-byte words): the words are
+// loaded with consecutive threads on consecutive words (each warp instruction
+// one contiguous 512-byte run: what the host link wants), then each thread
+// takes its four records from shared memory.
+constexpr int kMoveThreads = 256;
+
+__global__ void __launch_bounds__(kMoveThreads) load_nodes_scatter_kernel(
+    const char* __restrict__ rec, int elm, int vec12, const int32_t* __restrict__ inv, int64_t n,
+    float4* __restrict__ dst)
 {
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+    __shared__ float4 tile[3 * kMoveThreads];
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    int64_t head = 0;  // records moved in whole tiles
+    if (vec12) {
+        constexpr int64_t kTile = 4 * kMoveThreads;
+        head = n / kTile * kTile;
+        const float4* w = reinterpret_cast<const float4*>(rec);
+        for (int64_t t0 = (int64_t)blockIdx.x * kTile; t0 < head; t0 += (int64_t)gridDim.x * kTile) {
+            const float4* src = w + t0 / 4 * 3;
+#pragma unroll
+            for (int k = 0; k < 3; k++) tile[k * kMoveThreads + threadIdx.x] = src[k * kMoveThreads + threadIdx.x];
+            __syncthreads();
+            const float4 a = tile[3 * threadIdx.x], b = tile[3 * threadIdx.x + 1], c = tile[3 * threadIdx.x + 2];
+            __syncthreads();
+            const int64_t i = t0 + 4 * threadIdx.x;
+            dst[inv ? inv[i] : i] = make_float4(a.x, a.y, a.z, 0.f);
+            dst[inv ? inv[i + 1] : i + 1] = make_float4(a.w, b.x, b.y, 0.f);
+            dst[inv ? inv[i + 2] : i + 2] = make_float4(b.z, b.w, c.x, 0.f);
+            dst[inv ? inv[i + 3] : i + 3] = make_float4(c.y, c.z, c.w, 0.f);
+        }
+    }
+    for (int64_t i = head + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        float4 p;
+        if (elm == 24) {
+            const double* d = reinterpret_cast<const double*>(rec + i * 24);
+            p = make_float4((float)d[0], (float)d[1], (float)d[2], 0.f);
+        } else if (elm == 16) {
+            p = reinterpret_cast<const float4*>(rec)[i];
+            p.w = 0.f;
+        } else {
+            const float* f = reinterpret_cast<const float*>(rec + i * 12);
+            p = make_float4(f[0], f[1], f[2], 0.f);
+        }
+        dst[inv ? inv[i] : i] = p;
+    }
+}
+
+// Results in the caller's order: out[i] = force[inv ? inv[i] : i], written in
+// order (device staging or page-locked host memory).  vec12: 12-byte records
+// at a 16-byte aligned base, packed four per thread into shared memory and
+// stored in tiles with consecutive threads on consecutive 16-byte words.
+__global__ void __launch_bounds__(kMoveThreads) store_result_kernel(
+    const float4* force, const int32_t* inv, int64_t n, int elm, int vec12, char* out)
+{
+    __shared__ float4 tile[3 * kMoveThreads];
+    int64_t head = 0;
+    if (vec12) {
+        constexpr int64_t kTile = 4 * kMoveThreads;
+        head = n / kTile * kTile;
+        float4* w = reinterpret_cast<float4*>(out);
+        for (int64_t t0 = (int64_t)blockIdx.x * kTile; t0 < head; t0 += (int64_t)gridDim.x * kTile) {
+            const int64_t i = t0 + 4 * threadIdx.x;
+            const float4 f0 = force[inv ? inv[i] : i], f1 = force[inv ? inv[i + 1] : i + 1];
+            const float4 f2 = force[inv ? inv[i + 2] : i + 2], f3 = force[inv ? inv[i + 3] : i + 3];
+            tile[3 * threadIdx.x] = make_float4(f0.x, f0.y, f0.z, f1.x);
+            tile[3 * threadIdx.x + 1] = make_float4(f1.y, f1.z, f2.x, f2.y);
+            tile[3 * threadIdx.x + 2] = make_float4(f2.z, f3.x, f3.y, f3.z);
+            __syncthreads();
+            float4* dstw = w + t0 / 4 * 3;
+#pragma unroll
+            for (int k = 0; k < 3; k++) dstw[k * kMoveThreads + threadIdx.x] = tile[k * kMoveThreads + threadIdx.x];
+            __syncthreads();
+        }
+    }
+    for (int64_t i = head + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x) {
         const float4 f = force[inv ? inv[i] : i];
         if (elm == 24) {
@@ -901,9 +976,35 @@ cudaError_t launch_store_result(const float4* force, const int32_t* inv, int64_t
                                 int elm_size, void* out, cudaStream_t s)
 {
     if (n <= 0) return cudaSuccess;
-    store_result_kernel<<<grid_for(n), 256, 0, s>>>(force, inv, n, elm_size,
-                                                    static_cast<char*>(out));
+    const int vec12 = elm_size == 12 && (reinterpret_cast<uintptr_t>(out) & 15u) == 0;
+    store_result_kernel<<<grid_for(n, kMoveThreads), kMoveThreads, 0, s>>>(force, inv, n, elm_size,
+                                                                          vec12, static_cast<char*>(out));
     return cudaGetLastError();
+}
+
+cudaError_t launch_load_nodes_scatter(const void* rec, int elm_size, const int32_t* inv, int64_t n,
+                                      float4* dst, cudaStream_t s)
+{
+    if (n <= 0) return cudaSuccess;
+    const int vec12 = elm_size == 12 && (reinterpret_cast<uintptr_t>(rec) & 15u) == 0;
+    load_nodes_scatter_kernel<<<grid_for(n, kMoveThreads), kMoveThreads, 0, s>>>(
+        static_cast<const char*>(rec), elm_size, vec12, inv, n, dst);
+    return cudaGetLastError();
+}
+
+void* host_device_view(const void* p)
+{
+    if (!p) return nullptr;
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    // page-locked (or registered) host memory mapped at the same address, at
+    // a 16-byte boundary (every record format's loads and stores then align)
+    const bool ok = a.type == cudaMemoryTypeHost && a.devicePointer == p &&
+                    (reinterpret_cast<uintptr_t>(p) & 15u) == 0;
+    return ok ? const_cast<void*>(p) : nullptr;
 }
 
 cudaError_t launch_validate_edges(const int2* edges, int64_t e, int64_t n, int* d_status,

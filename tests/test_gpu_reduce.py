@@ -200,6 +200,70 @@ def test_result_formats_agree(built_lib, exec_mode):
     assert np.array_equal(f12.astype(np.float64), f24)
 
 
+@pytest.mark.parametrize("offset", [0, 4])
+@pytest.mark.parametrize("exec_mode", [0, 1])
+@pytest.mark.parametrize("fmt", [12, 16, 24])
+def test_page_locked_host_buffers(built_lib, exec_mode, fmt, offset):
+    """Page-locked caller buffers on a 16-byte boundary are read and written
+    by the kernels in place; other buffers (offset 4) go through staging.
+    Either way the partitioned results equal those through pageable buffers
+    bit for bit (the plain path's atomics only to rounding)."""
+    torch = pytest.importorskip("torch")
+    import irregular_gb300 as irr
+    c = load_golden("moldyn_random_2048")
+    n = c["pos"].shape[0]
+    dt = np.float64 if fmt == 24 else np.float32
+    width = fmt // np.dtype(dt).itemsize
+    rec = np.zeros((n, width), dt)
+    rec[:, :3] = c["pos"]
+    moved = rec.copy()
+    moved[:, :3] += np.random.Generator(np.random.PCG64(3)).normal(0, 1e-3, (n, 3)).astype(dt)
+    h = irr.Handle(irr.default_config(map_idx=0, exec=exec_mode))
+    h.set_params(c["param"])
+    h.set_edges(c["edges"])
+    h.set_nodes(rec, fmt)
+    h.step()
+    h.set_nodes(moved, fmt)  # pageable: staged
+    h.step()
+    ref = h.get_result(elm_size=fmt)
+
+    def pinned_view(shape, dtype):
+        raw = torch.empty(int(np.prod(shape)) * np.dtype(dtype).itemsize + 16, dtype=torch.uint8,
+                          pin_memory=True).numpy()
+        return np.frombuffer(raw.data, dtype=dtype, count=int(np.prod(shape)),
+                             offset=offset).reshape(shape), raw
+
+    h.set_nodes(rec, fmt)
+    h.step()
+    view_in, keep_in = pinned_view(moved.shape, dt)
+    view_in[:] = moved
+    h.set_nodes(view_in, fmt)
+    h.step()
+    view_out, keep_out = pinned_view(ref.shape, ref.dtype)
+    h.get_result(view_out, elm_size=fmt)
+    if exec_mode == 1:
+        assert np.array_equal(view_out.view(np.uint8), ref.view(np.uint8))
+    else:  # the plain path's float atomics add in no fixed order
+        assert normwise_error(view_out[:, :3], ref[:, :3]) <= TOL_NORMWISE_F64
+    h.close()
+
+
+def test_device_result_buffer_alignment_is_checked(built_lib):
+    torch = pytest.importorskip("torch")
+    import irregular_gb300 as irr
+    c = load_golden("moldyn_random_2048")
+    f, h = run_case(irr, c, exec=1)
+    d = torch.zeros(c["pos"].shape[0] * 6 + 4, dtype=torch.float32, device="cuda")
+    with pytest.raises(irr.IrregularError) as ei:
+        h.get_result_device(d[1:], elm_size=24)  # 4-byte aligned, 8 needed
+    assert ei.value.status == irr.IRR_ERR_ARG
+    h.get_result_device(d[2:], elm_size=24)
+    torch.cuda.synchronize()
+    got = d[2:2 + 6 * f.shape[0]].cpu().numpy().view(np.float64).reshape(-1, 3)
+    assert np.array_equal(got, f.astype(np.float64))
+    h.close()
+
+
 @pytest.mark.parametrize("exec_mode", [0, 1])
 @pytest.mark.parametrize("fmt", [12, 16, 24])
 def test_reset_node_data(built_lib, oracle_lib, exec_mode, fmt):
