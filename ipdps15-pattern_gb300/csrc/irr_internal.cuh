@@ -123,6 +123,20 @@ inline bool sliced_pays(const Sliced& sl, int64_t entries)
     return sl.words <= entries + entries / 2 + 64;
 }
 
+// -- device memory --
+// Stream-ordered allocation from the library's own memory pool on the current
+// device.  Its release threshold is unlimited: blocks freed with
+// cudaFreeAsync stay in the pool for the next allocation instead of going back
+// to the driver at every synchronisation (the default pool's behaviour), so a
+// rebuild that frees and re-allocates ~300 MB of layout does not re-map it.
+// The pool keeps the library's peak footprint until the process exits.
+cudaError_t irr_malloc_async(void** p, size_t bytes, cudaStream_t s);
+template <class T>
+inline cudaError_t irr_malloc_async(T** p, size_t bytes, cudaStream_t s)
+{
+    return irr_malloc_async(reinterpret_cast<void**>(p), bytes, s);
+}
+
 // -- reduction kernels (irr_reduce.cu) --
 cudaError_t launch_plain(const float4* pos, const int2* edges, int64_t e, float4* force,
                          const LawParams& law, cudaStream_t s);

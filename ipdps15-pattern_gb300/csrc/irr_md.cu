@@ -299,7 +299,7 @@ int md_rebuild(irr_md* m)
     std::vector<WorkItem> items;
     make_instance_items(ro.data(), m->sl, m->n, 0, m->shape, items);
     m->num_items = (int)items.size();
-    MD_CUDA(m, cudaMallocAsync(&m->d_items, sizeof(WorkItem) * (items.empty() ? 1 : items.size()), s),
+    MD_CUDA(m, irr_malloc_async(&m->d_items, sizeof(WorkItem) * (items.empty() ? 1 : items.size()), s),
             "work items");
     if (!items.empty())
         MD_CUDA(m, cudaMemcpyAsync(m->d_items, items.data(), sizeof(WorkItem) * items.size(),
@@ -449,17 +449,17 @@ int irr_md_create(const irr_md_config* cfg, const double* pos, const double* vel
     cudaError_t e = cudaSuccess;
     // stream-ordered (no device-wide synchronisation; see free_part)
     cudaStream_t os = m->own_stream;
-    if (e == cudaSuccess) e = cudaMallocAsync(&m->x, b3, os);
-    if (e == cudaSuccess) e = cudaMallocAsync(&m->v, b3, os);
-    if (e == cudaSuccess) e = cudaMallocAsync(&m->tmp, b3, os);
-    if (e == cudaSuccess) e = cudaMallocAsync(&m->pos4, sizeof(float4) * n, os);
-    if (e == cudaSuccess) e = cudaMallocAsync(&m->force, sizeof(float4) * n, os);
-    if (e == cudaSuccess) e = cudaMallocAsync(&m->ids, sizeof(int32_t) * n, os);
-    if (e == cudaSuccess) e = cudaMallocAsync(&m->ids_tmp, sizeof(int32_t) * n, os);
-    if (e == cudaSuccess) e = cudaMallocAsync(&m->d_inst, sizeof(InstDesc), os);
-    if (e == cudaSuccess) e = cudaMallocAsync(&m->d_queue, sizeof(int), os);
-    if (e == cudaSuccess) e = cudaMallocAsync(&m->d_status, sizeof(int), os);
-    if (e == cudaSuccess) e = cudaMallocAsync(&m->d_acc, (4 + 3 * kEnergyBlocks) * sizeof(double), os);
+    if (e == cudaSuccess) e = irr_malloc_async(&m->x, b3, os);
+    if (e == cudaSuccess) e = irr_malloc_async(&m->v, b3, os);
+    if (e == cudaSuccess) e = irr_malloc_async(&m->tmp, b3, os);
+    if (e == cudaSuccess) e = irr_malloc_async(&m->pos4, sizeof(float4) * n, os);
+    if (e == cudaSuccess) e = irr_malloc_async(&m->force, sizeof(float4) * n, os);
+    if (e == cudaSuccess) e = irr_malloc_async(&m->ids, sizeof(int32_t) * n, os);
+    if (e == cudaSuccess) e = irr_malloc_async(&m->ids_tmp, sizeof(int32_t) * n, os);
+    if (e == cudaSuccess) e = irr_malloc_async(&m->d_inst, sizeof(InstDesc), os);
+    if (e == cudaSuccess) e = irr_malloc_async(&m->d_queue, sizeof(int), os);
+    if (e == cudaSuccess) e = irr_malloc_async(&m->d_status, sizeof(int), os);
+    if (e == cudaSuccess) e = irr_malloc_async(&m->d_acc, (4 + 3 * kEnergyBlocks) * sizeof(double), os);
     if (e == cudaSuccess) e = cudaMemsetAsync(m->d_status, 0, sizeof(int), m->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(m->x, pos, b3, cudaMemcpyHostToDevice, m->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(m->v, vel, b3, cudaMemcpyHostToDevice, m->stream);

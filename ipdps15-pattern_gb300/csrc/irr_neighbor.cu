@@ -272,12 +272,12 @@ cudaError_t build_neighbor_list(const float4* pos, int64_t n, float box, float c
     const int64_t ncell = (int64_t)g.nc[0] * g.nc[1] * g.nc[2];
     uint32_t *keys = nullptr, *keys_tmp = nullptr, *cell_start = nullptr, *cnt = nullptr;
     int32_t *sorted = nullptr, *vals_tmp = nullptr, *nbr = nullptr;
-    IRR_CUDA_TRY(cudaMallocAsync((void**)&keys, sizeof(uint32_t) * n, s));
-    IRR_CUDA_TRY(cudaMallocAsync((void**)&keys_tmp, sizeof(uint32_t) * n, s));
-    IRR_CUDA_TRY(cudaMallocAsync((void**)&sorted, sizeof(int32_t) * n, s));
-    IRR_CUDA_TRY(cudaMallocAsync((void**)&vals_tmp, sizeof(int32_t) * n, s));
-    IRR_CUDA_TRY(cudaMallocAsync((void**)&cell_start, sizeof(uint32_t) * (ncell + 1), s));
-    IRR_CUDA_TRY(cudaMallocAsync((void**)&cnt, sizeof(uint32_t) * (n + 1), s));
+    IRR_CUDA_TRY(irr_malloc_async((void**)&keys, sizeof(uint32_t) * n, s));
+    IRR_CUDA_TRY(irr_malloc_async((void**)&keys_tmp, sizeof(uint32_t) * n, s));
+    IRR_CUDA_TRY(irr_malloc_async((void**)&sorted, sizeof(int32_t) * n, s));
+    IRR_CUDA_TRY(irr_malloc_async((void**)&vals_tmp, sizeof(int32_t) * n, s));
+    IRR_CUDA_TRY(irr_malloc_async((void**)&cell_start, sizeof(uint32_t) * (ncell + 1), s));
+    IRR_CUDA_TRY(irr_malloc_async((void**)&cnt, sizeof(uint32_t) * (n + 1), s));
     IRR_CUDA_TRY(cudaMemsetAsync(cell_start, 0, sizeof(uint32_t) * (ncell + 1), s));
     cell_keys_kernel<<<grid_of(n), 256, 0, s>>>(pos, n, g, keys, sorted, cell_start);
     IRR_CUDA_TRY(cudaGetLastError());
@@ -286,7 +286,7 @@ cudaError_t build_neighbor_list(const float4* pos, int64_t n, float box, float c
     IRR_CUDA_TRY(radix_sort_pairs(keys, sorted, keys_tmp, vals_tmp, n, bits, s));
     IRR_CUDA_TRY(scan_exclusive_u32(cell_start, cell_start, ncell + 1, nullptr, s));
     float4* pos_c = nullptr;
-    IRR_CUDA_TRY(cudaMallocAsync((void**)&pos_c, sizeof(float4) * n, s));
+    IRR_CUDA_TRY(irr_malloc_async((void**)&pos_c, sizeof(float4) * n, s));
     cell_order_kernel<<<grid_of(n), 256, 0, s>>>(pos, sorted, n, pos_c);
     IRR_CUDA_TRY(cudaGetLastError());
     // rows in any order are asked for: the half stencil, where the box allows it
@@ -312,14 +312,14 @@ cudaError_t build_neighbor_list(const float4* pos, int64_t n, float box, float c
     int2* edges = nullptr;
     if (total > 0) {
         if (stream_ordered)
-            IRR_CUDA_TRY(cudaMallocAsync((void**)&edges, sizeof(int2) * total, s));
+            IRR_CUDA_TRY(irr_malloc_async((void**)&edges, sizeof(int2) * total, s));
         else
             IRR_CUDA_TRY(cudaMalloc((void**)&edges, sizeof(int2) * total));
         if (sort_rows) {
             uint32_t longest = 0;
             IRR_CUDA_TRY(max_row_len(cnt, n, &longest, s));
             const int sort_here = longest > (uint32_t)kRowSortMax;
-            IRR_CUDA_TRY(cudaMallocAsync((void**)&nbr, sizeof(int32_t) * total, s));
+            IRR_CUDA_TRY(irr_malloc_async((void**)&nbr, sizeof(int32_t) * total, s));
             pairs_kernel<true><<<grid_of(n), 256, 0, s>>>(pos_c, sorted, cell_start, n, g, nullptr,
                                                           cnt, nbr, nullptr, sort_here);
             IRR_CUDA_TRY(cudaGetLastError());

@@ -22,6 +22,7 @@
 // 4. Optionally the sliced layout (struct Sliced): the same entries regrouped
 //    so that one warp reads one contiguous line per step.
 #include <algorithm>
+#include <mutex>
 
 #include "irr_internal.cuh"
 
@@ -623,8 +624,7 @@ int grid_for(int64_t n, int threads = 256)
 template <class T>
 cudaError_t alloc_async(T** p, int64_t count, cudaStream_t s)
 {
-    return cudaMallocAsync(reinterpret_cast<void**>(p), sizeof(T) * (size_t)(count > 0 ? count : 1),
-                           s);
+    return irr_malloc_async(p, sizeof(T) * (size_t)(count > 0 ? count : 1), s);
 }
 
 // ------------------------------------------------------- sliced layout
@@ -1013,6 +1013,40 @@ cudaError_t launch_validate_edges(const int2* edges, int64_t e, int64_t n, int* 
     if (e <= 0) return cudaSuccess;
     validate_edges_kernel<<<grid_for(e), 256, 0, s>>>(edges, e, n, d_status);
     return cudaGetLastError();
+}
+
+namespace {
+constexpr int kMaxPoolDevices = 64;
+std::mutex g_pool_mutex;
+cudaMemPool_t g_pools[kMaxPoolDevices] = {};
+}  // namespace
+
+cudaError_t irr_malloc_async(void** p, size_t bytes, cudaStream_t s)
+{
+    int dev = 0;
+    IRR_CUDA_TRY(cudaGetDevice(&dev));
+    cudaMemPool_t pool = nullptr;
+    if (dev >= 0 && dev < kMaxPoolDevices) {
+        std::lock_guard<std::mutex> lock(g_pool_mutex);
+        if (!g_pools[dev]) {
+            cudaMemPoolProps props{};
+            props.allocType = cudaMemAllocationTypePinned;
+            props.handleTypes = cudaMemHandleTypeNone;
+            props.location.type = cudaMemLocationTypeDevice;
+            props.location.id = dev;
+            cudaMemPool_t made = nullptr;
+            if (cudaMemPoolCreate(&made, &props) == cudaSuccess) {
+                uint64_t keep = ~0ull;
+                cudaMemPoolSetAttribute(made, cudaMemPoolAttrReleaseThreshold, &keep);
+                g_pools[dev] = made;
+            } else {
+                cudaGetLastError();
+            }
+        }
+        pool = g_pools[dev];
+    }
+    if (!pool) return cudaMallocAsync(p, bytes, s);  // the device's default pool
+    return cudaMallocFromPoolAsync(p, bytes, pool, s);
 }
 
 }  // namespace irr
