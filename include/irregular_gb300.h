@@ -378,7 +378,7 @@ typedef struct irr_serve_config {
     int rebuild_every;
     int mode;           /* enum irr_serve_mode                                 */
     int only_job;       /* >= 0: run that job alone (arriving at t = 0)        */
-    int max_resident;   /* slot limit on resident jobs (default 96)            */
+    int max_resident;   /* slot limit on resident jobs (default 64)            */
     int reserved0;
     double arrival_rate; /* jobs per second (Poisson)                         */
     double density;

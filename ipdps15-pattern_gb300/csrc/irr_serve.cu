@@ -369,10 +369,11 @@ void irr_serve_config_default(irr_serve_config* c)
     c->mode = IRR_SERVE_CONTINUOUS;
     c->only_job = -1;
     // A tick advances every resident job, so its time grows with the resident
-    // set and every resident job waits for it: with no limit the 200-job
-    // stream (200 jobs/s, 2K-2M atoms) had p50 1.44-1.48 s; with 96 slots,
-    // 1.08-1.09 s at a 2 % longer makespan (64: 1.15 s, 128: 1.30-1.35 s).
-    c->max_resident = 96;
+    // set and every resident job waits for it.  The 200-job stream (200
+    // jobs/s, 2K-2M atoms): p50 / p99 / makespan 0.51 / 0.60 / 1.36 s with no
+    // limit, 0.51 / 0.60 / 1.38 s with 96 slots, 0.41 / 0.54 / 1.37 s with 64,
+    // 0.40 / 0.53 / 1.40 s with 48, 0.38 / 0.53 / 1.45 s with 32.
+    c->max_resident = 64;
     c->arrival_rate = 200.0;
     c->density = 0.8442;
     c->cutforce = 2.5;

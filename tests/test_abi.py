@@ -61,7 +61,7 @@ def test_serve_and_md_config_defaults_and_validation(built_lib):
     L = irr.load()
     sc = irr.ServeConfig()
     L.irr_serve_config_default(C.byref(sc))
-    assert sc.policy == irr.IRR_SERVE_FIFO and sc.max_resident == 96
+    assert sc.policy == irr.IRR_SERVE_FIFO and sc.max_resident == 64
     mc = irr.MDConfig()
     L.irr_md_config_default(C.byref(mc))
     assert mc.reorder_every == 10 and mc.rebuild_every == 20
