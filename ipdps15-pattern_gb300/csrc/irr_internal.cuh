@@ -142,9 +142,9 @@ cudaError_t launch_plain(const float4* pos, const int2* edges, int64_t e, float4
                          const LawParams& law, cudaStream_t s);
 // A persistent grid of `grid` CTAs draws items from *d_queue (which must be
 // 0 at launch).  host_insts (a host copy of the num_insts descriptors of
-// d_insts) may be given: for one instance, or up to 512, the kernel then
-// takes the consumers' instance fields as a launch parameter and keeps none
-// in registers across items.
+// d_insts) may be given: for one instance (the whole descriptor), or up to
+// 1024 (the fields the step loop reads), the kernel then takes them as a
+// launch parameter instead of holding them in registers across items.
 cudaError_t launch_tiled(const TiledShape& shape, const InstDesc* d_insts,
                          const WorkItem* d_items, int num_items, int* d_queue, int grid,
                          int* d_status, cudaStream_t s, const InstDesc* host_insts = nullptr,

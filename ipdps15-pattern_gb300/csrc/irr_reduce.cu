@@ -170,9 +170,10 @@ __device__ __forceinline__ InstHot load_hot(const InstDesc* __restrict__ I)
 //   SrcGlobal: from the descriptor table in global memory (any batch size);
 //   SrcOne:    every item belongs to instance 0, whose descriptor is the
 //              parameter;
-//   SrcTable:  up to kTableInsts instances, the consumers' fields of each in
-//              the parameter (the producer still reads col / scol, and the
-//              rare path the law, from the global table).
+//   SrcTable:  up to kTableInsts instances, the fields the step loop reads
+//              (positions, law constants) of each in the parameter; the
+//              per-slice fields, the producer's col / scol and the rare
+//              path's law come from the global table.
 struct SrcGlobal {
     int unused;
 };
@@ -181,14 +182,10 @@ struct SrcOne {
 };
 struct HotEntry {
     const float4* pos;
-    const uint32_t* row_off;
-    const uint32_t* slice_off;
-    float4* force;
-    int64_t n;
     HotLaw H;
     float pad;
 };
-constexpr int kTableInsts = 512;  // 512 x 56 B stays inside the 32 KB of kernel parameters
+constexpr int kTableInsts = 1024;  // 1024 x 24 B stays inside the 32 KB of kernel parameters
 struct SrcTable {
     HotEntry h[kTableInsts];
 };
@@ -196,13 +193,14 @@ struct SrcTable {
 __device__ __forceinline__ InstHot hot_from(const SrcTable& t, const InstDesc* insts, int inst)
 {
     const HotEntry& e = t.h[inst];
+    const InstDesc* __restrict__ I = insts + inst;
     InstHot h;
     h.pos = e.pos;
-    h.row_off = e.row_off;
-    h.slice_off = e.slice_off;
-    h.force = e.force;
-    h.cold = &insts[inst].law;
-    h.n = e.n;
+    h.row_off = I->row_off;
+    h.slice_off = I->slice_off;
+    h.force = I->force;
+    h.cold = &I->law;
+    h.n = I->n;
     h.H = e.H;
     return h;
 }
@@ -611,8 +609,7 @@ cudaError_t launch_tiled_g(const TiledShape& shape, const InstDesc* d_insts,
         static thread_local SrcTable t;  // 28 KB: kept off the stack
         for (int k = 0; k < num_insts; k++) {
             const InstDesc& d = host_insts[k];
-            t.h[k] = HotEntry{d.pos, d.row_off, d.slice_off, d.force, d.n,
-                              HotLaw{d.law.half2, d.law.rc2, d.law.band}, 0.f};
+            t.h[k] = HotEntry{d.pos, HotLaw{d.law.half2, d.law.rc2, d.law.band}, 0.f};
         }
         return launch_tiled_src<PERIODIC, G>(shape, d_insts, d_items, num_items, d_queue, grid,
                                              d_status, s, t);
