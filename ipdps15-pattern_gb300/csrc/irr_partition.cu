@@ -630,22 +630,29 @@ cudaError_t alloc_async(T** p, int64_t count, cudaStream_t s)
 // ------------------------------------------------------- sliced layout
 // words[q] = 64 * ceil(longest row of slice q / 2G); *total += words[q] (64-bit,
 // so an overflowing layout is seen by the host before the 32-bit scan is used).
+// Whole warps walk the slices, so the total is summed over the warp first
+// (one atomic per warp instead of one per slice on a single address).
 __global__ void slice_words_kernel(const uint32_t* row_off, int64_t n, int G, int64_t slices,
                                    uint32_t* words, unsigned long long* total)
 {
     const int R = 32 / G;
-    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < slices;
-         q += (int64_t)gridDim.x * blockDim.x) {
-        uint32_t longest = 0;
-        const int64_t r0 = q * R;
-        const int64_t r1 = r0 + R < n ? r0 + R : n;
-        for (int64_t r = r0; r < r1; r++) {
-            const uint32_t len = row_off[r + 1] - row_off[r];
-            longest = len > longest ? len : longest;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t q0 = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); q0 < slices; q0 += stride) {
+        const int64_t q = q0 + (threadIdx.x & 31);
+        unsigned long long w = 0;
+        if (q < slices) {
+            uint32_t longest = 0;
+            const int64_t r0 = q * R;
+            const int64_t r1 = r0 + R < n ? r0 + R : n;
+            for (int64_t r = r0; r < r1; r++) {
+                const uint32_t len = row_off[r + 1] - row_off[r];
+                longest = len > longest ? len : longest;
+            }
+            w = 64ull * ((longest + 2ull * G - 1) / (2ull * G));
+            words[q] = (uint32_t)w;
         }
-        const unsigned long long w = 64ull * ((longest + 2ull * G - 1) / (2ull * G));
-        words[q] = (uint32_t)w;
-        atomicAdd(total, w);
+        for (int off = 16; off > 0; off >>= 1) w += __shfl_xor_sync(0xffffffffu, w, off);
+        if ((threadIdx.x & 31) == 0 && w) atomicAdd(total, w);
     }
 }
 
