@@ -200,12 +200,16 @@ __global__ void pairs_half_kernel(const float4* __restrict__ pos_c, const int32_
     }
 }
 
+// One warp per row: the lanes write consecutive pairs (coalesced stores).
 __global__ void expand_pairs_kernel(const uint32_t* row_off, const int32_t* nbr, int64_t n,
                                     int2* edges)
 {
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-         i += (int64_t)gridDim.x * blockDim.x)
-        for (uint32_t k = row_off[i]; k < row_off[i + 1]; k++) edges[k] = make_int2((int)i, nbr[k]);
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
+        const uint32_t k1 = row_off[i + 1];
+        for (uint32_t k = row_off[i] + lane; k < k1; k += 32) edges[k] = make_int2((int)i, nbr[k]);
+    }
 }
 
 int grid_of(int64_t n)
@@ -324,7 +328,7 @@ cudaError_t build_neighbor_list(const float4* pos, int64_t n, float box, float c
                                                           cnt, nbr, nullptr, sort_here);
             IRR_CUDA_TRY(cudaGetLastError());
             if (!sort_here) IRR_CUDA_TRY(launch_row_sort(cnt, n, nbr, s));
-            expand_pairs_kernel<<<grid_of(n), 256, 0, s>>>(cnt, nbr, n, edges);
+            expand_pairs_kernel<<<grid_of(32 * n), 256, 0, s>>>(cnt, nbr, n, edges);
             IRR_CUDA_TRY(cudaGetLastError());
             IRR_CUDA_TRY(cudaFreeAsync(nbr, s));
         } else if (half) {
