@@ -188,7 +188,9 @@ IRR_API int irr_set_edges_device(irr_handle *h, const int32_t *d_edges, int64_t 
  * 436-439) on later calls: num_nodes records of elm_size bytes (enum
  * irr_node_format), host memory, in the caller's node order.  Positions are
  * used in float; the first three components are the coordinates.  Changing
- * num_nodes after irr_init is IRR_ERR_STATE. */
+ * num_nodes after irr_init is IRR_ERR_STATE.  After irr_init, page-locked host
+ * memory on a 16-byte boundary is read in place, asynchronously: leave it
+ * unchanged until the next irr_get_result or irr_sync returns. */
 IRR_API int irr_set_nodes(irr_handle *h, const void *node_data, int elm_size, int64_t num_nodes);
 /* Same, from device memory. */
 IRR_API int irr_set_nodes_device(irr_handle *h, const void *d_node_data, int elm_size,
