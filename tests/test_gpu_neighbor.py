@@ -63,6 +63,19 @@ def test_known_answer_minimd(built_lib, oracle_lib):
     d.close()
 
 
+def test_known_answer_minimd_periodic(built_lib, oracle_lib):
+    """The same lattice with periodic images: every atom has the 78 lattice
+    neighbours of the first five FCC shells inside 2.8 (the sixth is at
+    2.91), so the half list holds 39 per atom: 19,500,000."""
+    import irregular_gb300 as irr
+    O = oracle_lib
+    pos32 = O.fcc_minimd(50, 50, 50, 0.8442).astype(np.float32)
+    side = float(np.float32(50 * (4 / 0.8442) ** (1 / 3)))
+    d = irr.neighbor_build(pos32, side, 2.8 * 2.8)
+    assert d.count == 19500000
+    d.close()
+
+
 def test_known_answer_moldyn(built_lib, oracle_lib):
     """moldyn: FCC 4*64^3, side (N/0.83134)^0.3333333, list cutoff 3.5*1.2,
     periodic (moldyn/moldyn.h:20, moldyn/irresult/2:5)."""

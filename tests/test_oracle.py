@@ -75,6 +75,15 @@ def test_known_answer_minimd_neighbor_count(oracle_lib):
     assert O.neighbor_count(pos, 0.0, np.float32(2.8 * 2.8)) == 18816288
 
 
+def test_known_answer_minimd_periodic_neighbor_count(oracle_lib):
+    """miniMD's lattice with periodic images: 78 neighbours per atom inside
+    2.8 (FCC shells 1-5; shell 6 is at 2.91), 39 per atom in the half list."""
+    O = oracle_lib
+    pos = O.fcc_minimd(50, 50, 50, 0.8442).astype(np.float32)
+    side = float(np.float32(50 * (4 / 0.8442) ** (1 / 3)))
+    assert O.neighbor_count(pos, side, np.float32(2.8 * 2.8)) == 19500000
+
+
 @pytest.mark.slow
 def test_known_answer_moldyn_neighbor_count(oracle_lib):
     """moldyn: FCC 4*64^3, side (N/0.83134)^0.3333333, list cutoff 3.5*1.2 periodic
