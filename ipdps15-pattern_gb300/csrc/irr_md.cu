@@ -97,6 +97,13 @@ __global__ void gather3_kernel(const double* __restrict__ src, const int32_t* __
     }
 }
 
+__global__ void iota_ids_kernel(int32_t* __restrict__ ids, int64_t n)
+{
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * blockDim.x)
+        ids[k] = (int32_t)k;
+}
+
 __global__ void gather_ids_kernel(const int32_t* __restrict__ src, const int32_t* __restrict__ perm,
                                   int64_t n, int32_t* __restrict__ dst)
 {
@@ -467,14 +474,11 @@ int irr_md_create(const irr_md_config* cfg, const double* pos, const double* vel
         irr_md_destroy(m);
         return e == cudaErrorMemoryAllocation ? IRR_ERR_NOMEM : IRR_ERR_CUDA;
     }
-    std::vector<int32_t> iota((size_t)n);
-    for (int64_t i = 0; i < n; i++) iota[(size_t)i] = (int32_t)i;
-    e = cudaMemcpy(m->ids, iota.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) {
-        // wrap the initial positions and make their float copy
-        to_float4_kernel<<<grid_of(n), 256, 0, m->stream>>>(m->x, n, cfg->side, m->pos4);
-        e = cudaGetLastError();
-    }
+    // execution slot k holds atom k until the first partition; then wrap the
+    // initial positions and make their float copy
+    iota_ids_kernel<<<grid_of(n), 256, 0, m->stream>>>(m->ids, n);
+    to_float4_kernel<<<grid_of(n), 256, 0, m->stream>>>(m->x, n, cfg->side, m->pos4);
+    e = cudaGetLastError();
     if (e != cudaSuccess) {
         irr_md_destroy(m);
         return IRR_ERR_CUDA;

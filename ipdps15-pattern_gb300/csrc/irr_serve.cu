@@ -20,6 +20,7 @@
 #include <atomic>
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <numeric>
@@ -40,6 +41,41 @@ struct JobSpec {
     uint64_t seed;
     double side;
     size_t est_bytes;
+};
+
+// A request's initial state (3n positions, 3n velocities), in page-locked
+// host memory when the driver grants it, else in ordinary memory.
+struct Payload {
+    double* pos = nullptr;
+    double* vel = nullptr;
+    bool locked = false;
+    void fill(const std::vector<double>& p, const std::vector<double>& v)
+    {
+        const size_t bytes = sizeof(double) * p.size();
+        locked = cudaHostAlloc((void**)&pos, bytes, cudaHostAllocDefault) == cudaSuccess &&
+                 cudaHostAlloc((void**)&vel, bytes, cudaHostAllocDefault) == cudaSuccess;
+        if (!locked) {
+            cudaGetLastError();
+            if (pos) cudaFreeHost(pos);
+            pos = static_cast<double*>(malloc(bytes));
+            vel = static_cast<double*>(malloc(bytes));
+        }
+        if (pos && vel) {
+            memcpy(pos, p.data(), bytes);
+            memcpy(vel, v.data(), bytes);
+        }
+    }
+    void release()
+    {
+        if (locked) {
+            if (pos) cudaFreeHost(pos);
+            if (vel) cudaFreeHost(vel);
+        } else {
+            free(pos);
+            free(vel);
+        }
+        pos = vel = nullptr;
+    }
 };
 
 struct Live {
@@ -434,17 +470,22 @@ int irr_serve_run(const irr_serve_config* cfg, irr_serve_stats* st, irr_serve_jo
     // Each request carries its initial state (FCC lattice, jitter, Maxwell
     // velocities): made before the serving clock starts, on all host cores,
     // so the loop times admission, upload and the GPU work, not the host RNG.
-    std::vector<std::vector<double>> req_pos(jobs.size()), req_vel(jobs.size());
+    // A request's payload arrives in page-locked host memory, as a server's
+    // receive buffers would be, so its upload runs at the host link's speed.
+    std::vector<Payload> req(jobs.size());
     {
         unsigned nth = std::thread::hardware_concurrency();
         nth = std::max(1u, std::min(nth, 64u));
         std::vector<std::thread> pool;
         for (unsigned t = 0; t < nth; t++)
             pool.emplace_back([&, t]() {
+                cudaSetDevice(cfg->device);
+                std::vector<double> pos, vel;
                 for (size_t q = t; q < order.size(); q += nth) {
                     const int k = order[q];
-                    if ((double)jobs[k].est_bytes <= cfg->budget_bytes)
-                        initial_state(jobs[k], cfg, req_pos[k], req_vel[k]);
+                    if ((double)jobs[k].est_bytes > cfg->budget_bytes) continue;
+                    initial_state(jobs[k], cfg, pos, vel);
+                    req[k].fill(pos, vel);
                 }
             });
         for (auto& th : pool) th.join();
@@ -507,9 +548,7 @@ int irr_serve_run(const irr_serve_config* cfg, irr_serve_stats* st, irr_serve_jo
                 mc.skin = cfg->skin;
                 mc.side = j.side;
                 mc.rebuild_every = cfg->rebuild_every;
-                made_rc[i] = irr_md_create(&mc, req_pos[id].data(), req_vel[id].data(), j.atoms, &made[i]);
-                std::vector<double>().swap(req_pos[id]);  // uploaded: release the host copy
-                std::vector<double>().swap(req_vel[id]);
+                made_rc[i] = irr_md_create(&mc, req[id].pos, req[id].vel, j.atoms, &made[i]);
             });
             for (size_t i = 0; i < admit.size(); i++) {
                 if (made_rc[i] != IRR_OK) {
@@ -610,6 +649,7 @@ int irr_serve_run(const irr_serve_config* cfg, irr_serve_stats* st, irr_serve_jo
         }
     }
     const double makespan = now();
+    for (auto& r : req) r.release();
     for (auto& L : live) irr_md_destroy(L.md);
     if (ev_kd) cudaEventDestroy(ev_kd);
     int dev_status = 0;
