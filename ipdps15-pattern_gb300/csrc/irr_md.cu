@@ -547,13 +547,13 @@ int irr_md_energy(irr_md* m, double* kinetic, double* potential, double* virial)
     energy_final_kernel<<<1, 32, 0, m->stream>>>(part, blocks, m->d_acc);
     MD_CUDA(m, cudaGetLastError(), "energy kernels");
     double h[4];
+    int st = 0;
     MD_CUDA(m, cudaMemcpyAsync(h, m->d_acc, sizeof(h), cudaMemcpyDeviceToHost, m->stream), "energy");
+    MD_CUDA(m, cudaMemcpyAsync(&st, m->d_status, sizeof(int), cudaMemcpyDeviceToHost, m->stream), "status");
     MD_CUDA(m, cudaStreamSynchronize(m->stream), "energy");
     if (kinetic) *kinetic = h[0];
     if (potential) *potential = h[1];
     if (virial) *virial = h[2];
-    int st = 0;
-    MD_CUDA(m, cudaMemcpy(&st, m->d_status, sizeof(int), cudaMemcpyDeviceToHost), "status");
     if (st) return md_fail(m, IRR_ERR_DEVICE, "device status set (a bounded wait gave up)");
     return IRR_OK;
 }
