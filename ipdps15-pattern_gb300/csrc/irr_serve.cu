@@ -6,11 +6,12 @@
 //   * admits arrived jobs in arrival order while their estimated device memory
 //     fits the budget (their state then stays resident until they finish);
 //   * every tick advances each resident job by one step: ONE kick/drift launch
-//     over all resident jobs; the rebuilds that are due start on worker
-//     threads while the other jobs' forces (one batched launch over their
-//     (instance, node block) work items, gathered on the device from each
-//     job's own table) and kicks (one launch) are queued; then the same two
-//     launches for the rebuilt jobs;
+//     over all resident jobs (with the previous step's closing kick folded in
+//     for the jobs that did not retire); the rebuilds that are due start on
+//     worker threads while the other jobs' forces (one batched launch over
+//     their (instance, node block) work items, gathered on the device from
+//     each job's own table) are queued; then the rebuilt jobs' forces; the
+//     jobs that finish get their closing kick at once;
 //   * retires finished jobs (their memory frees up for waiting arrivals).
 // A job's rows are computed by the same kernel code whatever else shares the
 // launch, so its trajectory is bitwise the same alone and in the mix.
@@ -84,6 +85,7 @@ struct Live {
     int steps;
     double admit_s;
     double pair_evals;
+    bool kick_pending;  // the last step's closing kick is left to the next kick-drift
 };
 
 // One resident job in a tick's device tables.  Its atoms occupy whole
@@ -100,7 +102,7 @@ struct TickJob {
     int32_t block0;
     int32_t item0;
     int32_t num_items;
-    int32_t pad;
+    int32_t kicks;  // kick-drift: 2 when the job's previous closing kick is folded in
 };
 constexpr int kTickThreads = 256;
 
@@ -117,14 +119,19 @@ __device__ __forceinline__ int find_job(int njobs, int64_t x, Start start)
     return lo;
 }
 
-template <int KICKS>
+// Each job's kick-drift; a job that did not retire last tick had its closing
+// kick left to this pass (kicks == 2, the same roundings as a separate kick).
 __global__ void __launch_bounds__(kTickThreads) tick_kick_drift_kernel(const TickJob* __restrict__ jobs,
                                                                        int njobs, double dt)
 {
     const int k = find_job(njobs, blockIdx.x, [&](int j) { return (int64_t)jobs[j].block0; });
     const TickJob& J = jobs[k];
     const int64_t i = (int64_t)(blockIdx.x - J.block0) * kTickThreads + threadIdx.x;
-    if (i < J.n) md_kick_drift_atom<KICKS>(J.x, J.v, J.force, i, dt, J.side, J.pos4);
+    if (i >= J.n) return;
+    if (J.kicks == 2)
+        md_kick_drift_atom<2>(J.x, J.v, J.force, i, dt, J.side, J.pos4);
+    else
+        md_kick_drift_atom<1>(J.x, J.v, J.force, i, dt, J.side, J.pos4);
 }
 
 __global__ void __launch_bounds__(kTickThreads) tick_kick_kernel(const TickJob* __restrict__ jobs,
@@ -180,10 +187,11 @@ struct Pinned {
 };
 
 // Fills the job table for the jobs ms (their current arrays: a rebuild swaps a
-// job's state buffers) and uploads it on s; returns the launch's block count
-// and the batch's item count.
+// job's state buffers; kicks[k] for the kick-drift, 1 if none given) and
+// uploads it on s; returns the launch's block count and the batch's item
+// count.
 bool upload_tick_jobs(const std::vector<irr_md*>& ms, Pinned<TickJob>& T, cudaStream_t s,
-                      int* blocks, int64_t* items)
+                      int* blocks, int64_t* items, const std::vector<int>* kicks = nullptr)
 {
     if (!T.reserve(ms.size())) return false;
     int64_t b = 0, it = 0;
@@ -200,7 +208,7 @@ bool upload_tick_jobs(const std::vector<irr_md*>& ms, Pinned<TickJob>& T, cudaSt
         J.block0 = (int32_t)b;
         J.item0 = (int32_t)it;
         J.num_items = m->num_items;
-        J.pad = 0;
+        J.kicks = kicks ? (*kicks)[k] : 1;
         b += (m->n + kTickThreads - 1) / kTickThreads;
         it += m->num_items;
     }
@@ -214,12 +222,14 @@ bool upload_tick_jobs(const std::vector<irr_md*>& ms, Pinned<TickJob>& T, cudaSt
 // The device tables of one force launch of a tick.
 struct ForceBatch {
     Pinned<TickJob> jobs;
+    Pinned<TickJob> closing;  // the jobs that retire this tick (their closing kick)
     Pinned<InstDesc> insts;
     WorkItem* d_items = nullptr;
     size_t items_cap = 0;
     void release()
     {
         jobs.release();
+        closing.release();
         insts.release();
         if (d_items) cudaFree(d_items);
         d_items = nullptr;
@@ -228,10 +238,12 @@ struct ForceBatch {
 };
 
 // The forces of the jobs ms (one persistent launch over their work items,
-// gathered on the device from each job's own table) and their closing kick
-// (one launch), queued on s.
-int force_and_kick(const std::vector<irr_md*>& ms, ForceBatch& B, const TiledShape& shape,
-                   int* d_queue, int* d_status, int sms, double dt, cudaStream_t s)
+// gathered on the device from each job's own table) and the closing kick of
+// those that retire after this step (one launch over them; the others' kicks
+// are folded into the next tick's kick-drift), queued on s.
+int force_and_kick(const std::vector<irr_md*>& ms, const std::vector<irr_md*>& retiring,
+                   ForceBatch& B, const TiledShape& shape, int* d_queue, int* d_status, int sms,
+                   double dt, cudaStream_t s)
 {
     if (ms.empty()) return IRR_OK;
     int blocks = 0;
@@ -260,7 +272,11 @@ int force_and_kick(const std::vector<irr_md*>& ms, ForceBatch& B, const TiledSha
         launch_tiled(shape, B.insts.d, B.d_items, (int)nitems, d_queue, sms * kCtasPerSm, d_status, s,
                      B.insts.h, (int)ms.size()) != cudaSuccess)
         return IRR_ERR_CUDA;
-    tick_kick_kernel<<<blocks, kTickThreads, 0, s>>>(B.jobs.d, (int)ms.size(), dt);
+    if (retiring.empty()) return IRR_OK;
+    int kblocks = 0;
+    int64_t unused = 0;
+    if (!upload_tick_jobs(retiring, B.closing, s, &kblocks, &unused)) return IRR_ERR_CUDA;
+    tick_kick_kernel<<<kblocks, kTickThreads, 0, s>>>(B.closing.d, (int)retiring.size(), dt);
     return cudaGetLastError() == cudaSuccess ? IRR_OK : IRR_ERR_CUDA;
 }
 
@@ -556,7 +572,7 @@ int irr_serve_run(const irr_serve_config* cfg, irr_serve_stats* st, irr_serve_jo
                     continue;
                 }
                 made[i]->stream = s;
-                live.push_back(Live{admit[i], made[i], 0, now(), 0.0});
+                live.push_back(Live{admit[i], made[i], 0, now(), 0.0, false});
             }
             st->max_resident = std::max<int64_t>(st->max_resident, (int64_t)live.size());
             admit.clear();
@@ -570,17 +586,25 @@ int irr_serve_run(const irr_serve_config* cfg, irr_serve_stats* st, irr_serve_jo
             continue;
         }
         // one tick: every resident job advances one step
-        std::vector<irr_md*> all, keep, due;
-        for (auto& L : live) all.push_back(L.md);
+        std::vector<irr_md*> all, keep, due, keep_retiring, due_retiring;
+        std::vector<int> kicks;
+        for (auto& L : live) {
+            all.push_back(L.md);
+            kicks.push_back(L.kick_pending ? 2 : 1);
+            if (L.kick_pending) L.md->steps++;  // the bookkeeping of md_kick
+            L.kick_pending = false;
+        }
         int blocks = 0;
         int64_t nitems = 0;
-        if (!upload_tick_jobs(all, tick_a, s, &blocks, &nitems)) { rc = IRR_ERR_CUDA; break; }
-        tick_kick_drift_kernel<1><<<blocks, kTickThreads, 0, s>>>(tick_a.d, (int)all.size(), cfg->dt);
+        if (!upload_tick_jobs(all, tick_a, s, &blocks, &nitems, &kicks)) { rc = IRR_ERR_CUDA; break; }
+        tick_kick_drift_kernel<<<blocks, kTickThreads, 0, s>>>(tick_a.d, (int)all.size(), cfg->dt);
         if (cudaGetLastError() != cudaSuccess) { rc = IRR_ERR_CUDA; break; }
         for (size_t k = 0; k < live.size(); k++) {
             irr_md* m = live[k].md;
             m->since_rebuild++;  // the bookkeeping of md_kick_drift
-            (m->since_rebuild >= m->cfg.rebuild_every ? due : keep).push_back(m);
+            const bool d = m->since_rebuild >= m->cfg.rebuild_every;
+            (d ? due : keep).push_back(m);
+            if (live[k].steps + 1 >= cfg->steps_per_job) (d ? due_retiring : keep_retiring).push_back(m);
         }
         // the rebuilds that are due start on worker threads, each on its
         // job's own stream after this tick's kick-drift, while this thread
@@ -595,18 +619,21 @@ int irr_serve_run(const irr_serve_config* cfg, irr_serve_stats* st, irr_serve_jo
             due_rc[i] = md_rebuild(m);
             m->stream = s;
         });
-        const int krc = force_and_kick(keep, keep_b, shape, d_queue, d_status, sms, cfg->dt, s);
+        const int krc = force_and_kick(keep, keep_retiring, keep_b, shape, d_queue, d_status, sms, cfg->dt, s);
         for (auto& th : rebuilding) th.join();
         if (krc != IRR_OK) rc = krc;
         for (int r : due_rc)
             if (r != IRR_OK && rc == IRR_OK) rc = r;
         if (rc) break;
-        rc = force_and_kick(due, due_b, shape, d_queue, d_status, sms, cfg->dt, s);
+        rc = force_and_kick(due, due_retiring, due_b, shape, d_queue, d_status, sms, cfg->dt, s);
         if (rc) break;
         for (auto& L : live) {
             L.pair_evals += (double)L.md->edges;
-            L.md->steps++;  // the bookkeeping of md_kick
             L.steps++;
+            if (L.steps >= cfg->steps_per_job)
+                L.md->steps++;  // kicked this tick (the bookkeeping of md_kick)
+            else
+                L.kick_pending = true;
         }
         // the host copies of the tables are reused next tick: wait for this one
         if (cudaStreamSynchronize(s) != cudaSuccess) { rc = IRR_ERR_CUDA; break; }
