@@ -79,6 +79,16 @@ struct Payload {
     }
 };
 
+// A job being set up (upload, first neighbour build, partition and forces)
+// on a worker thread while the resident jobs keep stepping.
+struct Admission {
+    int id = 0;
+    irr_md* made = nullptr;
+    int rc = IRR_OK;
+    std::atomic<bool> done{false};
+    std::thread worker;
+};
+
 struct Live {
     int id;
     irr_md* md;
@@ -508,14 +518,35 @@ int irr_serve_run(const irr_serve_config* cfg, irr_serve_stats* st, irr_serve_jo
     }
     const auto t0 = std::chrono::steady_clock::now();
     auto now = [&]() { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); };
-    std::vector<int> admit;
     const unsigned workers = cfg->mode == IRR_SERVE_SERIAL
                                  ? 1u
                                  : std::max(1u, std::min(std::thread::hardware_concurrency(), 16u));
     cudaEvent_t ev_kd = nullptr;
     cudaEventCreateWithFlags(&ev_kd, cudaEventDisableTiming);
     std::vector<int> waiting;  // arrived, not yet admitted, in arrival order
-    while (rc == IRR_OK && (next < order.size() || !waiting.empty() || !live.empty())) {
+    std::vector<std::unique_ptr<Admission>> creating;
+    auto harvest = [&]() {  // jobs whose set-up has finished join the resident set
+        for (size_t i = 0; i < creating.size();) {
+            Admission& a = *creating[i];
+            if (!a.done.load(std::memory_order_acquire)) {
+                i++;
+                continue;
+            }
+            a.worker.join();
+            if (a.rc != IRR_OK) {
+                if (rc == IRR_OK) rc = a.rc;
+            } else {
+                a.made->stream = s;
+                live.push_back(Live{a.id, a.made, 0, now(), 0.0, false});
+            }
+            creating.erase(creating.begin() + (std::ptrdiff_t)i);
+        }
+        st->max_resident = std::max<int64_t>(st->max_resident, (int64_t)live.size());
+    };
+    while (rc == IRR_OK &&
+           (next < order.size() || !waiting.empty() || !creating.empty() || !live.empty())) {
+        harvest();
+        if (rc) break;
         // arrivals (a job larger than the whole budget is rejected)
         while (next < order.size() && jobs[order[next]].arrival <= now()) {
             const int k = order[next++];
@@ -537,49 +568,42 @@ int irr_serve_run(const irr_serve_config* cfg, irr_serve_stats* st, irr_serve_jo
         if (cfg->policy == IRR_SERVE_SJF)
             std::stable_sort(waiting.begin(), waiting.end(),
                              [&](int a, int b) { return jobs[a].atoms < jobs[b].atoms; });
+        // an admitted job's set-up (upload, first neighbour build, partition,
+        // forces) runs on a worker thread on its own stream -- at most
+        // `workers` at a time -- while the resident jobs keep stepping; it
+        // joins them at the first tick after its set-up has finished
         size_t taken = 0;
-        while (taken < waiting.size()) {
+        while (taken < waiting.size() && creating.size() < workers) {
             const JobSpec& j = jobs[waiting[taken]];
-            if ((int)(live.size() + admit.size()) >= max_res ||
+            if ((int)(live.size() + creating.size()) >= max_res ||
                 used + (double)j.est_bytes > cfg->budget_bytes)
                 break;
-            admit.push_back(waiting[taken++]);
+            const int id = waiting[taken++];
             used += (double)j.est_bytes;
             peak = std::max(peak, used);
-        }
-        waiting.erase(waiting.begin(), waiting.begin() + (std::ptrdiff_t)taken);
-        if (!admit.empty()) {
-            // the admitted jobs' set-up (upload + first neighbour build and
-            // partition) runs concurrently, each on its own stream
-            std::vector<irr_md*> made(admit.size(), nullptr);
-            std::vector<int> made_rc(admit.size(), IRR_OK);
-            run_parallel(admit.size(), workers, cfg->device, [&](size_t i) {
-                const int id = admit[i];
-                const JobSpec& j = jobs[id];
+            creating.push_back(std::make_unique<Admission>());
+            Admission* a = creating.back().get();
+            a->id = id;
+            a->worker = std::thread([a, &jobs, &req, cfg]() {
+                cudaSetDevice(cfg->device);
+                const JobSpec& js = jobs[a->id];
                 irr_md_config mc;
                 irr_md_config_default(&mc);
                 mc.device = cfg->device;
                 mc.dt = cfg->dt;
                 mc.cutforce = cfg->cutforce;
                 mc.skin = cfg->skin;
-                mc.side = j.side;
+                mc.side = js.side;
                 mc.rebuild_every = cfg->rebuild_every;
-                made_rc[i] = irr_md_create(&mc, req[id].pos, req[id].vel, j.atoms, &made[i]);
+                a->rc = irr_md_create(&mc, req[a->id].pos, req[a->id].vel, js.atoms, &a->made);
+                a->done.store(true, std::memory_order_release);
             });
-            for (size_t i = 0; i < admit.size(); i++) {
-                if (made_rc[i] != IRR_OK) {
-                    if (rc == IRR_OK) rc = made_rc[i];
-                    continue;
-                }
-                made[i]->stream = s;
-                live.push_back(Live{admit[i], made[i], 0, now(), 0.0, false});
-            }
-            st->max_resident = std::max<int64_t>(st->max_resident, (int64_t)live.size());
-            admit.clear();
         }
-        if (rc) break;
+        waiting.erase(waiting.begin(), waiting.begin() + (std::ptrdiff_t)taken);
         if (live.empty()) {
-            if (next < order.size()) {
+            if (!creating.empty()) {
+                std::this_thread::sleep_for(std::chrono::microseconds(50));
+            } else if (next < order.size()) {
                 const double wait = jobs[order[next]].arrival - now();
                 if (wait > 0) std::this_thread::sleep_for(std::chrono::duration<double>(std::min(wait, 0.01)));
             }
@@ -676,6 +700,10 @@ int irr_serve_run(const irr_serve_config* cfg, irr_serve_stats* st, irr_serve_jo
         }
     }
     const double makespan = now();
+    for (auto& a : creating) {  // set-ups still running after an error
+        if (a->worker.joinable()) a->worker.join();
+        if (a->made) irr_md_destroy(a->made);
+    }
     for (auto& r : req) r.release();
     for (auto& L : live) irr_md_destroy(L.md);
     if (ev_kd) cudaEventDestroy(ev_kd);
