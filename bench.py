@@ -509,6 +509,10 @@ def run_served(args):
     out = {"leg": "served", "jobs": args.jobs, "arrival_rate_per_s": 200.0,
            "steps_per_job": 50, "budget_GB": 120.0,
            "data": "synthetic (seeded arrivals and sizes; FCC + jitter, Maxwell velocities)"}
+    # untimed warm-up: a long-running server has its memory pool grown and its
+    # kernels loaded; without it the first measured schedule would pay for both
+    irr.serve(num_jobs=max(1, args.jobs // 4), mode=irr.IRR_SERVE_CONTINUOUS, arrival_rate=200.0,
+              steps_per_job=50, budget_bytes=120e9, seed=SEED + 6)
     runs = ((irr.IRR_SERVE_CONTINUOUS, irr.IRR_SERVE_FIFO, "continuous"),
             (irr.IRR_SERVE_SERIAL, irr.IRR_SERVE_FIFO, "serial"),
             (irr.IRR_SERVE_CONTINUOUS, irr.IRR_SERVE_SJF, "continuous_sjf"))
