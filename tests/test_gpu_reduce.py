@@ -452,3 +452,32 @@ def test_larger_random_periodic_properties(built_lib, oracle_lib, n):
         tot = np.abs(out[exec_mode].astype(np.float64).sum(axis=0))
         assert np.all(tot <= 1e-6 * sabs.sum(axis=0))
     assert scaled_error(out[0], out[1], sabs) <= 2 * TOL_PERNODE_F64
+
+
+@pytest.mark.parametrize("layout", [1, 2])
+def test_row_longer_than_a_stage(built_lib, oracle_lib, layout):
+    """A hub row of 5999 entries, more than a shared-memory stage holds (5104):
+    its work item is read from global memory while the others are staged; CSR
+    (1) and sliced (2) layouts both stay on the FP64 oracle."""
+    import irregular_gb300 as irr
+    O = oracle_lib
+    n = 6000
+    rho = 32.0 / (4.0 / 3.0 * np.pi * 2.5 ** 3)
+    pos32, L = random_box(n, rho, 20260011)
+    near = O.neighbor_half_list(pos32, float(L), np.float32(2.5 * 2.5))
+    hub = 123
+    star = np.stack([np.full(n - 1, hub, np.int32), np.delete(np.arange(n, dtype=np.int32), hub)], axis=1)
+    edges = np.concatenate([near, star]).astype(np.int32)
+    pos = pos32.astype(np.float64)
+    p = O.lj_param(6.25, float(L), True)
+    f64, sabs = O.lj_reduce_f64(pos, edges, p)
+    h = irr.Handle(irr.default_config(map_idx=0, exec=1, layout=layout))
+    h.set_params(irr.moldyn_params(float(L), 2.5))
+    h.set_edges(edges)
+    h.set_nodes(pos, 24)
+    h.step()
+    f = h.get_result(elm_size=12)
+    assert h.info().layout == layout
+    assert normwise_error(f, f64) <= TOL_NORMWISE_F64
+    assert scaled_error(f, f64, sabs) <= TOL_PERNODE_F64
+    h.close()
