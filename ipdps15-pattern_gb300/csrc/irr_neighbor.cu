@@ -35,6 +35,7 @@ struct Grid {
     double inv[3];    // 1 / cell size
     float box, hb, cut2;
     int periodic;
+    int fast;         // periodic with >= 5 cells per axis: image decided by the cell
 };
 
 __device__ __forceinline__ bool list_pair(float4 a, float4 b, const Grid& g)
@@ -54,6 +55,45 @@ __device__ __forceinline__ bool list_pair(float4 a, float4 b, const Grid& g)
     return r2 <= g.cut2;
 }
 
+// The same rule when the neighbour cell decides the image: with at least 5
+// cells per axis and every position in [0, box), a partner in a cell that is
+// adjacent without wrapping is less than 2/5 of the box away on that axis
+// (the rule keeps d), and one in a cell reached across the boundary more
+// than 3/5 (the rule adds or subtracts the box, always the same way), so the
+// cell's shift s (0 or +-box) is added instead of compared for.  d + 0 is d
+// except for d = -0, whose square is the same.
+__device__ __forceinline__ bool list_pair_shifted(float4 a, float4 b, float sx, float sy, float sz,
+                                                  float cut2)
+{
+    const float dx = __fadd_rn(__fsub_rn(a.x, b.x), sx);
+    const float dy = __fadd_rn(__fsub_rn(a.y, b.y), sy);
+    const float dz = __fadd_rn(__fsub_rn(a.z, b.z), sz);
+    const float r2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+    return r2 <= cut2;
+}
+
+template <bool FAST>
+__device__ __forceinline__ bool pair_hit(float4 a, float4 b, const Grid& g, float sx, float sy, float sz)
+{
+    return FAST ? list_pair_shifted(a, b, sx, sy, sz, g.cut2) : list_pair(a, b, g);
+}
+
+// Neighbour cell (x, y, z) of a periodic grid wrapped into range, with the
+// image shift of each wrapped axis: a cell reached below 0 lies at the top of
+// the box (its partners are pulled down by +box), one reached past the top
+// at the bottom (-box).
+__device__ __forceinline__ void wrap_cell(int& v, int nc, float box, float& s)
+{
+    s = 0.f;
+    if (v < 0) {
+        v += nc;
+        s = box;
+    } else if (v >= nc) {
+        v -= nc;
+        s = -box;
+    }
+}
+
 __device__ __forceinline__ int cell_coord(float x, int axis, const Grid& g)
 {
     long long k = (long long)floor(((double)x - g.org[axis]) * g.inv[axis]);
@@ -63,12 +103,17 @@ __device__ __forceinline__ int cell_coord(float x, int axis, const Grid& g)
     return (int)k;
 }
 
+// Also raises *outside when a position of a periodic box lies outside
+// [0, box) (or is NaN): the cell-decided image above then does not hold.
 __global__ void cell_keys_kernel(const float4* pos, int64_t n, const __grid_constant__ Grid g, uint32_t* keys,
-                                 int32_t* vals, uint32_t* cell_count)
+                                 int32_t* vals, uint32_t* cell_count, int* outside)
 {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x) {
         const float4 p = pos[i];
+        if (g.periodic && !(p.x >= 0.f && p.x < g.box && p.y >= 0.f && p.y < g.box && p.z >= 0.f &&
+                            p.z < g.box))
+            *outside = 1;
         const uint32_t c = ((uint32_t)cell_coord(p.z, 2, g) * g.nc[1] + cell_coord(p.y, 1, g)) *
                                g.nc[0] +
                            cell_coord(p.x, 0, g);
@@ -90,13 +135,14 @@ __global__ void cell_order_kernel(const float4* __restrict__ pos, const int32_t*
 // WRITE == false: counts partners; WRITE == true: writes them from row_off[i],
 // as neighbour ids into nbr (with sort_here, sorting the row by j in place:
 // only for rows too long for the row sort that otherwise follows) or, when
-// pairs != nullptr, as the pairs (i, j) themselves.
-template <bool WRITE>
-__global__ void pairs_kernel(const float4* __restrict__ pos_c, const int32_t* __restrict__ sorted,
-                             const uint32_t* __restrict__ cell_start, int64_t n,
-                             const __grid_constant__ Grid g,
-                             uint32_t* count, const uint32_t* __restrict__ row_off, int32_t* nbr,
-                             int2* pairs, int sort_here)
+// pairs != nullptr, as the pairs (i, j) themselves.  FAST: the image decided
+// by the cell (list_pair_shifted).
+template <bool WRITE, bool FAST>
+__device__ __forceinline__ void pairs_rows(const float4* __restrict__ pos_c, const int32_t* __restrict__ sorted,
+                                           const uint32_t* __restrict__ cell_start, int64_t n,
+                                           const Grid& g, uint32_t* count,
+                                           const uint32_t* __restrict__ row_off, int32_t* nbr,
+                                           int2* pairs, int sort_here)
 {
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
          t += (int64_t)gridDim.x * blockDim.x) {
@@ -107,23 +153,30 @@ __global__ void pairs_kernel(const float4* __restrict__ pos_c, const int32_t* __
         const uint32_t base = WRITE ? row_off[i] : 0;
         for (int oz = 0; oz < g.noff[2]; oz++) {
             int z = cz + g.offs[2][oz];
-            if (g.periodic) z = (z + g.nc[2]) % g.nc[2];
+            float sz = 0.f;
+            if (FAST) wrap_cell(z, g.nc[2], g.box, sz);
+            else if (g.periodic) z = (z + g.nc[2]) % g.nc[2];
             else if (z < 0 || z >= g.nc[2]) continue;
             for (int oy = 0; oy < g.noff[1]; oy++) {
                 int y = cy + g.offs[1][oy];
-                if (g.periodic) y = (y + g.nc[1]) % g.nc[1];
+                float sy = 0.f;
+                if (FAST) wrap_cell(y, g.nc[1], g.box, sy);
+                else if (g.periodic) y = (y + g.nc[1]) % g.nc[1];
                 else if (y < 0 || y >= g.nc[1]) continue;
                 for (int ox = 0; ox < g.noff[0]; ox++) {
                     int x = cx + g.offs[0][ox];
-                    if (g.periodic) x = (x + g.nc[0]) % g.nc[0];
+                    float sx = 0.f;
+                    if (FAST) wrap_cell(x, g.nc[0], g.box, sx);
+                    else if (g.periodic) x = (x + g.nc[0]) % g.nc[0];
                     else if (x < 0 || x >= g.nc[0]) continue;
                     const uint32_t c = ((uint32_t)z * g.nc[1] + y) * g.nc[0] + x;
                     const uint32_t q1 = cell_start[c + 1];
+#pragma unroll 2
                     for (uint32_t q = cell_start[c]; q < q1; q++) {
                         const int32_t j = sorted[q];
                         const float4 b = pos_c[q];
                         if (j <= i) continue;
-                        if (list_pair(a, b, g)) {
+                        if (pair_hit<FAST>(a, b, g, sx, sy, sz)) {
                             if (WRITE) {
                                 if (pairs)
                                     pairs[base + m] = make_int2(i, j);
@@ -153,17 +206,30 @@ __global__ void pairs_kernel(const float4* __restrict__ pos_c, const int32_t* __
     }
 }
 
+template <bool WRITE>
+__global__ void pairs_kernel(const float4* __restrict__ pos_c, const int32_t* __restrict__ sorted,
+                             const uint32_t* __restrict__ cell_start, int64_t n,
+                             const __grid_constant__ Grid g, const int* __restrict__ outside,
+                             uint32_t* count, const uint32_t* __restrict__ row_off, int32_t* nbr,
+                             int2* pairs, int sort_here)
+{
+    if (g.fast && *outside == 0)
+        pairs_rows<WRITE, true>(pos_c, sorted, cell_start, n, g, count, row_off, nbr, pairs, sort_here);
+    else
+        pairs_rows<WRITE, false>(pos_c, sorted, cell_start, n, g, count, row_off, nbr, pairs, sort_here);
+}
+
 // The same pairs from a half stencil, for callers that take the pairs in any
 // order (with at least 3 cells per axis, so no cell is its own neighbour):
 // node t (in cell order) pairs with the later nodes of its own cell and with
 // the nodes of the 13 neighbour cells whose offset (dz, dy, dx) comes after
 // (0, 0, 0) in lexicographic order.  Each pair is found once and written as
 // (min id, max id).
-template <bool WRITE>
-__global__ void pairs_half_kernel(const float4* __restrict__ pos_c, const int32_t* __restrict__ sorted,
-                                  const uint32_t* __restrict__ cell_start, int64_t n,
-                                  const __grid_constant__ Grid g, uint32_t* count,
-                                  const uint32_t* __restrict__ row_off, int2* pairs)
+template <bool WRITE, bool FAST>
+__device__ __forceinline__ void half_rows(const float4* __restrict__ pos_c, const int32_t* __restrict__ sorted,
+                                          const uint32_t* __restrict__ cell_start, int64_t n,
+                                          const Grid& g, uint32_t* count,
+                                          const uint32_t* __restrict__ row_off, int2* pairs)
 {
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
          t += (int64_t)gridDim.x * blockDim.x) {
@@ -176,18 +242,20 @@ __global__ void pairs_half_kernel(const float4* __restrict__ pos_c, const int32_
             // o = 0: the own cell (later nodes only); o = 1..13: forward offsets
             const int k = o == 0 ? 13 : 13 + o;  // (dz+1)*9 + (dy+1)*3 + (dx+1)
             int z = cz + k / 9 - 1, y = cy + (k / 3) % 3 - 1, x = cx + k % 3 - 1;
+            float sx = 0.f, sy = 0.f, sz = 0.f;
             if (g.periodic) {
-                z = z < 0 ? z + g.nc[2] : (z >= g.nc[2] ? z - g.nc[2] : z);
-                y = y < 0 ? y + g.nc[1] : (y >= g.nc[1] ? y - g.nc[1] : y);
-                x = x < 0 ? x + g.nc[0] : (x >= g.nc[0] ? x - g.nc[0] : x);
+                wrap_cell(z, g.nc[2], g.box, sz);
+                wrap_cell(y, g.nc[1], g.box, sy);
+                wrap_cell(x, g.nc[0], g.box, sx);
             } else if (z < 0 || z >= g.nc[2] || y < 0 || y >= g.nc[1] || x < 0 || x >= g.nc[0]) {
                 continue;
             }
             const uint32_t c = ((uint32_t)z * g.nc[1] + y) * g.nc[0] + x;
             const uint32_t q1 = cell_start[c + 1];
+#pragma unroll 2
             for (uint32_t q = o == 0 ? (uint32_t)t + 1 : cell_start[c]; q < q1; q++) {
                 const float4 b = pos_c[q];
-                if (list_pair(a, b, g)) {
+                if (pair_hit<FAST>(a, b, g, sx, sy, sz)) {
                     if (WRITE) {
                         const int32_t j = sorted[q];
                         pairs[base + m] = i < j ? make_int2(i, j) : make_int2(j, i);
@@ -198,6 +266,18 @@ __global__ void pairs_half_kernel(const float4* __restrict__ pos_c, const int32_
         }
         if (!WRITE) count[i] = m;
     }
+}
+
+template <bool WRITE>
+__global__ void pairs_half_kernel(const float4* __restrict__ pos_c, const int32_t* __restrict__ sorted,
+                                  const uint32_t* __restrict__ cell_start, int64_t n,
+                                  const __grid_constant__ Grid g, const int* __restrict__ outside,
+                                  uint32_t* count, const uint32_t* __restrict__ row_off, int2* pairs)
+{
+    if (g.fast && *outside == 0)
+        half_rows<WRITE, true>(pos_c, sorted, cell_start, n, g, count, row_off, pairs);
+    else
+        half_rows<WRITE, false>(pos_c, sorted, cell_start, n, g, count, row_off, pairs);
 }
 
 // One warp per row: the lanes write consecutive pairs (coalesced stores).
@@ -273,6 +353,7 @@ cudaError_t build_neighbor_list(const float4* pos, int64_t n, float box, float c
             g.offs[c][0] = 0; g.noff[c] = 1;
         }
     }
+    g.fast = g.periodic && g.nc[0] >= 5 && g.nc[1] >= 5 && g.nc[2] >= 5;
     const int64_t ncell = (int64_t)g.nc[0] * g.nc[1] * g.nc[2];
     uint32_t *keys = nullptr, *keys_tmp = nullptr, *cell_start = nullptr, *cnt = nullptr;
     int32_t *sorted = nullptr, *vals_tmp = nullptr, *nbr = nullptr;
@@ -281,9 +362,12 @@ cudaError_t build_neighbor_list(const float4* pos, int64_t n, float box, float c
     IRR_CUDA_TRY(irr_malloc_async((void**)&sorted, sizeof(int32_t) * n, s));
     IRR_CUDA_TRY(irr_malloc_async((void**)&vals_tmp, sizeof(int32_t) * n, s));
     IRR_CUDA_TRY(irr_malloc_async((void**)&cell_start, sizeof(uint32_t) * (ncell + 1), s));
-    IRR_CUDA_TRY(irr_malloc_async((void**)&cnt, sizeof(uint32_t) * (n + 1), s));
+    // cnt[n + 1]: the flag that some position lies outside the box
+    IRR_CUDA_TRY(irr_malloc_async((void**)&cnt, sizeof(uint32_t) * (n + 2), s));
+    int* outside = reinterpret_cast<int*>(cnt + n + 1);
     IRR_CUDA_TRY(cudaMemsetAsync(cell_start, 0, sizeof(uint32_t) * (ncell + 1), s));
-    cell_keys_kernel<<<grid_of(n), 256, 0, s>>>(pos, n, g, keys, sorted, cell_start);
+    IRR_CUDA_TRY(cudaMemsetAsync(outside, 0, sizeof(int), s));
+    cell_keys_kernel<<<grid_of(n), 256, 0, s>>>(pos, n, g, keys, sorted, cell_start, outside);
     IRR_CUDA_TRY(cudaGetLastError());
     int bits = 1;
     while (bits < 32 && ((int64_t)1 << bits) < ncell) bits++;
@@ -296,11 +380,11 @@ cudaError_t build_neighbor_list(const float4* pos, int64_t n, float box, float c
     // rows in any order are asked for: the half stencil, where the box allows it
     const bool half = !sort_rows && g.nc[0] >= 3 && g.nc[1] >= 3 && g.nc[2] >= 3;
     if (half)
-        pairs_half_kernel<false><<<grid_of(n), 256, 0, s>>>(pos_c, sorted, cell_start, n, g, cnt,
-                                                            nullptr, nullptr);
+        pairs_half_kernel<false><<<grid_of(n), 256, 0, s>>>(pos_c, sorted, cell_start, n, g, outside,
+                                                            cnt, nullptr, nullptr);
     else
-        pairs_kernel<false><<<grid_of(n), 256, 0, s>>>(pos_c, sorted, cell_start, n, g, cnt, nullptr,
-                                                       nullptr, nullptr, 0);
+        pairs_kernel<false><<<grid_of(n), 256, 0, s>>>(pos_c, sorted, cell_start, n, g, outside, cnt,
+                                                       nullptr, nullptr, nullptr, 0);
     IRR_CUDA_TRY(cudaGetLastError());
     IRR_CUDA_TRY(cudaMemsetAsync(cnt + n, 0, sizeof(uint32_t), s));
     uint32_t* d_total = keys_tmp;  // reuse as the total's slot
@@ -324,8 +408,8 @@ cudaError_t build_neighbor_list(const float4* pos, int64_t n, float box, float c
             IRR_CUDA_TRY(max_row_len(cnt, n, &longest, s));
             const int sort_here = longest > (uint32_t)kRowSortMax;
             IRR_CUDA_TRY(irr_malloc_async((void**)&nbr, sizeof(int32_t) * total, s));
-            pairs_kernel<true><<<grid_of(n), 256, 0, s>>>(pos_c, sorted, cell_start, n, g, nullptr,
-                                                          cnt, nbr, nullptr, sort_here);
+            pairs_kernel<true><<<grid_of(n), 256, 0, s>>>(pos_c, sorted, cell_start, n, g, outside,
+                                                          nullptr, cnt, nbr, nullptr, sort_here);
             IRR_CUDA_TRY(cudaGetLastError());
             if (!sort_here) IRR_CUDA_TRY(launch_row_sort(cnt, n, nbr, s));
             expand_pairs_kernel<<<grid_of(32 * n), 256, 0, s>>>(cnt, nbr, n, edges);
@@ -333,11 +417,11 @@ cudaError_t build_neighbor_list(const float4* pos, int64_t n, float box, float c
             IRR_CUDA_TRY(cudaFreeAsync(nbr, s));
         } else if (half) {
             pairs_half_kernel<true><<<grid_of(n), 256, 0, s>>>(pos_c, sorted, cell_start, n, g,
-                                                               nullptr, cnt, edges);
+                                                               outside, nullptr, cnt, edges);
             IRR_CUDA_TRY(cudaGetLastError());
         } else {
-            pairs_kernel<true><<<grid_of(n), 256, 0, s>>>(pos_c, sorted, cell_start, n, g, nullptr,
-                                                          cnt, nullptr, edges, 0);
+            pairs_kernel<true><<<grid_of(n), 256, 0, s>>>(pos_c, sorted, cell_start, n, g, outside,
+                                                          nullptr, cnt, nullptr, edges, 0);
             IRR_CUDA_TRY(cudaGetLastError());
         }
     }

@@ -7,7 +7,7 @@ logs (miniMD 18,816,288; moldyn 130,023,424).
 import numpy as np
 import pytest
 
-from helpers import random_box
+from helpers import TOL_PERNODE_F64, random_box, scaled_error
 
 pytestmark = pytest.mark.gpu
 
@@ -50,6 +50,53 @@ def test_list_equals_oracle(built_lib, oracle_lib, case):
     assert np.array_equal(got, ref)
     if case == "dense_cluster":
         assert np.bincount(got[:, 0]).max() > 1024
+
+
+def boundary_box(seed: int, outside: bool):
+    """6,000 nodes, 7 cells per axis at cutoff 2.5 (the builder then takes each
+    pair's periodic image from its cell): a tenth of the coordinates moved onto
+    the places where that matters -- 0, -0, the last float below the box, each
+    cell boundary and its neighbouring floats.  With outside, some nodes also
+    sit up to 0.3 outside [0, box) or exactly on the box, where the builder
+    goes back to the per-pair rule."""
+    pos32, L = random_box(6000, 0.8442, seed)
+    assert int(np.floor(float(L) / (2.5 * 1.0001 + 1e-12))) == 7
+    rng = np.random.Generator(np.random.PCG64(seed + 1))
+    edges = np.float32(L) / np.float32(7) * np.arange(8, dtype=np.float32)
+    special = [np.float32(0.0), np.float32(-0.0), np.nextafter(np.float32(L), np.float32(0))]
+    for b in edges[1:7]:
+        special += [b, np.nextafter(b, np.float32(0)), np.nextafter(b, np.float32(L))]
+    if outside:
+        special += [np.float32(-0.3), np.float32(-0.2), np.float32(L),
+                    np.float32(L + np.float32(0.2)), np.float32(L + np.float32(0.3))]
+    k = rng.integers(0, pos32.size, size=pos32.size // 10)
+    flat = pos32.reshape(-1)
+    flat[k] = np.array(special, np.float32)[rng.integers(0, len(special), size=k.size)]
+    return pos32, float(L)
+
+
+@pytest.mark.parametrize("outside", [False, True])
+def test_cell_decided_image_at_the_boundaries(built_lib, oracle_lib, outside):
+    import irregular_gb300 as irr
+    pos32, L = boundary_box(7, outside)
+    cut2 = np.float32(2.5 * 2.5)
+    ref = oracle_lib.neighbor_half_list(pos32, L, cut2)
+    assert np.array_equal(gpu_list(irr, pos32, L, cut2), ref)
+    if outside:
+        return
+    # the MD loop's half-stencil build (each pair found once, from one end):
+    # its list size and the forces over it (law cutoff 2.2, list 2.2 + 0.3)
+    md = irr.MD(pos32.astype(np.float64), np.zeros((pos32.shape[0], 3)), L, cutforce=2.2, skin=0.3)
+    try:
+        assert md.info().num_edges == ref.shape[0]
+        f = md.forces()
+    finally:
+        md.close()
+    f64, sabs = oracle_lib.lj_reduce_f64(pos32.astype(np.float64), ref,
+                                         oracle_lib.lj_param(2.2 ** 2, L, True))
+    # per node, against the sum of its terms' magnitudes (a close pair's huge
+    # force would make a norm-wise bound meaningless for the rest)
+    assert scaled_error(f, 48.0 * f64, 48.0 * sabs) <= TOL_PERNODE_F64
 
 
 def test_known_answer_minimd(built_lib, oracle_lib):
