@@ -324,8 +324,10 @@ typedef struct irr_md_config {
     double cutforce;   /* force cutoff (2.5)                                */
     double skin;       /* neighbour skin (0.3)                              */
     double side;       /* periodic box side; > 2 (cutforce + skin)          */
-    int reorder_every; /* every this many rebuilds the atoms are re-sorted  */
-                       /* along the curve (10; 0 or 1: every rebuild)       */
+    int reorder_every; /* boxes of fewer than 3 list-cutoff cells per axis: */
+                       /* every this many rebuilds the atoms are re-sorted  */
+                       /* along the curve (10; 0 or 1: every rebuild).      */
+                       /* Larger boxes re-sort by cell at every rebuild.    */
     int reserved[7];
 } irr_md_config;
 

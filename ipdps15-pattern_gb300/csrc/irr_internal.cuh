@@ -172,6 +172,40 @@ cudaError_t launch_validate_edges(const int2* edges, int64_t e, int64_t n, int* 
                                   cudaStream_t s);
 
 // -- partitioner (irr_partition.cu) --
+// Hilbert index of a cell on the 2^10-per-axis grid: Skilling's transform
+// (J. Skilling, "Programming the Hilbert curve", AIP Conf. Proc. 707, 2004)
+// from axes to the transposed index, whose bits are then interleaved, axis 0
+// in the high bit of each 3-bit group.  The oracle restates it bit for bit.
+__device__ __forceinline__ uint32_t hilbert10(uint32_t x0, uint32_t x1, uint32_t x2)
+{
+    uint32_t X[3] = {x0, x1, x2};
+    for (uint32_t Q = 1u << 9; Q > 1; Q >>= 1) {
+        const uint32_t P = Q - 1;
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            if (X[i] & Q) {
+                X[0] ^= P;  // invert
+            } else {
+                const uint32_t t = (X[0] ^ X[i]) & P;  // exchange
+                X[0] ^= t;
+                X[i] ^= t;
+            }
+        }
+    }
+    X[1] ^= X[0];  // Gray encode
+    X[2] ^= X[1];
+    uint32_t t = 0;
+    for (uint32_t Q = 1u << 9; Q > 1; Q >>= 1)
+        if (X[2] & Q) t ^= Q - 1;
+    X[0] ^= t;
+    X[1] ^= t;
+    X[2] ^= t;
+    uint32_t key = 0;
+    for (int b = 9; b >= 0; b--)
+        key = (key << 3) | (((X[0] >> b) & 1u) << 2) | (((X[1] >> b) & 1u) << 1) | ((X[2] >> b) & 1u);
+    return key;
+}
+
 struct PartitionOut {
     int32_t* perm = nullptr;      // [n] new -> old
     int32_t* inv = nullptr;       // [n] old -> new
@@ -197,6 +231,14 @@ cudaError_t build_partition(const float4* pos_user, int64_t n, const int2* edges
 cudaError_t build_neighbor_list(const float4* pos, int64_t n, float box, float cut2,
                                 int2** d_edges, int64_t* num_edges, cudaStream_t s,
                                 bool stream_ordered = false, bool sort_rows = true);
+// Full neighbour rows of a periodic box of at least 3 cells per axis (and no
+// more cells than nodes), for the MD rebuild: out->perm (new -> old) orders
+// the nodes by the Hilbert index of their cell, out->row_off / out->col hold
+// each node's partners j != i (rule of build_neighbor_list) in that order,
+// ascending; out->inv is not made.  *num_edges = pairs (entries / 2).
+// cudaErrorNotSupported, with nothing allocated, for other boxes.
+cudaError_t build_rows_by_cell(const float4* pos, int64_t n, float box, float cut2, PartitionOut* out,
+                               int64_t* num_edges, cudaStream_t s);
 // Sorts each row of a CSR (row_off[n + 1], col) ascending; every row must
 // hold at most kRowSortMax entries.
 constexpr int kRowSortMax = 1024;

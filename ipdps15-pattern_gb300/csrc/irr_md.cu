@@ -257,24 +257,36 @@ int md_rebuild(irr_md* m)
 {
     cudaStream_t s = m->stream;
     const double lc = m->cfg.cutforce + m->cfg.skin;
-    int2* d_edges = nullptr;
+    const float list_cut2 = (float)(lc * lc);
     int64_t e = 0;
-    // the partition lays the entries out in (row, col) order itself: the
-    // half list's rows need no sort here
-    MD_CUDA(m, build_neighbor_list(m->pos4, m->n, (float)m->cfg.side, (float)(lc * lc), &d_edges, &e, s,
-                                   true, false),
-            "neighbour build");
     free_part(m, s);
-    // The node order only decides locality: atoms move a fraction of the skin
-    // between rebuilds, so the curve order of an earlier rebuild stays nearly
-    // as local, and the atoms are re-sorted only every reorder_every-th
-    // rebuild (the first one included); the others keep the execution order.
-    const bool reorder = m->rebuilds % (m->cfg.reorder_every > 1 ? m->cfg.reorder_every : 1) == 0;
+    // A box of at least 3 cells per axis: the atoms are re-sorted by cell
+    // along a Hilbert curve of the cells at every rebuild, and each row is
+    // written already in (row, col) order straight from the cell search.
     PartitionOut p;
-    cudaError_t pe = build_partition(m->pos4, m->n, d_edges, e, reorder ? 1 : 0, &p, s);
-    if (d_edges) cudaFreeAsync(d_edges, s);
+    cudaError_t pe = build_rows_by_cell(m->pos4, m->n, (float)m->cfg.side, list_cut2, &p, &e, s);
+    bool reorder = true;
+    if (pe == cudaErrorNotSupported) {
+        // Smaller boxes: the half list, then the partition's node order and
+        // (row, col) layout.  The node order only decides locality: atoms
+        // move a fraction of the skin between rebuilds, so the curve order of
+        // an earlier rebuild stays nearly as local, and the atoms are
+        // re-sorted only every reorder_every-th rebuild (the first one
+        // included); the others keep the execution order.
+        int2* d_edges = nullptr;
+        MD_CUDA(m, build_neighbor_list(m->pos4, m->n, (float)m->cfg.side, list_cut2, &d_edges, &e, s,
+                                       true, false),
+                "neighbour build");
+        reorder = m->rebuilds % (m->cfg.reorder_every > 1 ? m->cfg.reorder_every : 1) == 0;
+        pe = build_partition(m->pos4, m->n, d_edges, e, reorder ? 1 : 0, &p, s);
+        if (d_edges) cudaFreeAsync(d_edges, s);
+    }
     m->part = p;
-    if (pe != cudaSuccess) return md_fail(m, IRR_ERR_CUDA, "partition", pe);
+    if (pe != cudaSuccess)
+        return md_fail(m, pe == cudaErrorMemoryAllocation ? IRR_ERR_NOMEM
+                          : pe == cudaErrorInvalidValue  ? IRR_ERR_CAPACITY
+                                                         : IRR_ERR_CUDA,
+                       "neighbour rows", pe);
     if (reorder) {
         // state into the new order
         const int g = grid_of(m->n);

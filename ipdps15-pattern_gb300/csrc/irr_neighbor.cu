@@ -20,6 +20,7 @@
 // dy*dy) + dz*dz) with every operation rounded.  Output: pairs (i, j), i < j,
 // sorted by i then j -- moldyn's loop order; miniMD lists the same pairs.
 #include <cmath>
+#include <vector>
 
 #include "irr_internal.cuh"
 #include "../../include/irregular_gb300.h"
@@ -292,6 +293,144 @@ __global__ void expand_pairs_kernel(const uint32_t* row_off, const int32_t* nbr,
     }
 }
 
+// ---- full rows in cell order (the MD rebuild)
+// Nodes sorted by the Hilbert index of their cell (cells of the 10-bit curve
+// grid: at most 1024 per axis), so each cell's nodes are one contiguous run
+// and runs follow the curve; a node's row visits its 27 neighbour cells in
+// curve order, so the row comes out ascending with no sort and no atomics.
+
+__device__ __forceinline__ uint32_t cell_of(float4 p, const Grid& g)
+{
+    return ((uint32_t)cell_coord(p.z, 2, g) * g.nc[1] + cell_coord(p.y, 1, g)) * g.nc[0] +
+           cell_coord(p.x, 0, g);
+}
+
+// keys[i] = curve index of node i's cell, vals[i] = i; *outside as in cell_keys.
+__global__ void cell_curve_keys_kernel(const float4* pos, int64_t n, const __grid_constant__ Grid g,
+                                       uint32_t* keys, int32_t* vals, int* outside)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const float4 p = pos[i];
+        if (g.periodic && !(p.x >= 0.f && p.x < g.box && p.y >= 0.f && p.y < g.box && p.z >= 0.f &&
+                            p.z < g.box))
+            *outside = 1;
+        keys[i] = hilbert10(cell_coord(p.x, 0, g), cell_coord(p.y, 1, g), cell_coord(p.z, 2, g));
+        vals[i] = (int32_t)i;
+    }
+}
+
+// span[c] = [first, end) of cell c's run in the sorted order (0, 0 if empty).
+__global__ void cell_spans_kernel(const float4* __restrict__ pos_c, const uint32_t* __restrict__ keys,
+                                  int64_t n, const __grid_constant__ Grid g, uint2* span)
+{
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t k = keys[t];
+        const bool first = t == 0 || keys[t - 1] != k;
+        const bool last = t == n - 1 || keys[t + 1] != k;
+        if (first || last) {
+            const uint32_t c = cell_of(pos_c[t], g);
+            if (first) span[c].x = (uint32_t)t;
+            if (last) span[c].y = (uint32_t)(t + 1);
+        }
+    }
+}
+
+// Per cell, its 27 neighbour cells (periodic, at least 3 per axis, so all
+// distinct) in curve order: {run first, run end, image code}, the code 2 bits
+// per axis (1: +box, 2: -box; the shift list_pair_shifted adds).
+__global__ void cell_stencil_kernel(const __grid_constant__ Grid g, const uint2* __restrict__ span,
+                                    int64_t ncell, int4* table)
+{
+    for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncell;
+         c += (int64_t)gridDim.x * blockDim.x) {
+        const int cx = (int)(c % g.nc[0]), cy = (int)((c / g.nc[0]) % g.nc[1]),
+                  cz = (int)(c / ((int64_t)g.nc[0] * g.nc[1]));
+        uint32_t key[27];
+        int4 ent[27];
+        for (int k = 0; k < 27; k++) {
+            int z = cz + k / 9 - 1, y = cy + (k / 3) % 3 - 1, x = cx + k % 3 - 1;
+            float sx, sy, sz;
+            wrap_cell(z, g.nc[2], g.box, sz);
+            wrap_cell(y, g.nc[1], g.box, sy);
+            wrap_cell(x, g.nc[0], g.box, sx);
+            const int code = (sx > 0.f ? 1 : sx < 0.f ? 2 : 0) | (sy > 0.f ? 4 : sy < 0.f ? 8 : 0) |
+                             (sz > 0.f ? 16 : sz < 0.f ? 32 : 0);
+            const uint2 sp = span[((int64_t)z * g.nc[1] + y) * g.nc[0] + x];
+            key[k] = hilbert10((uint32_t)x, (uint32_t)y, (uint32_t)z);
+            ent[k] = make_int4((int)sp.x, (int)sp.y, code, 0);
+            for (int u = k; u > 0 && key[u - 1] > key[u]; u--) {  // insertion by key
+                const uint32_t tk = key[u];
+                key[u] = key[u - 1];
+                key[u - 1] = tk;
+                const int4 te = ent[u];
+                ent[u] = ent[u - 1];
+                ent[u - 1] = te;
+            }
+        }
+        for (int k = 0; k < 27; k++) table[c * 27 + k] = ent[k];
+    }
+}
+
+__device__ __forceinline__ float image_shift(int code, float box)
+{
+    return code == 1 ? box : (code == 2 ? -box : 0.f);
+}
+
+// WRITE == false: deg[t] = row length; WRITE: the row's columns from
+// row_off[t], ascending.
+template <bool WRITE, bool FAST>
+__device__ __forceinline__ void cell_rows_body(const float4* __restrict__ pos_c, int64_t n, const Grid& g,
+                                               const int4* __restrict__ table, uint32_t* deg,
+                                               const uint32_t* __restrict__ row_off, int32_t* col)
+{
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const float4 a = pos_c[t];
+        const int4* st = table + (int64_t)cell_of(a, g) * 27;
+        uint32_t m = 0;
+        const uint32_t base = WRITE ? row_off[t] : 0;
+        for (int k = 0; k < 27; k++) {
+            const int4 e = st[k];
+            const float sx = image_shift(e.z & 3, g.box), sy = image_shift((e.z >> 2) & 3, g.box),
+                        sz = image_shift((e.z >> 4) & 3, g.box);
+#pragma unroll 2
+            for (uint32_t q = (uint32_t)e.x; q < (uint32_t)e.y; q++) {
+                const float4 b = pos_c[q];
+                if (q != (uint32_t)t && pair_hit<FAST>(a, b, g, sx, sy, sz)) {
+                    if (WRITE) col[base + m] = (int32_t)q;
+                    m++;
+                }
+            }
+        }
+        if (!WRITE) deg[t] = m;
+    }
+}
+
+// *total += sum of deg[0, n) in 64 bits (the row offsets are 32-bit: the
+// caller refuses a list whose entries do not fit)
+__global__ void sum_u32_kernel(const uint32_t* __restrict__ deg, int64_t n, unsigned long long* total)
+{
+    unsigned long long w = 0;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+         t += (int64_t)gridDim.x * blockDim.x)
+        w += deg[t];
+    for (int off = 16; off > 0; off >>= 1) w += __shfl_down_sync(0xffffffffu, w, off);
+    if ((threadIdx.x & 31) == 0 && w) atomicAdd(total, w);
+}
+
+template <bool WRITE>
+__global__ void cell_rows_kernel(const float4* __restrict__ pos_c, int64_t n, const __grid_constant__ Grid g,
+                                 const int* __restrict__ outside, const int4* __restrict__ table,
+                                 uint32_t* deg, const uint32_t* __restrict__ row_off, int32_t* col)
+{
+    if (g.fast && *outside == 0)
+        cell_rows_body<WRITE, true>(pos_c, n, g, table, deg, row_off, col);
+    else
+        cell_rows_body<WRITE, false>(pos_c, n, g, table, deg, row_off, col);
+}
+
 int grid_of(int64_t n)
 {
     int64_t g = (n + 255) / 256;
@@ -302,13 +441,13 @@ int grid_of(int64_t n)
 
 // Builds the list; *d_edges is cudaMalloc'd, or cudaMallocAsync'd on s when
 // stream_ordered (2 * *num_edges int32).
-cudaError_t build_neighbor_list(const float4* pos, int64_t n, float box, float cut2,
-                                int2** d_edges, int64_t* num_edges, cudaStream_t s,
-                                bool stream_ordered, bool sort_rows)
+namespace {
+
+// The cell grid of a list cutoff: cells at least as wide as the cutoff (so a
+// partner is in the same or an adjacent cell), at most 1024 per axis and a
+// few per node; a periodic axis of fewer than 3 cells becomes one cell.
+cudaError_t make_grid(const float4* pos, int64_t n, float box, float cut2, Grid* out, cudaStream_t s)
 {
-    *d_edges = nullptr;
-    *num_edges = 0;
-    if (n <= 1) return cudaSuccess;
     Grid g{};
     g.periodic = box > 0.0f;
     g.box = box;
@@ -354,6 +493,21 @@ cudaError_t build_neighbor_list(const float4* pos, int64_t n, float box, float c
         }
     }
     g.fast = g.periodic && g.nc[0] >= 5 && g.nc[1] >= 5 && g.nc[2] >= 5;
+    *out = g;
+    return cudaSuccess;
+}
+
+}  // namespace
+
+cudaError_t build_neighbor_list(const float4* pos, int64_t n, float box, float cut2,
+                                int2** d_edges, int64_t* num_edges, cudaStream_t s,
+                                bool stream_ordered, bool sort_rows)
+{
+    *d_edges = nullptr;
+    *num_edges = 0;
+    if (n <= 1) return cudaSuccess;
+    Grid g{};
+    IRR_CUDA_TRY(make_grid(pos, n, box, cut2, &g, s));
     const int64_t ncell = (int64_t)g.nc[0] * g.nc[1] * g.nc[2];
     uint32_t *keys = nullptr, *keys_tmp = nullptr, *cell_start = nullptr, *cnt = nullptr;
     int32_t *sorted = nullptr, *vals_tmp = nullptr, *nbr = nullptr;
@@ -435,6 +589,95 @@ cudaError_t build_neighbor_list(const float4* pos, int64_t n, float box, float c
     IRR_CUDA_TRY(cudaStreamSynchronize(s));
     *d_edges = edges;
     *num_edges = total;
+    return cudaSuccess;
+}
+
+namespace {
+
+// Stream-ordered temporaries freed on every return.
+struct Temps {
+    cudaStream_t s;
+    std::vector<void*> p;
+    template <typename T>
+    cudaError_t get(T** out, size_t count)
+    {
+        *out = nullptr;
+        const cudaError_t e = irr_malloc_async((void**)out, sizeof(T) * (count ? count : 1), s);
+        if (e == cudaSuccess) p.push_back(*out);
+        return e;
+    }
+    ~Temps()
+    {
+        for (void* q : p) cudaFreeAsync(q, s);
+    }
+};
+
+}  // namespace
+
+cudaError_t build_rows_by_cell(const float4* pos, int64_t n, float box, float cut2, PartitionOut* out,
+                               int64_t* num_edges, cudaStream_t s)
+{
+    *out = PartitionOut{};
+    *num_edges = 0;
+    if (n <= 1 || !(box > 0.0f) || n > 0x7fffffffLL) return cudaErrorNotSupported;
+    Grid g{};
+    IRR_CUDA_TRY(make_grid(pos, n, box, cut2, &g, s));  // periodic: host arithmetic only
+    const int64_t ncell = (int64_t)g.nc[0] * g.nc[1] * g.nc[2];
+    if (g.nc[0] < 3 || g.nc[1] < 3 || g.nc[2] < 3 || ncell > n) return cudaErrorNotSupported;
+    Temps tmp{s, {}};
+    uint32_t *keys = nullptr, *keys_tmp = nullptr;
+    int32_t* vals_tmp = nullptr;
+    float4* pos_c = nullptr;
+    uint2* span = nullptr;
+    int4* table = nullptr;
+    unsigned long long* aux = nullptr;  // [0] the entry count, [1] the outside flag
+    PartitionOut p;
+    auto run = [&]() -> cudaError_t {
+        IRR_CUDA_TRY(irr_malloc_async((void**)&p.perm, sizeof(int32_t) * n, s));
+        IRR_CUDA_TRY(irr_malloc_async((void**)&p.row_off, sizeof(uint32_t) * (n + 1), s));
+        IRR_CUDA_TRY(tmp.get(&keys, n));
+        IRR_CUDA_TRY(tmp.get(&keys_tmp, n));
+        IRR_CUDA_TRY(tmp.get(&vals_tmp, n));
+        IRR_CUDA_TRY(tmp.get(&pos_c, n));
+        IRR_CUDA_TRY(tmp.get(&span, ncell));
+        IRR_CUDA_TRY(tmp.get(&table, ncell * 27));
+        IRR_CUDA_TRY(tmp.get(&aux, 2));
+        IRR_CUDA_TRY(cudaMemsetAsync(span, 0, sizeof(uint2) * ncell, s));
+        IRR_CUDA_TRY(cudaMemsetAsync(aux, 0, 2 * sizeof(unsigned long long), s));
+        int* outside = reinterpret_cast<int*>(aux + 1);
+        const int gn = grid_of(n);
+        cell_curve_keys_kernel<<<gn, 256, 0, s>>>(pos, n, g, keys, p.perm, outside);
+        IRR_CUDA_TRY(cudaGetLastError());
+        IRR_CUDA_TRY(radix_sort_pairs(keys, p.perm, keys_tmp, vals_tmp, n, 30, s));
+        cell_order_kernel<<<gn, 256, 0, s>>>(pos, p.perm, n, pos_c);
+        cell_spans_kernel<<<gn, 256, 0, s>>>(pos_c, keys, n, g, span);
+        cell_stencil_kernel<<<grid_of(ncell), 256, 0, s>>>(g, span, ncell, table);
+        cell_rows_kernel<false><<<gn, 256, 0, s>>>(pos_c, n, g, outside, table, p.row_off, nullptr, nullptr);
+        sum_u32_kernel<<<gn, 256, 0, s>>>(p.row_off, n, aux);
+        IRR_CUDA_TRY(cudaGetLastError());
+        unsigned long long total = 0;
+        IRR_CUDA_TRY(cudaMemcpyAsync(&total, aux, sizeof(total), cudaMemcpyDeviceToHost, s));
+        IRR_CUDA_TRY(cudaStreamSynchronize(s));
+        if (total > 0x7fffffffull) return cudaErrorInvalidValue;
+        IRR_CUDA_TRY(cudaMemsetAsync(p.row_off + n, 0, sizeof(uint32_t), s));
+        IRR_CUDA_TRY(scan_exclusive_u32(p.row_off, p.row_off, n + 1, nullptr, s));
+        // + kColPad: bulk copies of an entry segment may read past the last one
+        IRR_CUDA_TRY(irr_malloc_async((void**)&p.col, sizeof(int32_t) * (total + kColPad), s));
+        IRR_CUDA_TRY(cudaMemsetAsync(p.col + total, 0, sizeof(int32_t) * kColPad, s));
+        cell_rows_kernel<true><<<gn, 256, 0, s>>>(pos_c, n, g, outside, table, nullptr, p.row_off, p.col);
+        IRR_CUDA_TRY(cudaGetLastError());
+        *num_edges = (int64_t)(total / 2);
+        return cudaSuccess;
+    };
+    const cudaError_t e = run();
+    if (e != cudaSuccess) {
+        if (p.perm) cudaFreeAsync(p.perm, s);
+        if (p.row_off) cudaFreeAsync(p.row_off, s);
+        if (p.col) cudaFreeAsync(p.col, s);
+        *num_edges = 0;
+        return e;
+    }
+    *out = p;
     return cudaSuccess;
 }
 

@@ -353,40 +353,6 @@ __device__ __forceinline__ uint32_t quant10(float x, float lo, float scale)
     return __float2uint_rz(t);
 }
 
-// Hilbert index of a cell on the 2^10-per-axis grid: Skilling's transform
-// (J. Skilling, "Programming the Hilbert curve", AIP Conf. Proc. 707, 2004)
-// from axes to the transposed index, whose bits are then interleaved, axis 0
-// in the high bit of each 3-bit group.  The oracle restates it bit for bit.
-__device__ __forceinline__ uint32_t hilbert10(uint32_t x0, uint32_t x1, uint32_t x2)
-{
-    uint32_t X[3] = {x0, x1, x2};
-    for (uint32_t Q = 1u << 9; Q > 1; Q >>= 1) {
-        const uint32_t P = Q - 1;
-#pragma unroll
-        for (int i = 0; i < 3; i++) {
-            if (X[i] & Q) {
-                X[0] ^= P;  // invert
-            } else {
-                const uint32_t t = (X[0] ^ X[i]) & P;  // exchange
-                X[0] ^= t;
-                X[i] ^= t;
-            }
-        }
-    }
-    X[1] ^= X[0];  // Gray encode
-    X[2] ^= X[1];
-    uint32_t t = 0;
-    for (uint32_t Q = 1u << 9; Q > 1; Q >>= 1)
-        if (X[2] & Q) t ^= Q - 1;
-    X[0] ^= t;
-    X[1] ^= t;
-    X[2] ^= t;
-    uint32_t key = 0;
-    for (int b = 9; b >= 0; b--)
-        key = (key << 3) | (((X[0] >> b) & 1u) << 2) | (((X[1] >> b) & 1u) << 1) | ((X[2] >> b) & 1u);
-    return key;
-}
-
 // Curve key of each node (curve 0: Hilbert, 1: Morton) on the 10-bit grid.
 __global__ void curve_key_kernel(const float4* pos, int64_t n, float3 lo, float3 scale, int curve,
                                  uint32_t* keys, int32_t* vals)

@@ -16,8 +16,10 @@ def system(cells=6, rho=0.8442, temp=1.44, seed=20260003, jitter=0.03):
 
 @pytest.mark.parametrize("cells", [4, 6, 12])
 def test_initial_forces_match_fp64(built_lib, oracle_lib, cells):
-    """cells 4: two list cells per axis (the full-stencil search); 6 and 12:
-    3 and 7 cells per axis (the half stencil, each pair found once)."""
+    """cells 4: two list cells per axis (the half list, then the partition's
+    node order and row layout); 6 and 12: 3 and 7 cells per axis (atoms sorted
+    by cell, rows written in order by the cell search; at 7 cells each pair's
+    image is decided by its cell)."""
     import irregular_gb300 as irr
     O = oracle_lib
     pos, vel, side = system(cells=cells)
@@ -34,13 +36,14 @@ def test_initial_forces_match_fp64(built_lib, oracle_lib, cells):
     md.close()
 
 
-@pytest.mark.parametrize("reorder_every", [1, 10])
-def test_short_trajectory_matches_fp64_reference(built_lib, oracle_lib, reorder_every):
-    """reorder_every 1: the second rebuild re-sorts the atoms; 10: it keeps
-    their order (either way the same physics)."""
+@pytest.mark.parametrize("cells,reorder_every", [(4, 1), (4, 10), (6, 10), (12, 10)])
+def test_short_trajectory_matches_fp64_reference(built_lib, oracle_lib, cells, reorder_every):
+    """cells 4 (two list cells per axis): reorder_every 1 re-sorts the atoms
+    at the second rebuild, 10 keeps their order; cells 6 and 12 re-sort by
+    cell at every rebuild (either way the same physics)."""
     import irregular_gb300 as irr
     O = oracle_lib
-    pos, vel, side = system()
+    pos, vel, side = system(cells=cells)
     steps = 25  # crosses one rebuild (every 20 steps)
     md = irr.MD(pos, vel, side, dt=0.005, rebuild_every=20, reorder_every=reorder_every)
     md.run(steps)
