@@ -235,10 +235,14 @@ cudaError_t build_neighbor_list(const float4* pos, int64_t n, float box, float c
 // more cells than nodes), for the MD rebuild: out->perm (new -> old) orders
 // the nodes by the Hilbert index of their cell, out->row_off / out->col hold
 // each node's partners j != i (rule of build_neighbor_list) in that order,
-// ascending; out->inv is not made.  *num_edges = pairs (entries / 2).
-// cudaErrorNotSupported, with nothing allocated, for other boxes.
+// ascending; out->inv is not made.  *num_edges = pairs (entries / 2),
+// *longest = the longest row.  cap_hint > 0 (e.g. from the previous build's
+// longest row) lets one search pass write rows of up to cap_hint entries into
+// per-node slots, packed afterwards; 0, or a longer row, takes a counting and
+// a writing pass.  cudaErrorNotSupported, with nothing allocated, for other
+// boxes.
 cudaError_t build_rows_by_cell(const float4* pos, int64_t n, float box, float cut2, PartitionOut* out,
-                               int64_t* num_edges, cudaStream_t s);
+                               int64_t* num_edges, uint32_t* longest, uint32_t cap_hint, cudaStream_t s);
 // Sorts each row of a CSR (row_off[n + 1], col) ascending; every row must
 // hold at most kRowSortMax entries.
 constexpr int kRowSortMax = 1024;

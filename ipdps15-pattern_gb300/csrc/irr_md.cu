@@ -264,7 +264,12 @@ int md_rebuild(irr_md* m)
     // along a Hilbert curve of the cells at every rebuild, and each row is
     // written already in (row, col) order straight from the cell search.
     PartitionOut p;
-    cudaError_t pe = build_rows_by_cell(m->pos4, m->n, (float)m->cfg.side, list_cut2, &p, &e, s);
+    // Rows change little between rebuilds: slots a quarter longer than the
+    // last build's longest row let one search pass write them.
+    uint32_t longest = 0;
+    cudaError_t pe = build_rows_by_cell(m->pos4, m->n, (float)m->cfg.side, list_cut2, &p, &e, &longest,
+                                        m->row_cap, s);
+    if (pe == cudaSuccess) m->row_cap = (longest + longest / 4 + 8 + 7) & ~7u;
     bool reorder = true;
     if (pe == cudaErrorNotSupported) {
         // Smaller boxes: the half list, then the partition's node order and

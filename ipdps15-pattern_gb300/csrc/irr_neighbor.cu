@@ -339,18 +339,21 @@ __global__ void cell_spans_kernel(const float4* __restrict__ pos_c, const uint32
 
 // Per cell, its 27 neighbour cells (periodic, at least 3 per axis, so all
 // distinct) in curve order: {run first, run end, image code}, the code 2 bits
-// per axis (1: +box, 2: -box; the shift list_pair_shifted adds).
+// per axis (1: +box, 2: -box; the shift list_pair_shifted adds).  One warp
+// per cell: lane k < 27 takes neighbour k, and a bitonic network over the
+// warp's 32 (key, lane) pairs (5 padding keys at the top) puts them in order.
 __global__ void cell_stencil_kernel(const __grid_constant__ Grid g, const uint2* __restrict__ span,
                                     int64_t ncell, int4* table)
 {
-    for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncell;
-         c += (int64_t)gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t c = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < ncell; c += warps) {
         const int cx = (int)(c % g.nc[0]), cy = (int)((c / g.nc[0]) % g.nc[1]),
                   cz = (int)(c / ((int64_t)g.nc[0] * g.nc[1]));
-        uint32_t key[27];
-        int4 ent[27];
-        for (int k = 0; k < 27; k++) {
-            int z = cz + k / 9 - 1, y = cy + (k / 3) % 3 - 1, x = cx + k % 3 - 1;
+        uint32_t key = 0xffffffffu;
+        int4 ent = make_int4(0, 0, 0, 0);
+        if (lane < 27) {
+            int z = cz + lane / 9 - 1, y = cy + (lane / 3) % 3 - 1, x = cx + lane % 3 - 1;
             float sx, sy, sz;
             wrap_cell(z, g.nc[2], g.box, sz);
             wrap_cell(y, g.nc[1], g.box, sy);
@@ -358,18 +361,29 @@ __global__ void cell_stencil_kernel(const __grid_constant__ Grid g, const uint2*
             const int code = (sx > 0.f ? 1 : sx < 0.f ? 2 : 0) | (sy > 0.f ? 4 : sy < 0.f ? 8 : 0) |
                              (sz > 0.f ? 16 : sz < 0.f ? 32 : 0);
             const uint2 sp = span[((int64_t)z * g.nc[1] + y) * g.nc[0] + x];
-            key[k] = hilbert10((uint32_t)x, (uint32_t)y, (uint32_t)z);
-            ent[k] = make_int4((int)sp.x, (int)sp.y, code, 0);
-            for (int u = k; u > 0 && key[u - 1] > key[u]; u--) {  // insertion by key
-                const uint32_t tk = key[u];
-                key[u] = key[u - 1];
-                key[u - 1] = tk;
-                const int4 te = ent[u];
-                ent[u] = ent[u - 1];
-                ent[u - 1] = te;
+            key = hilbert10((uint32_t)x, (uint32_t)y, (uint32_t)z);
+            ent = make_int4((int)sp.x, (int)sp.y, code, 0);
+        }
+        int src = lane;  // whose entry this lane holds after the network
+#pragma unroll
+        for (int size = 2; size <= 32; size <<= 1) {
+#pragma unroll
+            for (int stride = size >> 1; stride > 0; stride >>= 1) {
+                const uint32_t ok = __shfl_xor_sync(0xffffffffu, key, stride);
+                const int os = __shfl_xor_sync(0xffffffffu, src, stride);
+                const bool up = (lane & size) == 0;
+                const bool lower = (lane & stride) == 0;
+                // keep the smaller key in the lower lane of an ascending pair
+                const bool take = (up == lower) ? (ok < key) : (ok > key);
+                if (take) {
+                    key = ok;
+                    src = os;
+                }
             }
         }
-        for (int k = 0; k < 27; k++) table[c * 27 + k] = ent[k];
+        const int4 got = make_int4(__shfl_sync(0xffffffffu, ent.x, src), __shfl_sync(0xffffffffu, ent.y, src),
+                                   __shfl_sync(0xffffffffu, ent.z, src), 0);
+        if (lane < 27) table[c * 27 + lane] = got;
     }
 }
 
@@ -378,19 +392,24 @@ __device__ __forceinline__ float image_shift(int code, float box)
     return code == 1 ? box : (code == 2 ? -box : 0.f);
 }
 
-// WRITE == false: deg[t] = row length; WRITE: the row's columns from
-// row_off[t], ascending.
-template <bool WRITE, bool FAST>
+// MODE kCount: deg[t] = row length.  kWrite: the row's columns from
+// row_off[t], ascending.  kScratch: both in one pass, the columns into a
+// fixed-capacity slot scratch[t * cap, +cap) (the count goes on past cap, so
+// an overflowing row is known and its entries are not stored).
+enum RowsMode { kCount = 0, kWrite = 1, kScratch = 2 };
+
+template <int MODE, bool FAST>
 __device__ __forceinline__ void cell_rows_body(const float4* __restrict__ pos_c, int64_t n, const Grid& g,
                                                const int4* __restrict__ table, uint32_t* deg,
-                                               const uint32_t* __restrict__ row_off, int32_t* col)
+                                               const uint32_t* __restrict__ row_off, int32_t* col,
+                                               uint32_t cap)
 {
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
          t += (int64_t)gridDim.x * blockDim.x) {
         const float4 a = pos_c[t];
         const int4* st = table + (int64_t)cell_of(a, g) * 27;
         uint32_t m = 0;
-        const uint32_t base = WRITE ? row_off[t] : 0;
+        int32_t* out = MODE == kWrite ? col + row_off[t] : (MODE == kScratch ? col + t * (int64_t)cap : nullptr);
         for (int k = 0; k < 27; k++) {
             const int4 e = st[k];
             const float sx = image_shift(e.z & 3, g.box), sy = image_shift((e.z >> 2) & 3, g.box),
@@ -399,36 +418,59 @@ __device__ __forceinline__ void cell_rows_body(const float4* __restrict__ pos_c,
             for (uint32_t q = (uint32_t)e.x; q < (uint32_t)e.y; q++) {
                 const float4 b = pos_c[q];
                 if (q != (uint32_t)t && pair_hit<FAST>(a, b, g, sx, sy, sz)) {
-                    if (WRITE) col[base + m] = (int32_t)q;
+                    if (MODE == kWrite || (MODE == kScratch && m < cap)) out[m] = (int32_t)q;
                     m++;
                 }
             }
         }
-        if (!WRITE) deg[t] = m;
+        if (MODE != kWrite) deg[t] = m;
     }
 }
 
-// *total += sum of deg[0, n) in 64 bits (the row offsets are 32-bit: the
-// caller refuses a list whose entries do not fit)
-__global__ void sum_u32_kernel(const uint32_t* __restrict__ deg, int64_t n, unsigned long long* total)
+// Scratch rows (cap apart) packed into col at row_off: one warp per row.
+__global__ void compact_rows_kernel(const int32_t* __restrict__ scratch, uint32_t cap,
+                                    const uint32_t* __restrict__ row_off, int64_t n, int32_t* __restrict__ col)
 {
-    unsigned long long w = 0;
-    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
-         t += (int64_t)gridDim.x * blockDim.x)
-        w += deg[t];
-    for (int off = 16; off > 0; off >>= 1) w += __shfl_down_sync(0xffffffffu, w, off);
-    if ((threadIdx.x & 31) == 0 && w) atomicAdd(total, w);
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t t = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < n; t += warps) {
+        const uint32_t b = row_off[t], len = row_off[t + 1] - b;
+        const int32_t* src = scratch + t * (int64_t)cap;
+        for (uint32_t k = lane; k < len; k += 32) col[b + k] = src[k];
+    }
 }
 
-template <bool WRITE>
+// total[0] += sum of deg[0, n) in 64 bits (the row offsets are 32-bit: the
+// caller refuses a list whose entries do not fit), and total[1] = max(total[1], the longest row).
+__global__ void sum_u32_kernel(const uint32_t* __restrict__ deg, int64_t n, unsigned long long* total)
+{
+    unsigned long long w = 0, mx = 0;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        w += deg[t];
+        mx = deg[t] > mx ? deg[t] : mx;
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        w += __shfl_down_sync(0xffffffffu, w, off);
+        const unsigned long long o = __shfl_down_sync(0xffffffffu, mx, off);
+        mx = o > mx ? o : mx;
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (w) atomicAdd(total, w);
+        if (mx) atomicMax(total + 1, mx);
+    }
+}
+
+template <int MODE>
 __global__ void cell_rows_kernel(const float4* __restrict__ pos_c, int64_t n, const __grid_constant__ Grid g,
                                  const int* __restrict__ outside, const int4* __restrict__ table,
-                                 uint32_t* deg, const uint32_t* __restrict__ row_off, int32_t* col)
+                                 uint32_t* deg, const uint32_t* __restrict__ row_off, int32_t* col,
+                                 uint32_t cap)
 {
     if (g.fast && *outside == 0)
-        cell_rows_body<WRITE, true>(pos_c, n, g, table, deg, row_off, col);
+        cell_rows_body<MODE, true>(pos_c, n, g, table, deg, row_off, col, cap);
     else
-        cell_rows_body<WRITE, false>(pos_c, n, g, table, deg, row_off, col);
+        cell_rows_body<MODE, false>(pos_c, n, g, table, deg, row_off, col, cap);
 }
 
 int grid_of(int64_t n)
@@ -615,10 +657,11 @@ struct Temps {
 }  // namespace
 
 cudaError_t build_rows_by_cell(const float4* pos, int64_t n, float box, float cut2, PartitionOut* out,
-                               int64_t* num_edges, cudaStream_t s)
+                               int64_t* num_edges, uint32_t* longest, uint32_t cap_hint, cudaStream_t s)
 {
     *out = PartitionOut{};
     *num_edges = 0;
+    *longest = 0;
     if (n <= 1 || !(box > 0.0f) || n > 0x7fffffffLL) return cudaErrorNotSupported;
     Grid g{};
     IRR_CUDA_TRY(make_grid(pos, n, box, cut2, &g, s));  // periodic: host arithmetic only
@@ -626,11 +669,11 @@ cudaError_t build_rows_by_cell(const float4* pos, int64_t n, float box, float cu
     if (g.nc[0] < 3 || g.nc[1] < 3 || g.nc[2] < 3 || ncell > n) return cudaErrorNotSupported;
     Temps tmp{s, {}};
     uint32_t *keys = nullptr, *keys_tmp = nullptr;
-    int32_t* vals_tmp = nullptr;
+    int32_t *vals_tmp = nullptr, *scratch = nullptr;
     float4* pos_c = nullptr;
     uint2* span = nullptr;
     int4* table = nullptr;
-    unsigned long long* aux = nullptr;  // [0] the entry count, [1] the outside flag
+    unsigned long long* aux = nullptr;  // [0] the entry count, [1] the longest row, [2] the outside flag
     PartitionOut p;
     auto run = [&]() -> cudaError_t {
         IRR_CUDA_TRY(irr_malloc_async((void**)&p.perm, sizeof(int32_t) * n, s));
@@ -641,32 +684,50 @@ cudaError_t build_rows_by_cell(const float4* pos, int64_t n, float box, float cu
         IRR_CUDA_TRY(tmp.get(&pos_c, n));
         IRR_CUDA_TRY(tmp.get(&span, ncell));
         IRR_CUDA_TRY(tmp.get(&table, ncell * 27));
-        IRR_CUDA_TRY(tmp.get(&aux, 2));
+        IRR_CUDA_TRY(tmp.get(&aux, 3));
+        // one search pass into cap_hint slots per node when they fit in memory;
+        // otherwise (and at the first build) a counting pass, then the writing one
+        bool one_pass = false;
+        if (cap_hint > 0 && cap_hint <= 4096) {
+            one_pass = tmp.get(&scratch, (size_t)n * cap_hint) == cudaSuccess;
+            if (!one_pass) cudaGetLastError();
+        }
         IRR_CUDA_TRY(cudaMemsetAsync(span, 0, sizeof(uint2) * ncell, s));
-        IRR_CUDA_TRY(cudaMemsetAsync(aux, 0, 2 * sizeof(unsigned long long), s));
-        int* outside = reinterpret_cast<int*>(aux + 1);
+        IRR_CUDA_TRY(cudaMemsetAsync(aux, 0, 3 * sizeof(unsigned long long), s));
+        int* outside = reinterpret_cast<int*>(aux + 2);
         const int gn = grid_of(n);
         cell_curve_keys_kernel<<<gn, 256, 0, s>>>(pos, n, g, keys, p.perm, outside);
         IRR_CUDA_TRY(cudaGetLastError());
         IRR_CUDA_TRY(radix_sort_pairs(keys, p.perm, keys_tmp, vals_tmp, n, 30, s));
         cell_order_kernel<<<gn, 256, 0, s>>>(pos, p.perm, n, pos_c);
         cell_spans_kernel<<<gn, 256, 0, s>>>(pos_c, keys, n, g, span);
-        cell_stencil_kernel<<<grid_of(ncell), 256, 0, s>>>(g, span, ncell, table);
-        cell_rows_kernel<false><<<gn, 256, 0, s>>>(pos_c, n, g, outside, table, p.row_off, nullptr, nullptr);
+        cell_stencil_kernel<<<grid_of(32 * ncell), 256, 0, s>>>(g, span, ncell, table);
+        if (one_pass)
+            cell_rows_kernel<kScratch><<<gn, 256, 0, s>>>(pos_c, n, g, outside, table, p.row_off, nullptr,
+                                                          scratch, cap_hint);
+        else
+            cell_rows_kernel<kCount><<<gn, 256, 0, s>>>(pos_c, n, g, outside, table, p.row_off, nullptr,
+                                                        nullptr, 0);
         sum_u32_kernel<<<gn, 256, 0, s>>>(p.row_off, n, aux);
         IRR_CUDA_TRY(cudaGetLastError());
-        unsigned long long total = 0;
-        IRR_CUDA_TRY(cudaMemcpyAsync(&total, aux, sizeof(total), cudaMemcpyDeviceToHost, s));
+        unsigned long long host_aux[2] = {0, 0};
+        IRR_CUDA_TRY(cudaMemcpyAsync(host_aux, aux, sizeof(host_aux), cudaMemcpyDeviceToHost, s));
         IRR_CUDA_TRY(cudaStreamSynchronize(s));
+        const unsigned long long total = host_aux[0];
         if (total > 0x7fffffffull) return cudaErrorInvalidValue;
         IRR_CUDA_TRY(cudaMemsetAsync(p.row_off + n, 0, sizeof(uint32_t), s));
         IRR_CUDA_TRY(scan_exclusive_u32(p.row_off, p.row_off, n + 1, nullptr, s));
         // + kColPad: bulk copies of an entry segment may read past the last one
         IRR_CUDA_TRY(irr_malloc_async((void**)&p.col, sizeof(int32_t) * (total + kColPad), s));
         IRR_CUDA_TRY(cudaMemsetAsync(p.col + total, 0, sizeof(int32_t) * kColPad, s));
-        cell_rows_kernel<true><<<gn, 256, 0, s>>>(pos_c, n, g, outside, table, nullptr, p.row_off, p.col);
+        if (one_pass && host_aux[1] <= cap_hint)
+            compact_rows_kernel<<<grid_of(32 * n), 256, 0, s>>>(scratch, cap_hint, p.row_off, n, p.col);
+        else  // a row longer than the slots (or no scratch): search again, writing in place
+            cell_rows_kernel<kWrite><<<gn, 256, 0, s>>>(pos_c, n, g, outside, table, nullptr, p.row_off,
+                                                        p.col, 0);
         IRR_CUDA_TRY(cudaGetLastError());
         *num_edges = (int64_t)(total / 2);
+        *longest = (uint32_t)host_aux[1];
         return cudaSuccess;
     };
     const cudaError_t e = run();
@@ -675,6 +736,7 @@ cudaError_t build_rows_by_cell(const float4* pos, int64_t n, float box, float cu
         if (p.row_off) cudaFreeAsync(p.row_off, s);
         if (p.col) cudaFreeAsync(p.col, s);
         *num_edges = 0;
+        *longest = 0;
         return e;
     }
     *out = p;
