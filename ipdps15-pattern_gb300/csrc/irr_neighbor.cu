@@ -708,7 +708,7 @@ cudaError_t build_rows_by_cell(const float4* pos, int64_t n, float box, float cu
         else
             cell_rows_kernel<kCount><<<gn, 256, 0, s>>>(pos_c, n, g, outside, table, p.row_off, nullptr,
                                                         nullptr, 0);
-        sum_u32_kernel<<<gn, 256, 0, s>>>(p.row_off, n, aux);
+        sum_u32_kernel<<<gn < 256 ? gn : 256, 256, 0, s>>>(p.row_off, n, aux);  // few atomics
         IRR_CUDA_TRY(cudaGetLastError());
         unsigned long long host_aux[2] = {0, 0};
         IRR_CUDA_TRY(cudaMemcpyAsync(host_aux, aux, sizeof(host_aux), cudaMemcpyDeviceToHost, s));
