@@ -20,6 +20,7 @@
 // dy*dy) + dz*dz) with every operation rounded.  Output: pairs (i, j), i < j,
 // sorted by i then j -- moldyn's loop order; miniMD lists the same pairs.
 #include <cmath>
+#include <type_traits>
 #include <vector>
 
 #include "irr_internal.cuh"
@@ -69,6 +70,14 @@ __device__ __forceinline__ bool list_pair_shifted(float4 a, float4 b, float sx, 
     const float dx = __fadd_rn(__fsub_rn(a.x, b.x), sx);
     const float dy = __fadd_rn(__fsub_rn(a.y, b.y), sy);
     const float dz = __fadd_rn(__fsub_rn(a.z, b.z), sz);
+    const float r2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+    return r2 <= cut2;
+}
+
+// list_pair_shifted with no shift (a cell reached without crossing the box).
+__device__ __forceinline__ bool list_pair_unshifted(float4 a, float4 b, float cut2)
+{
+    const float dx = __fsub_rn(a.x, b.x), dy = __fsub_rn(a.y, b.y), dz = __fsub_rn(a.z, b.z);
     const float r2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
     return r2 <= cut2;
 }
@@ -339,9 +348,13 @@ __global__ void cell_spans_kernel(const float4* __restrict__ pos_c, const uint32
 
 // Per cell, its 27 neighbour cells (periodic, at least 3 per axis, so all
 // distinct) in curve order: {run first, run end, image code}, the code 2 bits
-// per axis (1: +box, 2: -box; the shift list_pair_shifted adds).  One warp
+// per axis (1: +box, 2: -box; the shift list_pair_shifted adds) and kOwnCell
+// on the cell itself (whose run holds the node: the only one that needs a
+// self test).  One warp
 // per cell: lane k < 27 takes neighbour k, and a bitonic network over the
 // warp's 32 (key, lane) pairs (5 padding keys at the top) puts them in order.
+constexpr int kOwnCell = 64;
+
 __global__ void cell_stencil_kernel(const __grid_constant__ Grid g, const uint2* __restrict__ span,
                                     int64_t ncell, int4* table)
 {
@@ -359,7 +372,7 @@ __global__ void cell_stencil_kernel(const __grid_constant__ Grid g, const uint2*
             wrap_cell(y, g.nc[1], g.box, sy);
             wrap_cell(x, g.nc[0], g.box, sx);
             const int code = (sx > 0.f ? 1 : sx < 0.f ? 2 : 0) | (sy > 0.f ? 4 : sy < 0.f ? 8 : 0) |
-                             (sz > 0.f ? 16 : sz < 0.f ? 32 : 0);
+                             (sz > 0.f ? 16 : sz < 0.f ? 32 : 0) | (lane == 13 ? kOwnCell : 0);
             const uint2 sp = span[((int64_t)z * g.nc[1] + y) * g.nc[0] + x];
             key = hilbert10((uint32_t)x, (uint32_t)y, (uint32_t)z);
             ent = make_int4((int)sp.x, (int)sp.y, code, 0);
@@ -410,17 +423,40 @@ __device__ __forceinline__ void cell_rows_body(const float4* __restrict__ pos_c,
         const int4* st = table + (int64_t)cell_of(a, g) * 27;
         uint32_t m = 0;
         int32_t* out = MODE == kWrite ? col + row_off[t] : (MODE == kScratch ? col + t * (int64_t)cap : nullptr);
-        for (int k = 0; k < 27; k++) {
-            const int4 e = st[k];
-            const float sx = image_shift(e.z & 3, g.box), sy = image_shift((e.z >> 2) & 3, g.box),
-                        sz = image_shift((e.z >> 4) & 3, g.box);
+        // one run of candidates; SELF: the node's own run (skip q == t),
+        // SHIFT: a run across the box boundary (FAST only: elsewhere the cell
+        // decides no shift, and the rule's own test runs when !FAST)
+        auto run = [&](auto self, auto shift, uint32_t q0, uint32_t q1, float sx, float sy, float sz) {
+            constexpr bool SELF = decltype(self)::value, SHIFT = decltype(shift)::value;
 #pragma unroll 2
-            for (uint32_t q = (uint32_t)e.x; q < (uint32_t)e.y; q++) {
+            for (uint32_t q = q0; q < q1; q++) {
                 const float4 b = pos_c[q];
-                if (q != (uint32_t)t && pair_hit<FAST>(a, b, g, sx, sy, sz)) {
+                bool hit;
+                if (!FAST)
+                    hit = list_pair(a, b, g);
+                else if (SHIFT)
+                    hit = list_pair_shifted(a, b, sx, sy, sz, g.cut2);
+                else
+                    hit = list_pair_unshifted(a, b, g.cut2);
+                if (SELF) hit = hit && q != (uint32_t)t;
+                if (hit) {
                     if (MODE == kWrite || (MODE == kScratch && m < cap)) out[m] = (int32_t)q;
                     m++;
                 }
+            }
+        };
+        using T = std::true_type;
+        using F = std::false_type;
+        for (int k = 0; k < 27; k++) {
+            const int4 e = st[k];
+            const uint32_t q0 = (uint32_t)e.x, q1 = (uint32_t)e.y;
+            if (e.z & kOwnCell) {
+                run(T{}, F{}, q0, q1, 0.f, 0.f, 0.f);
+            } else if (FAST && e.z != 0) {
+                run(F{}, T{}, q0, q1, image_shift(e.z & 3, g.box), image_shift((e.z >> 2) & 3, g.box),
+                    image_shift((e.z >> 4) & 3, g.box));
+            } else {
+                run(F{}, F{}, q0, q1, 0.f, 0.f, 0.f);
             }
         }
         if (MODE != kWrite) deg[t] = m;
