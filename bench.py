@@ -501,9 +501,11 @@ def run_md(args):
 def run_served(args):
     """Config 5: Poisson arrivals at 200 jobs/s, sizes log-uniform in
     [2,048, 2,097,152] atoms, density 0.8442, cutoff 2.5, 50 velocity-Verlet
-    steps each, 120 GB admission budget; continuous batching vs serial, both
-    admitting in arrival order, and continuous batching admitting the smallest
-    waiting job first."""
+    steps each, 120 GB admission budget; continuous batching vs serial
+    execution (one job at a time through the partitioned force kernel) and
+    serial plain execution (one job at a time, every force by the plain
+    edge-parallel kernel), all admitting in arrival order, and continuous
+    batching admitting the smallest waiting job first."""
     import irregular_gb300 as irr
 
     out = {"leg": "served", "jobs": args.jobs, "arrival_rate_per_s": 200.0,
@@ -515,6 +517,7 @@ def run_served(args):
               steps_per_job=50, budget_bytes=120e9, seed=SEED + 6)
     runs = ((irr.IRR_SERVE_CONTINUOUS, irr.IRR_SERVE_FIFO, "continuous"),
             (irr.IRR_SERVE_SERIAL, irr.IRR_SERVE_FIFO, "serial"),
+            (irr.IRR_SERVE_SERIAL_PLAIN, irr.IRR_SERVE_FIFO, "serial_plain"),
             (irr.IRR_SERVE_CONTINUOUS, irr.IRR_SERVE_SJF, "continuous_sjf"))
     for mode, policy, name in runs:
         st, _ = irr.serve(num_jobs=args.jobs, mode=mode, policy=policy, arrival_rate=200.0,
@@ -524,6 +527,7 @@ def run_served(args):
                      "edges_per_s": st.edges_per_s, "jobs_done": int(st.jobs_done),
                      "max_resident": int(st.max_resident)}
     out["speedup_edges_per_s"] = out["continuous"]["edges_per_s"] / out["serial"]["edges_per_s"]
+    out["speedup_vs_serial_plain"] = out["continuous"]["edges_per_s"] / out["serial_plain"]["edges_per_s"]
     print(json.dumps(out), flush=True)
     return 0
 

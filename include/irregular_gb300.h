@@ -328,7 +328,11 @@ typedef struct irr_md_config {
                        /* every this many rebuilds the atoms are re-sorted  */
                        /* along the curve (10; 0 or 1: every rebuild).      */
                        /* Larger boxes re-sort by cell at every rebuild.    */
-    int reserved[7];
+    int exec_plain;    /* 1: forces by the plain edge-parallel kernel over  */
+                       /* the half list (atomics: the reference's per-edge  */
+                       /* semantics, run to run not bitwise); 0 (default):  */
+                       /* the partitioned owner-computes kernel             */
+    int reserved[6];
 } irr_md_config;
 
 typedef struct irr_md_info {
@@ -368,9 +372,11 @@ IRR_API int irr_md_get_info(const irr_md *m, irr_md_info *info);
  * while their estimated device memory fits budget_bytes; every tick advances
  * every resident job one step with ONE batched force launch over all of
  * them; finished jobs leave and free their memory.  IRR_SERVE_SERIAL runs the
- * same jobs one at a time.  A job's trajectory is bitwise the same alone
- * (only_job = its index) and in the mix. */
-enum irr_serve_mode { IRR_SERVE_CONTINUOUS = 0, IRR_SERVE_SERIAL = 1 };
+ * same jobs one at a time; IRR_SERVE_SERIAL_PLAIN one at a time with every
+ * force evaluation by the plain edge-parallel kernel (irr_md_config
+ * exec_plain).  A job's trajectory is bitwise the same alone (only_job = its
+ * index) and in the mix. */
+enum irr_serve_mode { IRR_SERVE_CONTINUOUS = 0, IRR_SERVE_SERIAL = 1, IRR_SERVE_SERIAL_PLAIN = 2 };
 /* Which waiting job a free slot admits: the earliest arrival, or the smallest
  * job (shortest-job-first: the lowest mean latency, the largest jobs last). */
 enum irr_serve_policy { IRR_SERVE_FIFO = 0, IRR_SERVE_SJF = 1 };

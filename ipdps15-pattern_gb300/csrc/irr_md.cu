@@ -62,6 +62,31 @@ __global__ void kick_drift_kernel(double* __restrict__ x, double* __restrict__ v
         md_kick_drift_atom<KICKS>(x, v, f, i, dt, L, pos4);
 }
 
+// cnt[t] = entries of row t with a column above t (rows ascending: a suffix).
+__global__ void half_count_kernel(const uint32_t* __restrict__ row_off, const int32_t* __restrict__ col,
+                                  int64_t n, uint32_t* __restrict__ cnt)
+{
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t b = row_off[t], e = row_off[t + 1];
+        uint32_t k = b;
+        while (k < e && col[k] <= (int32_t)t) k++;
+        cnt[t] = e - k;
+    }
+}
+
+// half[off[t] ..] = (t, j) for the entries j > t of row t.
+__global__ void half_write_kernel(const uint32_t* __restrict__ row_off, const int32_t* __restrict__ col,
+                                  int64_t n, const uint32_t* __restrict__ off, int2* __restrict__ half)
+{
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t e = row_off[t + 1];
+        const uint32_t k0 = e - (off[t + 1] - off[t]);
+        for (uint32_t k = k0; k < e; k++) half[off[t] + (k - k0)] = make_int2((int)t, col[k]);
+    }
+}
+
 __global__ void kick_kernel(double* __restrict__ v, const float4* __restrict__ f, int64_t n,
                             double dt)
 {
@@ -246,6 +271,8 @@ void free_part(irr_md* m, cudaStream_t s)
     if (m->d_items) cudaFreeAsync(m->d_items, s);
     m->d_items = nullptr;
     m->num_items = 0;
+    if (m->half) cudaFreeAsync(m->half, s);
+    m->half = nullptr;
 }
 
 }  // namespace
@@ -339,6 +366,18 @@ int md_rebuild(irr_md* m)
     d.n = m->n;
     m->inst = d;
     MD_CUDA(m, cudaMemcpyAsync(m->d_inst, &d, sizeof(d), cudaMemcpyHostToDevice, s), "instance");
+    if (m->cfg.exec_plain && e > 0) {
+        // the plain kernel's edge list: each pair once, (i, j) with i < j
+        uint32_t* off = nullptr;
+        MD_CUDA(m, irr_malloc_async(&off, sizeof(uint32_t) * (m->n + 1), s), "half list");
+        MD_CUDA(m, irr_malloc_async(&m->half, sizeof(int2) * e, s), "half list");
+        half_count_kernel<<<grid_of(m->n), 256, 0, s>>>(m->part.row_off, m->part.col, m->n, off);
+        MD_CUDA(m, cudaMemsetAsync(off + m->n, 0, sizeof(uint32_t), s), "half list");
+        MD_CUDA(m, scan_exclusive_u32(off, off, m->n + 1, nullptr, s), "half list");
+        half_write_kernel<<<grid_of(m->n), 256, 0, s>>>(m->part.row_off, m->part.col, m->n, off, m->half);
+        MD_CUDA(m, cudaGetLastError(), "half list");
+        cudaFreeAsync(off, s);
+    }
     MD_CUDA(m, cudaStreamSynchronize(s), "rebuild");
     m->edges = e;
     m->rebuilds++;
@@ -348,6 +387,11 @@ int md_rebuild(irr_md* m)
 
 int md_forces(irr_md* m)
 {
+    if (m->cfg.exec_plain) {
+        MD_CUDA(m, cudaMemsetAsync(m->force, 0, sizeof(float4) * m->n, m->stream), "clear forces");
+        MD_CUDA(m, launch_plain(m->pos4, m->half, m->edges, m->force, m->law, m->stream), "plain kernel");
+        return IRR_OK;
+    }
     MD_CUDA(m, cudaMemsetAsync(m->d_queue, 0, sizeof(int), m->stream), "queue");
     MD_CUDA(m, launch_tiled(m->shape, m->d_inst, m->d_items, m->num_items, m->d_queue,
                             m->sms * kCtasPerSm, m->d_status, m->stream, &m->inst, 1), "force kernel");
@@ -435,6 +479,7 @@ int irr_md_create(const irr_md_config* cfg, const double* pos, const double* vel
         cfg->rebuild_every < 1)
         return IRR_ERR_ARG;
     if (2.0 * (cfg->cutforce + cfg->skin) > cfg->side) return IRR_ERR_ARG;  // one image per pair
+    if (cfg->exec_plain != 0 && cfg->exec_plain != 1) return IRR_ERR_ARG;
     if (n > 0x7fffffffLL) return IRR_ERR_CAPACITY;
     irr_md* m = new (std::nothrow) irr_md();
     if (!m) return IRR_ERR_NOMEM;

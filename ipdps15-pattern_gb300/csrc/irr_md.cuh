@@ -118,6 +118,7 @@ struct irr_md {
     int64_t rebuilds = 0;
     int64_t since_rebuild = 0;
     uint32_t row_cap = 0;      // per-node slots for the next rebuild's one-pass search (0: two passes)
+    int2* half = nullptr;      // exec_plain: the half list (i < j, execution order) of the rows
 };
 
 

@@ -253,35 +253,42 @@ struct ForceBatch {
 // are folded into the next tick's kick-drift), queued on s.
 int force_and_kick(const std::vector<irr_md*>& ms, const std::vector<irr_md*>& retiring,
                    ForceBatch& B, const TiledShape& shape, int* d_queue, int* d_status, int sms,
-                   double dt, cudaStream_t s)
+                   double dt, cudaStream_t s, bool plain)
 {
     if (ms.empty()) return IRR_OK;
-    int blocks = 0;
-    int64_t nitems = 0;
-    if (!upload_tick_jobs(ms, B.jobs, s, &blocks, &nitems) || !B.insts.reserve(ms.size()))
-        return IRR_ERR_CUDA;
-    for (size_t k = 0; k < ms.size(); k++) B.insts.h[k] = md_instance(ms[k]);
-    if ((size_t)nitems > B.items_cap) {
-        if (B.d_items) cudaFree(B.d_items);
-        B.items_cap = (size_t)nitems * 2;
-        if (cudaMalloc(&B.d_items, sizeof(WorkItem) * B.items_cap) != cudaSuccess) {
-            B.d_items = nullptr;
-            B.items_cap = 0;
-            return IRR_ERR_NOMEM;
+    if (plain) {  // each job by its own plain force launch
+        for (irr_md* m : ms) {
+            const int frc = md_forces(m);
+            if (frc != IRR_OK) return frc;
         }
+    } else {
+        int blocks = 0;
+        int64_t nitems = 0;
+        if (!upload_tick_jobs(ms, B.jobs, s, &blocks, &nitems) || !B.insts.reserve(ms.size()))
+            return IRR_ERR_CUDA;
+        for (size_t k = 0; k < ms.size(); k++) B.insts.h[k] = md_instance(ms[k]);
+        if ((size_t)nitems > B.items_cap) {
+            if (B.d_items) cudaFree(B.d_items);
+            B.items_cap = (size_t)nitems * 2;
+            if (cudaMalloc(&B.d_items, sizeof(WorkItem) * B.items_cap) != cudaSuccess) {
+                B.d_items = nullptr;
+                B.items_cap = 0;
+                return IRR_ERR_NOMEM;
+            }
+        }
+        if (cudaMemcpyAsync(B.insts.d, B.insts.h, sizeof(InstDesc) * ms.size(), cudaMemcpyHostToDevice, s) !=
+            cudaSuccess)
+            return IRR_ERR_CUDA;
+        if (nitems > 0) {
+            const int64_t want = (nitems + 255) / 256;
+            tick_items_kernel<<<(unsigned)(want < 4096 ? want : 4096), 256, 0, s>>>(B.jobs.d, (int)ms.size(),
+                                                                                    nitems, B.d_items);
+        }
+        if (cudaGetLastError() != cudaSuccess || cudaMemsetAsync(d_queue, 0, sizeof(int), s) != cudaSuccess ||
+            launch_tiled(shape, B.insts.d, B.d_items, (int)nitems, d_queue, sms * kCtasPerSm, d_status, s,
+                         B.insts.h, (int)ms.size()) != cudaSuccess)
+            return IRR_ERR_CUDA;
     }
-    if (cudaMemcpyAsync(B.insts.d, B.insts.h, sizeof(InstDesc) * ms.size(), cudaMemcpyHostToDevice, s) !=
-        cudaSuccess)
-        return IRR_ERR_CUDA;
-    if (nitems > 0) {
-        const int64_t want = (nitems + 255) / 256;
-        tick_items_kernel<<<(unsigned)(want < 4096 ? want : 4096), 256, 0, s>>>(B.jobs.d, (int)ms.size(),
-                                                                                nitems, B.d_items);
-    }
-    if (cudaGetLastError() != cudaSuccess || cudaMemsetAsync(d_queue, 0, sizeof(int), s) != cudaSuccess ||
-        launch_tiled(shape, B.insts.d, B.d_items, (int)nitems, d_queue, sms * kCtasPerSm, d_status, s,
-                     B.insts.h, (int)ms.size()) != cudaSuccess)
-        return IRR_ERR_CUDA;
     if (retiring.empty()) return IRR_OK;
     int kblocks = 0;
     int64_t unused = 0;
@@ -457,6 +464,8 @@ int irr_serve_run(const irr_serve_config* cfg, irr_serve_stats* st, irr_serve_jo
         return IRR_ERR_ARG;
     if (cfg->only_job >= cfg->num_jobs) return IRR_ERR_ARG;
     if (cfg->policy != IRR_SERVE_FIFO && cfg->policy != IRR_SERVE_SJF) return IRR_ERR_ARG;
+    if (cfg->mode != IRR_SERVE_CONTINUOUS && cfg->mode != IRR_SERVE_SERIAL && cfg->mode != IRR_SERVE_SERIAL_PLAIN)
+        return IRR_ERR_ARG;
     memset(st, 0, sizeof(*st));
     if (cudaSetDevice(cfg->device) != cudaSuccess) {
         cudaGetLastError();
@@ -480,7 +489,9 @@ int irr_serve_run(const irr_serve_config* cfg, irr_serve_stats* st, irr_serve_jo
     } else {
         for (int k = 0; k < cfg->num_jobs; k++) order.push_back(k);
     }
-    const int max_res = cfg->mode == IRR_SERVE_SERIAL ? 1 : cfg->max_resident;
+    const bool serial = cfg->mode == IRR_SERVE_SERIAL || cfg->mode == IRR_SERVE_SERIAL_PLAIN;
+    const bool plain = cfg->mode == IRR_SERVE_SERIAL_PLAIN;
+    const int max_res = serial ? 1 : cfg->max_resident;
     std::vector<double> latency;
     std::vector<Live> live;
     Pinned<TickJob> tick_a;        // every resident job (the kick-drift)
@@ -518,7 +529,7 @@ int irr_serve_run(const irr_serve_config* cfg, irr_serve_stats* st, irr_serve_jo
     }
     const auto t0 = std::chrono::steady_clock::now();
     auto now = [&]() { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); };
-    const unsigned workers = cfg->mode == IRR_SERVE_SERIAL
+    const unsigned workers = serial
                                  ? 1u
                                  : std::max(1u, std::min(std::thread::hardware_concurrency(), 16u));
     cudaEvent_t ev_kd = nullptr;
@@ -584,7 +595,7 @@ int irr_serve_run(const irr_serve_config* cfg, irr_serve_stats* st, irr_serve_jo
             creating.push_back(std::make_unique<Admission>());
             Admission* a = creating.back().get();
             a->id = id;
-            a->worker = std::thread([a, &jobs, &req, cfg]() {
+            a->worker = std::thread([a, &jobs, &req, cfg, plain]() {
                 cudaSetDevice(cfg->device);
                 const JobSpec& js = jobs[a->id];
                 irr_md_config mc;
@@ -595,6 +606,7 @@ int irr_serve_run(const irr_serve_config* cfg, irr_serve_stats* st, irr_serve_jo
                 mc.skin = cfg->skin;
                 mc.side = js.side;
                 mc.rebuild_every = cfg->rebuild_every;
+                mc.exec_plain = plain ? 1 : 0;
                 a->rc = irr_md_create(&mc, req[a->id].pos, req[a->id].vel, js.atoms, &a->made);
                 a->done.store(true, std::memory_order_release);
             });
@@ -643,13 +655,14 @@ int irr_serve_run(const irr_serve_config* cfg, irr_serve_stats* st, irr_serve_jo
             due_rc[i] = md_rebuild(m);
             m->stream = s;
         });
-        const int krc = force_and_kick(keep, keep_retiring, keep_b, shape, d_queue, d_status, sms, cfg->dt, s);
+        const int krc =
+            force_and_kick(keep, keep_retiring, keep_b, shape, d_queue, d_status, sms, cfg->dt, s, plain);
         for (auto& th : rebuilding) th.join();
         if (krc != IRR_OK) rc = krc;
         for (int r : due_rc)
             if (r != IRR_OK && rc == IRR_OK) rc = r;
         if (rc) break;
-        rc = force_and_kick(due, due_retiring, due_b, shape, d_queue, d_status, sms, cfg->dt, s);
+        rc = force_and_kick(due, due_retiring, due_b, shape, d_queue, d_status, sms, cfg->dt, s, plain);
         if (rc) break;
         for (auto& L : live) {
             L.pair_evals += (double)L.md->edges;

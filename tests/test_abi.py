@@ -55,7 +55,8 @@ def test_status_strings_and_defaults(built_lib):
 
 def test_serve_and_md_config_defaults_and_validation(built_lib):
     """New fields sit in the configs' reserved space with their defaults, and
-    a bad admission policy is refused before any device call."""
+    a bad admission policy, serving mode or MD force path is refused before
+    any device call."""
     import ctypes as C
     import irregular_gb300 as irr
     L = irr.load()
@@ -64,12 +65,21 @@ def test_serve_and_md_config_defaults_and_validation(built_lib):
     assert sc.policy == irr.IRR_SERVE_FIFO and sc.max_resident == 64
     mc = irr.MDConfig()
     L.irr_md_config_default(C.byref(mc))
-    assert mc.reorder_every == 10 and mc.rebuild_every == 20
+    assert mc.reorder_every == 10 and mc.rebuild_every == 20 and mc.exec_plain == 0
     # the sizes the structs had before the new fields took reserved slots
     assert C.sizeof(irr.ServeConfig) == 144 and C.sizeof(irr.MDConfig) == 72
-    with pytest.raises(irr.IrregularError) as ei:
-        irr.serve(policy=7)
-    assert ei.value.status == irr.IRR_ERR_ARG
+    for bad in (dict(policy=7), dict(mode=9)):
+        with pytest.raises(irr.IrregularError) as ei:
+            irr.serve(**bad)
+        assert ei.value.status == irr.IRR_ERR_ARG
+    # an MD force path other than 0 (partitioned) or 1 (plain)
+    import numpy as np
+    mc.side, mc.exec_plain = 10.0, 7
+    pos = np.zeros((4, 3))
+    h = C.c_void_p()
+    rc = L.irr_md_create(C.byref(mc), pos.ctypes.data_as(C.c_void_p), pos.ctypes.data_as(C.c_void_p),
+                         4, C.byref(h))
+    assert rc == irr.IRR_ERR_ARG and not h.value
 
 
 def test_create_rejects_bad_config_without_crashing(built_lib):

@@ -58,6 +58,34 @@ def test_short_trajectory_matches_fp64_reference(built_lib, oracle_lib, cells, r
     md.close()
 
 
+@pytest.mark.parametrize("cells", [4, 12])
+def test_plain_force_path_matches_fp64(built_lib, oracle_lib, cells):
+    """exec_plain: the forces by the plain edge-parallel kernel over the half
+    list taken from the rows (atomics), the same bound against FP64 and the
+    same short trajectory as the reference MD."""
+    import irregular_gb300 as irr
+    O = oracle_lib
+    pos, vel, side = system(cells=cells)
+    md = irr.MD(pos, vel, side, exec_plain=True)
+    f = md.forces()
+    p32 = pos.astype(np.float32)
+    edges = O.neighbor_half_list(p32, float(np.float32(side)), np.float32(2.8 ** 2))
+    f64, _ = O.lj_reduce_f64(p32.astype(np.float64), edges, O.lj_param(2.5 ** 2, side, True))
+    f64 *= 48.0
+    assert np.abs(f - f64).max() / np.abs(f64).max() <= 1e-6
+    assert md.info().num_edges == edges.shape[0]
+    md.close()
+    md = irr.MD(pos, vel, side, dt=0.005, rebuild_every=20, exec_plain=True)
+    md.run(25)
+    gp, gv = md.state()
+    rp, rv, _, _ = O.md_run(pos, vel, side, 2.5, 0.3, 0.005, 25, 20)
+    dx = gp - rp
+    dx -= side * np.round(dx / side)
+    assert np.abs(dx).max() <= 1e-5
+    assert np.abs(gv - rv).max() <= 1e-4
+    md.close()
+
+
 def test_energy_and_momentum_conservation(built_lib):
     import irregular_gb300 as irr
     pos, vel, side = system(cells=8)

@@ -59,3 +59,17 @@ def test_shortest_job_first_admission(built_lib):
     atoms = [sjf[k].atoms for k in by_admit]
     assert atoms[1:] == sorted(atoms[1:])  # the first admission may precede the last arrival
     assert [j.state_hash for j in sjf] == [j.state_hash for j in fifo]
+
+
+def test_serial_plain_schedule(built_lib):
+    """IRR_SERVE_SERIAL_PLAIN: one job at a time, every force by the plain
+    edge-parallel kernel (atomics: another summation order, so the final
+    energies agree with the partitioned schedule's to FP32 reordering, not
+    bit for bit)."""
+    import irregular_gb300 as irr
+    stats, plain = irr.serve(mode=irr.IRR_SERVE_SERIAL_PLAIN, **SMALL)
+    assert stats.jobs_done == SMALL["num_jobs"] and stats.max_resident == 1
+    _, serial = irr.serve(mode=irr.IRR_SERVE_SERIAL, **SMALL)
+    for p, s in zip(plain, serial):
+        assert p.status == 0 and p.edges == s.edges
+        assert abs(p.energy - s.energy) <= 1e-5 * abs(s.energy)
