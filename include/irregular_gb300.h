@@ -332,7 +332,10 @@ typedef struct irr_md_config {
                        /* the half list (atomics: the reference's per-edge  */
                        /* semantics, run to run not bitwise); 0 (default):  */
                        /* the partitioned owner-computes kernel             */
-    int reserved[6];
+    int row_slots;     /* per-atom slots of the one-pass neighbour search   */
+                       /* (0: the last rebuild's longest row + 25 % + 8; a  */
+                       /* longer row falls back to counting first), 0..4096 */
+    int reserved[5];
 } irr_md_config;
 
 typedef struct irr_md_info {

@@ -295,7 +295,7 @@ int md_rebuild(irr_md* m)
     // last build's longest row let one search pass write them.
     uint32_t longest = 0;
     cudaError_t pe = build_rows_by_cell(m->pos4, m->n, (float)m->cfg.side, list_cut2, &p, &e, &longest,
-                                        m->row_cap, s);
+                                        m->cfg.row_slots > 0 ? (uint32_t)m->cfg.row_slots : m->row_cap, s);
     if (pe == cudaSuccess) m->row_cap = (longest + longest / 4 + 8 + 7) & ~7u;
     bool reorder = true;
     if (pe == cudaErrorNotSupported) {
@@ -480,6 +480,7 @@ int irr_md_create(const irr_md_config* cfg, const double* pos, const double* vel
         return IRR_ERR_ARG;
     if (2.0 * (cfg->cutforce + cfg->skin) > cfg->side) return IRR_ERR_ARG;  // one image per pair
     if (cfg->exec_plain != 0 && cfg->exec_plain != 1) return IRR_ERR_ARG;
+    if (cfg->row_slots < 0 || cfg->row_slots > 4096) return IRR_ERR_ARG;
     if (n > 0x7fffffffLL) return IRR_ERR_CAPACITY;
     irr_md* m = new (std::nothrow) irr_md();
     if (!m) return IRR_ERR_NOMEM;

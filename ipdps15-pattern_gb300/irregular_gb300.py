@@ -67,7 +67,8 @@ class Info(C.Structure):
 class MDConfig(C.Structure):
     _fields_ = [("device", C.c_int), ("rebuild_every", C.c_int), ("dt", C.c_double),
                 ("cutforce", C.c_double), ("skin", C.c_double), ("side", C.c_double),
-                ("reorder_every", C.c_int), ("exec_plain", C.c_int), ("reserved", C.c_int * 6)]
+                ("reorder_every", C.c_int), ("exec_plain", C.c_int), ("row_slots", C.c_int),
+                ("reserved", C.c_int * 5)]
 
 
 class MDInfo(C.Structure):
@@ -522,7 +523,8 @@ class MD:
 
     def __init__(self, pos, vel, side: float, dt: float = 0.005, cutforce: float = 2.5,
                  skin: float = 0.3, rebuild_every: int = 20, device: int = 0,
-                 reorder_every: Optional[int] = None, exec_plain: bool = False):
+                 reorder_every: Optional[int] = None, exec_plain: bool = False,
+                 row_slots: int = 0):
         L = load()
         cfg = MDConfig()
         L.irr_md_config_default(C.byref(cfg))
@@ -531,6 +533,7 @@ class MD:
         if reorder_every is not None:
             cfg.reorder_every = reorder_every
         cfg.exec_plain = 1 if exec_plain else 0
+        cfg.row_slots = int(row_slots)
         p = np.ascontiguousarray(pos, np.float64).reshape(-1, 3)
         v = np.ascontiguousarray(vel, np.float64).reshape(-1, 3)
         self.n = p.shape[0]

@@ -55,8 +55,8 @@ def test_status_strings_and_defaults(built_lib):
 
 def test_serve_and_md_config_defaults_and_validation(built_lib):
     """New fields sit in the configs' reserved space with their defaults, and
-    a bad admission policy, serving mode or MD force path is refused before
-    any device call."""
+    a bad admission policy, serving mode, MD force path or slot count is
+    refused before any device call."""
     import ctypes as C
     import irregular_gb300 as irr
     L = irr.load()
@@ -65,7 +65,7 @@ def test_serve_and_md_config_defaults_and_validation(built_lib):
     assert sc.policy == irr.IRR_SERVE_FIFO and sc.max_resident == 64
     mc = irr.MDConfig()
     L.irr_md_config_default(C.byref(mc))
-    assert mc.reorder_every == 10 and mc.rebuild_every == 20 and mc.exec_plain == 0
+    assert mc.reorder_every == 10 and mc.rebuild_every == 20 and mc.exec_plain == 0 and mc.row_slots == 0
     # the sizes the structs had before the new fields took reserved slots
     assert C.sizeof(irr.ServeConfig) == 144 and C.sizeof(irr.MDConfig) == 72
     for bad in (dict(policy=7), dict(mode=9)):
@@ -77,6 +77,10 @@ def test_serve_and_md_config_defaults_and_validation(built_lib):
     mc.side, mc.exec_plain = 10.0, 7
     pos = np.zeros((4, 3))
     h = C.c_void_p()
+    rc = L.irr_md_create(C.byref(mc), pos.ctypes.data_as(C.c_void_p), pos.ctypes.data_as(C.c_void_p),
+                         4, C.byref(h))
+    assert rc == irr.IRR_ERR_ARG and not h.value
+    mc.exec_plain, mc.row_slots = 0, 5000
     rc = L.irr_md_create(C.byref(mc), pos.ctypes.data_as(C.c_void_p), pos.ctypes.data_as(C.c_void_p),
                          4, C.byref(h))
     assert rc == irr.IRR_ERR_ARG and not h.value

@@ -86,6 +86,23 @@ def test_plain_force_path_matches_fp64(built_lib, oracle_lib, cells):
     md.close()
 
 
+def test_neighbour_slots_overflow_gives_the_same_trajectory(built_lib):
+    """row_slots = 8 (rows hold ~78): every rebuild's one-pass search
+    overflows its slots and falls back to counting and writing in place; the
+    rows, and so the trajectory, are bitwise those of the automatic slots."""
+    import irregular_gb300 as irr
+    pos, vel, side = system(cells=12)
+    states = []
+    for slots in (0, 8):
+        md = irr.MD(pos, vel, side, dt=0.005, rebuild_every=10, row_slots=slots)
+        md.run(45)  # the first build and four rebuilds
+        assert md.info().rebuilds == 5
+        states.append(md.state())
+        md.close()
+    for a, b in zip(states[0], states[1]):
+        assert np.array_equal(a.view(np.uint64), b.view(np.uint64))
+
+
 def test_energy_and_momentum_conservation(built_lib):
     import irregular_gb300 as irr
     pos, vel, side = system(cells=8)
