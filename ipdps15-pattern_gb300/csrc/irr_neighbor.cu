@@ -19,6 +19,14 @@
 // float, wrapped once by +-box when |d| > box/2 (periodic), r2 = ((dx*dx +
 // dy*dy) + dz*dz) with every operation rounded.  Output: pairs (i, j), i < j,
 // sorted by i then j -- moldyn's loop order; miniMD lists the same pairs.
+// With at least 5 cells per axis and every position inside the periodic box,
+// a neighbour cell decides the image of all its partners (list_pair_shifted).
+//
+// The MD rebuild takes another route (build_rows_by_cell): the nodes are
+// re-sorted by the Hilbert index of their cell, and each node's full row is
+// written by one search over its 27 cells visited in curve order -- ascending
+// by construction, so the rows need neither the pair list, nor atomic row
+// cursors, nor a sort.
 #include <cmath>
 #include <type_traits>
 #include <vector>
