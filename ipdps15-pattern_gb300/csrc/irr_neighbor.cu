@@ -436,7 +436,7 @@ __device__ __forceinline__ void cell_rows_body(const float4* __restrict__ pos_c,
         // decides no shift, and the rule's own test runs when !FAST)
         auto run = [&](auto self, auto shift, uint32_t q0, uint32_t q1, float sx, float sy, float sz) {
             constexpr bool SELF = decltype(self)::value, SHIFT = decltype(shift)::value;
-#pragma unroll 2
+#pragma unroll 4
             for (uint32_t q = q0; q < q1; q++) {
                 const float4 b = pos_c[q];
                 bool hit;
