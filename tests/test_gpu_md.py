@@ -103,6 +103,40 @@ def test_neighbour_slots_overflow_gives_the_same_trajectory(built_lib):
         assert np.array_equal(a.view(np.uint64), b.view(np.uint64))
 
 
+def test_dilute_gas_takes_the_half_list_path(built_lib, oracle_lib):
+    """A gas at density 0.03: 16 cells per axis but more cells than atoms, so
+    the rebuild takes the half-stencil pair list and the partition instead of
+    rows written in cell order; the list and the forces (per atom, against the
+    sum of its terms' magnitudes) match the FP64 oracle, before and after a
+    rebuild."""
+    import irregular_gb300 as irr
+    from helpers import TOL_PERNODE_F64, scaled_error
+    O = oracle_lib
+    # a simple cubic lattice (spacing 3.22 > the 2.8 list cutoff) with a 0.35
+    # jitter: ~2,000 pairs inside 2.8, none closer than ~1.1
+    a, m = (1 / 0.03) ** (1 / 3), 16
+    side = float(np.float32(m * a))
+    grid = np.stack(np.meshgrid(*(np.arange(m),) * 3, indexing="ij"), -1).reshape(-1, 3) * a
+    rng = np.random.Generator(np.random.PCG64(41))
+    pos = (grid + rng.normal(0, 0.35, grid.shape)) % side
+    n = pos.shape[0]
+    assert int(side / 2.8) ** 3 > n
+    vel = rng.normal(0, 0.5, (n, 3))
+    md = irr.MD(pos, vel, side, dt=0.002, rebuild_every=5)
+    try:
+        for steps in (0, 10):  # the initial build, then right after the second rebuild
+            if steps:
+                md.run(steps)
+            pos, _ = md.state()
+            q32 = pos.astype(np.float32)
+            edges = O.neighbor_half_list(q32, float(np.float32(side)), np.float32(2.8 ** 2))
+            assert md.info().num_edges == edges.shape[0] > 0
+            f64, sabs = O.lj_reduce_f64(q32.astype(np.float64), edges, O.lj_param(2.5 ** 2, side, True))
+            assert scaled_error(md.forces(), 48.0 * f64, 48.0 * sabs) <= TOL_PERNODE_F64
+    finally:
+        md.close()
+
+
 def test_energy_and_momentum_conservation(built_lib):
     import irregular_gb300 as irr
     pos, vel, side = system(cells=8)
