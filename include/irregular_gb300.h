@@ -324,10 +324,11 @@ typedef struct irr_md_config {
     double cutforce;   /* force cutoff (2.5)                                */
     double skin;       /* neighbour skin (0.3)                              */
     double side;       /* periodic box side; > 2 (cutforce + skin)          */
-    int reorder_every; /* boxes of fewer than 3 list-cutoff cells per axis: */
-                       /* every this many rebuilds the atoms are re-sorted  */
-                       /* along the curve (10; 0 or 1: every rebuild).      */
-                       /* Larger boxes re-sort by cell at every rebuild.    */
+    int reorder_every; /* boxes with fewer than 3 list-cutoff cells on an   */
+                       /* axis, or more cells than atoms: every this many   */
+                       /* rebuilds the atoms are re-sorted along the curve  */
+                       /* (10; 0 or 1: every rebuild).  Other boxes re-sort */
+                       /* by cell at every rebuild.                         */
     int exec_plain;    /* 1: forces by the plain edge-parallel kernel over  */
                        /* the half list (atomics: the reference's per-edge  */
                        /* semantics, run to run not bitwise); 0 (default):  */
