@@ -235,8 +235,8 @@ IRR_API int irr_get_partition(irr_handle *h, int32_t *perm, int64_t *row_off, in
  * 1-based neighbour ids, read up to the first value <= 0; only neighbours
  * j >= i are kept, so each pair is listed once, and their count must equal
  * the header's (else IRR_ERR_STATE).  Pairs are written to `edges` (at most
- * `cap`; NULL to count), 1-based when one_based != 0 as the reference's build
- * returns them, else 0-based.
+ * `cap`; NULL to count), 0-based as moldyn's build of the reader returns them
+ * (misc.c defines CSTYLE), or 1-based when one_based != 0.
  * irr_read_coords: num_nodes whitespace-separated "x y z" triples
  * (moldyn/misc.c:224-246); a different count is IRR_ERR_STATE.
  * irr_write_graph / irr_write_coords: the same formats from a 0-based half
@@ -447,16 +447,21 @@ IRR_API int irr_serve_run(const irr_serve_config *cfg, irr_serve_stats *stats,
  * an application that has already reserved the GPU's memory for its own
  * pool, or a latency-bound loop where cudaMalloc/cudaFree (which may
  * synchronise the device) are not acceptable.  It calls no allocator: its
- * scratch is a fixed device array inside this library, held by every GPU
- * that loads the library until the process exits.
- *   d_pos: n device records of pos_elm bytes (12: float xyz, 16: float xyzw);
- *   d_perm: n int32 of device output;  n <= IRR_MORTON_STATIC_MAX_NODES, else
+ * scratch is a fixed device array inside this library of
+ * IRR_MORTON_STATIC_SCRATCH_BYTES (about 12.3 MiB), held by every GPU that
+ * loads the library until the process exits.
+ *   d_pos: n device records of pos_elm bytes (12: float xyz, 16: float xyzw),
+ *   on a 4-byte boundary; d_perm: n int32 of device output, on a 4-byte
+ *   boundary (else IRR_ERR_ARG);  n <= IRR_MORTON_STATIC_MAX_NODES, else
  *   IRR_ERR_CAPACITY.
- * The first call on a device looks up the array's device address (make that
- * call before any stream capture).  Every call shares the one array: calls
- * that overlap on the GPU race, so order them (one stream, or events).
- * Enqueued on `stream`; the host does not wait. */
+ * Each call on a stream that is not capturing looks up the array's device
+ * address (so a device reset is picked up); a call on a capturing stream uses
+ * the last look-up on that device: make the first call on a device before any
+ * stream capture.  Every call shares the one array: calls that overlap on the
+ * GPU race, so order them (one stream, or events).  Enqueued on `stream`; the
+ * host does not wait.  The caller's current device is restored on return. */
 #define IRR_MORTON_STATIC_MAX_NODES 1048576
+#define IRR_MORTON_STATIC_SCRATCH_BYTES 12886272
 IRR_API int irr_morton_order_static(int device, void *stream, const void *d_pos, int pos_elm,
                                     int64_t n, int32_t *d_perm);
 

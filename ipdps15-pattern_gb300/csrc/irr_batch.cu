@@ -228,7 +228,8 @@ int irr_batch_create(int device, irr_batch** out)
     irr_batch* b = new (std::nothrow) irr_batch();
     if (!b) return IRR_ERR_NOMEM;
     b->device = device;
-    if (cudaSetDevice(device) != cudaSuccess ||
+    DeviceGuard dev_guard(device);
+    if (!dev_guard.ok() ||
         cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
         cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaMalloc(&b->d_queue, sizeof(int)) != cudaSuccess ||
@@ -250,7 +251,7 @@ int irr_batch_create(int device, irr_batch** out)
 int irr_batch_destroy(irr_batch* b)
 {
     if (!b) return IRR_ERR_ARG;
-    cudaSetDevice(b->device);
+    DeviceGuard dev_guard(b->device);
     if (b->stream) cudaStreamSynchronize(b->stream);
     drop_graph(b);
     if (b->d_insts) cudaFree(b->d_insts);
@@ -295,7 +296,7 @@ int irr_batch_finalize(irr_batch* b, int autotune_shape)
     if (!b) return IRR_ERR_ARG;
     if (b->finalized) return IRR_OK;
     if (b->handles.empty()) return bfail(b, IRR_ERR_STATE, "empty batch");
-    cudaSetDevice(b->device);
+    DeviceGuard dev_guard(b->device);
     b->nodes = b->edges = 0;
     for (irr_handle* h : b->handles) {
         cudaStreamSynchronize(h->stream);
@@ -313,7 +314,7 @@ int irr_batch_step(irr_batch* b)
 {
     if (!b) return IRR_ERR_ARG;
     if (!b->finalized) return bfail(b, IRR_ERR_STATE, "irr_batch_step before irr_batch_finalize");
-    cudaSetDevice(b->device);
+    DeviceGuard dev_guard(b->device);
     if (b->exec) {
         B_CUDA(b, cudaGraphLaunch(b->exec, b->stream), "graph replay");
         return IRR_OK;
@@ -326,7 +327,7 @@ int irr_batch_capture(irr_batch* b)
     if (!b) return IRR_ERR_ARG;
     if (!b->finalized) return bfail(b, IRR_ERR_STATE, "irr_batch_capture before irr_batch_finalize");
     if (b->stream == nullptr) return bfail(b, IRR_ERR_STATE, "capture needs a non-default stream");
-    cudaSetDevice(b->device);
+    DeviceGuard dev_guard(b->device);
     drop_graph(b);
     int rc = launch_step(b, b->shape);  // sets the kernel's attributes outside the capture
     if (rc) return rc;
@@ -348,7 +349,7 @@ int irr_batch_capture(irr_batch* b)
 int irr_batch_sync(irr_batch* b)
 {
     if (!b) return IRR_ERR_ARG;
-    cudaSetDevice(b->device);
+    DeviceGuard dev_guard(b->device);
     B_CUDA(b, cudaStreamSynchronize(b->stream), "synchronise");
     int st = 0;
     B_CUDA(b, cudaMemcpy(&st, b->d_status, sizeof(int), cudaMemcpyDeviceToHost), "status");

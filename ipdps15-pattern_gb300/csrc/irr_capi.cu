@@ -249,7 +249,7 @@ int set_edges_common(irr_handle* h, const int32_t* src, int64_t e, cudaMemcpyKin
 int irr_ensure_layout(irr_handle* h, int lanes_per_row, int block_nodes)
 {
     if (!h || !h->inited || h->cfg.exec != IRR_EXEC_PARTITIONED) return IRR_ERR_STATE;
-    cudaSetDevice(h->device);
+    DeviceGuard dev_guard(h->device);
     H_CUDA(h, cudaStreamSynchronize(h->stream), "layout");  // no launch may use the old layout
     const int64_t n = h->n, e = h->e;
     h->shape.lanes_per_row = lanes_per_row;
@@ -343,7 +343,8 @@ int irr_create(const irr_config* cfg, irr_handle** out)
     h->device = c.device;
     h->map_idx = c.map_idx;
     h->reduce_idx = c.reduce_idx;
-    if (cudaSetDevice(h->device) != cudaSuccess ||
+    DeviceGuard dev_guard(h->device);
+    if (!dev_guard.ok() ||
         cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, h->device) != cudaSuccess ||
         cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaMalloc(&h->d_status, sizeof(int)) != cudaSuccess ||
@@ -372,7 +373,7 @@ int irr_create(const irr_config* cfg, irr_handle** out)
 int irr_destroy(irr_handle* h)
 {
     if (!h) return IRR_ERR_ARG;
-    cudaSetDevice(h->device);
+    DeviceGuard dev_guard(h->device);
     if (h->stream) cudaStreamSynchronize(h->stream);
     free_layout(h);
     dfree(h->d_raw);
@@ -421,7 +422,7 @@ int irr_set_params(irr_handle* h, const void* param, int param_size)
 {
     if (!h) return IRR_ERR_ARG;
     if (!param || param_size <= 0) return fail(h, IRR_ERR_ARG, "empty parameter block");
-    cudaSetDevice(h->device);
+    DeviceGuard dev_guard(h->device);
     std::vector<unsigned char> keep = h->param;
     h->param.assign((const unsigned char*)param, (const unsigned char*)param + param_size);
     int rc = make_law(h);
@@ -435,28 +436,28 @@ int irr_set_params(irr_handle* h, const void* param, int param_size)
 int irr_set_edges(irr_handle* h, const int32_t* edges, int64_t num_edges)
 {
     if (!h) return IRR_ERR_ARG;
-    cudaSetDevice(h->device);
+    DeviceGuard dev_guard(h->device);
     return set_edges_common(h, edges, num_edges, cudaMemcpyHostToDevice);
 }
 
 int irr_set_edges_device(irr_handle* h, const int32_t* d_edges, int64_t num_edges)
 {
     if (!h) return IRR_ERR_ARG;
-    cudaSetDevice(h->device);
+    DeviceGuard dev_guard(h->device);
     return set_edges_common(h, d_edges, num_edges, cudaMemcpyDeviceToDevice);
 }
 
 int irr_set_nodes(irr_handle* h, const void* node_data, int elm_size, int64_t num_nodes)
 {
     if (!h) return IRR_ERR_ARG;
-    cudaSetDevice(h->device);
+    DeviceGuard dev_guard(h->device);
     return set_nodes_common(h, node_data, elm_size, num_nodes, cudaMemcpyHostToDevice);
 }
 
 int irr_set_nodes_device(irr_handle* h, const void* d_node_data, int elm_size, int64_t num_nodes)
 {
     if (!h) return IRR_ERR_ARG;
-    cudaSetDevice(h->device);
+    DeviceGuard dev_guard(h->device);
     return set_nodes_common(h, d_node_data, elm_size, num_nodes, cudaMemcpyDeviceToDevice);
 }
 
@@ -467,7 +468,7 @@ int irr_init(irr_handle* h)
     if (h->n < 0) return fail(h, IRR_ERR_STATE, "irr_init before irr_set_nodes");
     if (h->e < 0) return fail(h, IRR_ERR_STATE, "irr_init before irr_set_edges");
     if (!h->have_law) return fail(h, IRR_ERR_STATE, "irr_init before irr_set_params");
-    cudaSetDevice(h->device);
+    DeviceGuard dev_guard(h->device);
     cudaStream_t s = h->stream;
     const int64_t n = h->n, e = h->e;
     H_CUDA(h, launch_validate_edges(h->d_edges, e, n, h->d_status, s), "validate edges");
@@ -521,7 +522,7 @@ int irr_step(irr_handle* h)
         int rc = irr_init(h);
         if (rc) return rc;
     }
-    cudaSetDevice(h->device);
+    DeviceGuard dev_guard(h->device);
     if (h->raw_pending) {
         H_CUDA(h, launch_load_nodes(h->d_raw, h->raw_elm, h->part.perm, h->n, h->d_pos, h->stream), "load node data");
         h->raw_pending = false;
@@ -547,7 +548,7 @@ int irr_get_result_device(irr_handle* h, void* d_out, int elm_size)
     if (reinterpret_cast<uintptr_t>(d_out) % align)
         return fail(h, IRR_ERR_ARG, "result buffer not aligned to %d bytes for %d-byte records",
                     (int)align, elm_size);
-    cudaSetDevice(h->device);
+    DeviceGuard dev_guard(h->device);
     H_CUDA(h, launch_store_result(h->d_force, h->part.inv, h->n, elm_size, d_out, h->stream), "store result");
     return IRR_OK;
 }
@@ -557,7 +558,7 @@ int irr_get_result(irr_handle* h, void* out, int elm_size)
     if (!h || (!out && h->n > 0)) return fail(h, IRR_ERR_ARG, "null output");
     if (elm_size != 12 && elm_size != 16 && elm_size != 24) return fail(h, IRR_ERR_ARG, "result elm_size %d: use 12, 16 or 24", elm_size);
     if (!h->inited) return fail(h, IRR_ERR_STATE, "no result before irr_step");
-    cudaSetDevice(h->device);
+    DeviceGuard dev_guard(h->device);
     if (h->n > 0) {
         // into page-locked host memory directly: written in order over the
         // host link, gathered from execution order on the device
@@ -584,7 +585,7 @@ int irr_get_result(irr_handle* h, void* out, int elm_size)
 int irr_sync(irr_handle* h)
 {
     if (!h) return IRR_ERR_ARG;
-    cudaSetDevice(h->device);
+    DeviceGuard dev_guard(h->device);
     return check_status(h);
 }
 
@@ -612,7 +613,7 @@ int irr_get_partition(irr_handle* h, int32_t* perm, int64_t* row_off, int32_t* c
     if (!h) return IRR_ERR_ARG;
     if (h->cfg.exec != IRR_EXEC_PARTITIONED) return fail(h, IRR_ERR_STATE, "handle is not partitioned");
     if (!h->inited) return fail(h, IRR_ERR_STATE, "no partition before irr_init");
-    cudaSetDevice(h->device);
+    DeviceGuard dev_guard(h->device);
     const int64_t n = h->n, m = 2 * h->e;
     if (perm && n > 0)
         H_CUDA(h, cudaMemcpyAsync(perm, h->part.perm, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, h->stream), "copy perm");

@@ -17,6 +17,34 @@ enum : int {
     kStatusBadAlign = 1 << 2,   // a bulk copy was asked for an unaligned range
 };
 
+// Makes `device` current for the guard's lifetime and then restores the
+// calling thread's previous current device, so that no entry point leaves a
+// multi-GPU host program on another GPU.  ok() is false when the device could
+// not be made current (the CUDA error is cleared).
+class DeviceGuard {
+public:
+    explicit DeviceGuard(int device)
+    {
+        if (cudaGetDevice(&prev_) != cudaSuccess) {
+            cudaGetLastError();
+            prev_ = -1;
+        }
+        ok_ = cudaSetDevice(device) == cudaSuccess;
+        if (!ok_) cudaGetLastError();
+    }
+    ~DeviceGuard()
+    {
+        if (prev_ >= 0 && cudaSetDevice(prev_) != cudaSuccess) cudaGetLastError();
+    }
+    bool ok() const { return ok_; }
+    DeviceGuard(const DeviceGuard&) = delete;
+    DeviceGuard& operator=(const DeviceGuard&) = delete;
+
+private:
+    int prev_ = -1;
+    bool ok_ = false;
+};
+
 // One system of the (possibly batched) owner-computes reduction.
 struct InstDesc {
     const float4* pos;        // node positions, execution (partition) order

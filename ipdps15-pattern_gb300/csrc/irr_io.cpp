@@ -5,12 +5,17 @@
 // node i (1-based ids) listing its neighbours.  A line is read up to its first
 // value <= 0 or non-number, and only neighbours j >= i are kept, so each
 // undirected pair is listed once (as (i, j) with i <= j) and the header's edge
-// count must equal the number kept.  The reference builds without CSTYLE, so
-// its reader returns 1-based pairs; `one_based` selects that, 0 gives 0-based
-// pairs (the library's node ids).  A node line missing at the end of the file
-// counts as empty (the reference would re-read the previous line).
+// count must equal the number kept.  moldyn's misc.c defines CSTYLE
+// (misc.c:20), so its reader returns 0-based pairs [0, n), which is the
+// default here (the library's node ids); `one_based` gives the [1, n] pairs of
+// its non-CSTYLE branch.  A node line missing at the end of the file counts as
+// empty, as in the reference.  Differences, on files the reference does not
+// read: a last line without its newline is read here (the reference stops at
+// end of file before parsing it), and lines are not limited to its 1,280,000
+// characters.
 // Coordinates (moldyn/misc.c:224-246, ReadCoord): whitespace-separated x y z
-// triples, exactly num_nodes of them.
+// triples, exactly num_nodes of them (reading stops at the first token that is
+// not a number, where the reference's fscanf loop would not end).
 #include <cerrno>
 #include <cstdio>
 #include <cstdlib>

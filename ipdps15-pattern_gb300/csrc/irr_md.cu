@@ -488,7 +488,8 @@ int irr_md_create(const irr_md_config* cfg, const double* pos, const double* vel
     m->device = cfg->device;
     m->n = n;
     int rc = IRR_OK;
-    if (cudaSetDevice(m->device) != cudaSuccess ||
+    DeviceGuard dev_guard(m->device);
+    if (!dev_guard.ok() ||
         cudaDeviceGetAttribute(&m->sms, cudaDevAttrMultiProcessorCount, m->device) != cudaSuccess ||
         cudaStreamCreateWithFlags(&m->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
         cudaGetLastError();
@@ -560,7 +561,7 @@ int irr_md_create(const irr_md_config* cfg, const double* pos, const double* vel
 int irr_md_destroy(irr_md* m)
 {
     if (!m) return IRR_ERR_ARG;
-    cudaSetDevice(m->device);
+    DeviceGuard dev_guard(m->device);
     if (m->stream) cudaStreamSynchronize(m->stream);
     if (m->own_stream) {
         free_part(m, m->own_stream);
@@ -587,7 +588,7 @@ int irr_md_set_stream(irr_md* m, void* stream)
 int irr_md_run(irr_md* m, int steps)
 {
     if (!m || steps < 0) return IRR_ERR_ARG;
-    cudaSetDevice(m->device);
+    DeviceGuard dev_guard(m->device);
     for (int t = 0; t < steps; t++) {
         // a step's closing kick is fused into the next step's kick-drift
         int rc = t == 0 ? md_kick_drift(m) : md_kick_kick_drift(m);
@@ -601,7 +602,7 @@ int irr_md_run(irr_md* m, int steps)
 int irr_md_energy(irr_md* m, double* kinetic, double* potential, double* virial)
 {
     if (!m) return IRR_ERR_ARG;
-    cudaSetDevice(m->device);
+    DeviceGuard dev_guard(m->device);
     const int blocks = grid_of(m->n) < kEnergyBlocks ? grid_of(m->n) : kEnergyBlocks;
     double* part = m->d_acc + 4;
     kinetic_kernel<<<blocks, 256, 0, m->stream>>>(m->v, m->n, part);
@@ -624,7 +625,7 @@ int irr_md_energy(irr_md* m, double* kinetic, double* potential, double* virial)
 int irr_md_get_state(irr_md* m, double* pos, double* vel)
 {
     if (!m) return IRR_ERR_ARG;
-    cudaSetDevice(m->device);
+    DeviceGuard dev_guard(m->device);
     const size_t b3 = sizeof(double) * 3 * (size_t)m->n;
     const int g = grid_of(m->n);
     std::vector<double> host;
@@ -643,7 +644,7 @@ int irr_md_get_state(irr_md* m, double* pos, double* vel)
 int irr_md_get_forces(irr_md* m, double* f)
 {
     if (!m || !f) return IRR_ERR_ARG;
-    cudaSetDevice(m->device);
+    DeviceGuard dev_guard(m->device);
     // F = 48 * reduction result, in the caller's atom order
     std::vector<float4> fr((size_t)m->n);
     std::vector<int32_t> ids((size_t)m->n);

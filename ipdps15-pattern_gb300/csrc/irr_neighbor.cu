@@ -802,10 +802,8 @@ int irr_neighbor_build(int device, void* stream, const void* pos, int pos_elm, i
     if (n > 0x7fffffffLL) return IRR_ERR_CAPACITY;
     *d_edges = nullptr;
     *num_edges = 0;
-    if (cudaSetDevice(device) != cudaSuccess) {
-        cudaGetLastError();
-        return IRR_ERR_CUDA;
-    }
+    irr::DeviceGuard dev_guard(device);
+    if (!dev_guard.ok()) return IRR_ERR_CUDA;
     cudaStream_t s = (cudaStream_t)stream;
     void* raw = nullptr;
     float4* p4 = nullptr;
@@ -840,7 +838,8 @@ int irr_neighbor_build(int device, void* stream, const void* pos, int pos_elm, i
 int irr_device_free(int device, void* d_ptr)
 {
     if (!d_ptr) return IRR_OK;
-    if (cudaSetDevice(device) != cudaSuccess || cudaFree(d_ptr) != cudaSuccess) {
+    irr::DeviceGuard dev_guard(device);
+    if (!dev_guard.ok() || cudaFree(d_ptr) != cudaSuccess) {
         cudaGetLastError();
         return IRR_ERR_CUDA;
     }

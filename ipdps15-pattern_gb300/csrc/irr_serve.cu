@@ -467,10 +467,8 @@ int irr_serve_run(const irr_serve_config* cfg, irr_serve_stats* st, irr_serve_jo
     if (cfg->mode != IRR_SERVE_CONTINUOUS && cfg->mode != IRR_SERVE_SERIAL && cfg->mode != IRR_SERVE_SERIAL_PLAIN)
         return IRR_ERR_ARG;
     memset(st, 0, sizeof(*st));
-    if (cudaSetDevice(cfg->device) != cudaSuccess) {
-        cudaGetLastError();
-        return IRR_ERR_CUDA;
-    }
+    DeviceGuard dev_guard(cfg->device);
+    if (!dev_guard.ok()) return IRR_ERR_CUDA;
     int sms = 0;
     cudaStream_t s = nullptr;
     int *d_queue = nullptr, *d_status = nullptr;

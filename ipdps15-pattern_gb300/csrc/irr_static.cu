@@ -9,14 +9,17 @@
 // positions and the output; all scratch lives in g_morton_scratch below.
 //
 // g_morton_scratch is a file-scope device array: every GPU that loads this
-// library holds kStaticScratchBytes of it until the process exits.  Host code
-// cannot use its name as a device address, so each device's address is looked
-// up once, with that device current, by cudaGetSymbolAddress; the first call
-// on a device does that look-up (make that first call before any stream
-// capture).  Calls share the array and it keeps the previous call's contents:
-// everything this code reads from it is written earlier in the same call,
-// and calls that overlap on the GPU (from two streams or two threads) race on
-// it, so callers must order them.
+// library holds kStaticScratchBytes (12,886,272 bytes, about 12.3 MiB) of it
+// until the process exits.  Host code cannot use its name as a device
+// address, so the address is looked up with the device current, by
+// cudaGetSymbolAddress: on every call whose stream is not capturing (so a
+// device reset, which gives the array a new address, is picked up), and
+// taken from the last look-up on that device while a capture is under way
+// (so make the first call on a device before any stream capture, and none
+// after a device reset while capturing).  Calls share the array and it keeps
+// the previous call's contents: everything this code reads from it is written
+// earlier in the same call, and calls that overlap on the GPU (from two
+// streams or two threads) race on it, so callers must order them.
 #include <cmath>
 #include <mutex>
 
@@ -41,23 +44,34 @@ constexpr size_t kScanWords = 4096;  // block sums of every scan level
 constexpr size_t kOffBbox = align256(kOffScan + 4 * kScanWords);
 constexpr size_t kOffFrame = align256(kOffBbox + 4 * 6 * kBboxParts);
 constexpr size_t kStaticScratchBytes = align256(kOffFrame + 4 * 8);
+static_assert(kStaticScratchBytes == IRR_MORTON_STATIC_SCRATCH_BYTES,
+              "the header states the scratch array's size");
 
 __device__ __align__(256) unsigned char g_morton_scratch[kStaticScratchBytes];
 
 std::mutex g_addr_mutex;
 void* g_addr[64] = {};
 
-// Device address of g_morton_scratch on `device` (looked up once per device).
-cudaError_t scratch_address(int device, unsigned char** out)
+// Device address of g_morton_scratch on `device` (the current device): looked
+// up again unless `s` is capturing, when the last look-up on the device is
+// used (a capture may not be the place for a first look-up, which can load
+// the module).
+cudaError_t scratch_address(int device, cudaStream_t s, unsigned char** out)
 {
     if (device < 0 || device >= 64) return cudaErrorInvalidDevice;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cap) != cudaSuccess) {
+        cudaGetLastError();
+        cap = cudaStreamCaptureStatusActive;  // unknown: do not risk a look-up
+    }
     std::lock_guard<std::mutex> lock(g_addr_mutex);
-    if (!g_addr[device]) {
+    if (cap == cudaStreamCaptureStatusNone) {
         void* p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_morton_scratch);
         if (e != cudaSuccess) return e;
         g_addr[device] = p;
     }
+    if (!g_addr[device]) return cudaErrorStreamCaptureUnsupported;
     *out = static_cast<unsigned char*>(g_addr[device]);
     return cudaSuccess;
 }
@@ -168,17 +182,18 @@ extern "C" int irr_morton_order_static(int device, void* stream, const void* d_p
     if (n < 0 || (n > 0 && (!d_pos || !d_perm))) return IRR_ERR_ARG;
     if (pos_elm != 12 && pos_elm != 16) return IRR_ERR_ARG;
     if (n > kStaticMaxNodes) return IRR_ERR_CAPACITY;
-    if (cudaSetDevice(device) != cudaSuccess) {
-        cudaGetLastError();
-        return IRR_ERR_CUDA;
-    }
+    // float records and int32 output: both read or written as 4-byte words
+    if ((reinterpret_cast<uintptr_t>(d_pos) | reinterpret_cast<uintptr_t>(d_perm)) % 4u)
+        return IRR_ERR_ARG;
+    DeviceGuard dev_guard(device);  // the caller's current device comes back on return
+    if (!dev_guard.ok()) return IRR_ERR_CUDA;
+    cudaStream_t s = (cudaStream_t)stream;
     unsigned char* ws = nullptr;
-    if (scratch_address(device, &ws) != cudaSuccess) {
+    if (scratch_address(device, s, &ws) != cudaSuccess) {
         cudaGetLastError();
         return IRR_ERR_CUDA;
     }
     if (n == 0) return IRR_OK;
-    cudaStream_t s = (cudaStream_t)stream;
     const char* raw = static_cast<const char*>(d_pos);
     uint32_t* keys = reinterpret_cast<uint32_t*>(ws + kOffKeys);
     uint32_t* keys_tmp = reinterpret_cast<uint32_t*>(ws + kOffKeysTmp);

@@ -29,6 +29,24 @@ class LJParam(C.Structure):
     _fields_ = [("side", C.c_double), ("cutoff2", C.c_double), ("periodic", C.c_int)]
 
 
+def reference_tree() -> str:
+    """Where the reference's sources are read from: $IRR_REFERENCE_TREE, else the
+    `REF ?=` default of oracle/Makefile (the recipe that compiles them).  The
+    tree may be absent; callers check before using it."""
+    env = os.environ.get("IRR_REFERENCE_TREE")
+    if env:
+        return env
+    try:
+        with open(os.path.join(HERE, "Makefile")) as f:
+            for line in f:
+                key, sep, val = line.partition("?=")
+                if sep and key.strip() == "REF":
+                    return val.strip()
+    except OSError:
+        pass
+    return ""
+
+
 def build(quiet: bool = True) -> None:
     """Compiles liboracle.so with the committed Makefile."""
     out = subprocess.run(["make", "-C", HERE, "liboracle.so"], capture_output=True, text=True)
@@ -328,3 +346,27 @@ def ref_compute_cpu(which: str, pos, edges, param_blob: np.ndarray, threads: int
     if rc != 0:
         raise RuntimeError("ref_compute_cpu failed")
     return out, secs.value
+
+
+def ref_read_graph(path: str, max_edges: int) -> np.ndarray:
+    """moldyn's own ReadInputGraph (moldyn/misc.c:62-146, built by `make ref`):
+    the half list it returns, as int32 pairs.  The reference exits the process
+    on an unreadable file or an edge-count mismatch, so call it only on files
+    it accepts; `max_edges` bounds its output buffer."""
+    L = C.CDLL(os.path.join(REF_DIR, "libref_misc.so"))
+    L.ReadInputGraph.argtypes = [C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_void_p]
+    L.ReadInputGraph.restype = None
+    n, m = C.c_int(0), C.c_int(0)
+    el = np.full((max(max_edges, 1), 2), -1, np.int32)
+    L.ReadInputGraph(path.encode(), C.byref(n), C.byref(m), _p(el))
+    return el[: m.value].copy(), n.value
+
+
+def ref_read_coords(path: str, n: int) -> np.ndarray:
+    """moldyn's own ReadCoord (moldyn/misc.c:224-246): n xyz triples in double."""
+    L = C.CDLL(os.path.join(REF_DIR, "libref_misc.so"))
+    L.ReadCoord.argtypes = [C.c_char_p, C.c_int, C.c_void_p]
+    L.ReadCoord.restype = None
+    xyz = np.zeros((max(n, 1), 3), np.float64)
+    L.ReadCoord(path.encode(), int(n), _p(xyz))
+    return xyz[:n].copy()

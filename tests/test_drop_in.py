@@ -12,8 +12,9 @@ import subprocess
 import pytest
 
 from conftest import PKG, ROOT
+from oracle.oracle import reference_tree
 
-REF = os.environ.get("IRR_REFERENCE_TREE", "/root/reference")
+REF = reference_tree()
 COMPAT = os.path.join(PKG, "compat")
 
 pytestmark = pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "moldyn", "irregular")),

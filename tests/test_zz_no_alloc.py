@@ -65,6 +65,27 @@ def test_static_ordering_after_a_different_size(built_lib):
     assert np.array_equal(got, partitioner_perm(irr, small))
 
 
+@pytest.mark.parametrize("case", ["flat_axis", "signed_zero_minimum"])
+def test_static_ordering_degenerate_frames(built_lib, case):
+    """Where the two routes form the curve frame differently (on the device here,
+    on the host after a warp reduction in the partitioner): an axis with no
+    extent (scale 0), and an axis whose minimum is +0.0 for some nodes and -0.0
+    for others."""
+    torch = pytest.importorskip("torch")
+    import irregular_gb300 as irr
+    pos32, _ = random_box(20000, 0.9, 21)
+    if case == "flat_axis":
+        pos32[:, 2] = np.float32(1.5)
+    else:
+        pos32[::3, 0] = np.float32(0.0)
+        pos32[1::3, 0] = np.float32(-0.0)
+    ref = partitioner_perm(irr, pos32)
+    got = static_perm(irr, torch, torch.from_numpy(pos32).cuda(), 12, pos32.shape[0])
+    again = static_perm(irr, torch, torch.from_numpy(pos32).cuda(), 12, pos32.shape[0])
+    assert np.array_equal(got, ref)
+    assert np.array_equal(again, ref)
+
+
 def test_static_ordering_rejects_oversize_and_bad_args(built_lib):
     torch = pytest.importorskip("torch")
     import irregular_gb300 as irr
@@ -76,3 +97,8 @@ def test_static_ordering_rejects_oversize_and_bad_args(built_lib):
     assert L.irr_morton_order_static(0, None, d.data_ptr(), 24, 4, o.data_ptr()) == irr.IRR_ERR_ARG
     assert L.irr_morton_order_static(0, None, None, 12, 4, o.data_ptr()) == irr.IRR_ERR_ARG
     assert L.irr_morton_order_static(0, None, d.data_ptr(), 12, 0, None) == irr.IRR_OK
+    # records and output are read and written as 4-byte words
+    assert L.irr_morton_order_static(0, None, d.data_ptr() + 2, 12, 4, o.data_ptr()) == \
+        irr.IRR_ERR_ARG
+    assert L.irr_morton_order_static(0, None, d.data_ptr(), 12, 2, o.data_ptr() + 1) == \
+        irr.IRR_ERR_ARG
