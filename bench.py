@@ -21,7 +21,16 @@ Our arm prints one JSON line with
                measured step time, against the measured HBM copy bandwidth;
   cpu_baseline the reference's CPU executor (ported, oracle/) on all host
                cores over a bounded sample of the same edge list;
-  clocks       nvidia-smi samples taken during the timed region.
+  clocks       nvidia-smi samples taken during the timed region;
+  force_err    a seeded sample of 2,000 nodes recomputed in FP64 by this
+               file's own checker (fp64_forces): normwise, per node against
+               the terms' magnitudes, and per result (p50 / p99 / max);
+  md, batched, served
+               the other configurations of the metric, measured in the same
+               run (N = 1): the 1,048,576-atom MD loop, 512 batched instances
+               in one graph-captured persistent launch per step against the
+               same instances run one by one, and the served stream (p50 /
+               p99 latency, throughput against serial execution, capacity).
 `--impl reference` times that CPU executor alone (rank 0; other ranks exit).
 With N > 1 (torchrun) every rank reduces its own replica of the workload
 (weak scaling, no collective on the data path); times are maxed over ranks.
@@ -47,6 +56,7 @@ for _p in (ROOT, PKG):
 import numpy as np  # noqa: E402
 
 N_NODES = 4194304
+FORCE_SAMPLE = 2000   # nodes whose results the FP64 checker recomputes
 CUTOFF = 2.5
 DENSITY = 64.0 / (4.0 / 3.0 * math.pi * CUTOFF ** 3)
 SEED = 20260002
@@ -89,6 +99,79 @@ def ncu_traffic(key: str):
     except OSError:
         pass
     return None
+
+
+def fp64_forces(pos32, edges, side: float, cutoff: float, periodic: bool = True):
+    """FP64 checker for the force-error fields: the LJ law d (r^-14 - r^-8/2) of
+    the reference's `map` (moldyn/irregular.h:47-78) on the float positions
+    widened to double, minimum image in a cube of side `side`, applied when
+    r^2 < cutoff^2, +f to idx0 and -f to idx1.  Returns per node the forces,
+    the per-component sum of the terms' magnitudes |d_c| (r^-14 + r^-8/2), and
+    the sum of each term's largest component."""
+    n = pos32.shape[0]
+    p = np.asarray(pos32, np.float64)
+    i, j = edges[:, 0].astype(np.int64), edges[:, 1].astype(np.int64)
+    d = p[i] - p[j]
+    if periodic:
+        half = 0.5 * side
+        d = np.where(d < -half, d + side, d)
+        d = np.where(d > half, d - side, d)
+    rd = (d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1]) + d[:, 2] * d[:, 2]
+    inside = rd < cutoff * cutoff
+    with np.errstate(divide="ignore", invalid="ignore"):
+        r = np.where(inside, 1.0 / np.where(inside, rd, 1.0), 0.0)
+    r4 = (r * r) * (r * r)
+    s = r4 * (r * r * r) - 0.5 * r4
+    sa = r4 * (r * r * r) + 0.5 * r4
+    fe = d * s[:, None]
+    ae = np.abs(d) * sa[:, None]
+    f = np.zeros((n, 3))
+    sabs = np.zeros((n, 3))
+    sinf = np.zeros(n)
+    np.add.at(f, i, fe)
+    np.add.at(f, j, -fe)
+    np.add.at(sabs, i, ae)
+    np.add.at(sabs, j, ae)
+    m = np.abs(fe).max(axis=1)
+    np.add.at(sinf, i, m)
+    np.add.at(sinf, j, m)
+    return f, sabs, sinf
+
+
+def incident(edges, n: int, sample):
+    sel = np.zeros(n, bool)
+    sel[sample] = True
+    return edges[sel[edges[:, 0]] | sel[edges[:, 1]]]
+
+
+def force_err(f, f64, sabs, sinf) -> dict:
+    """Errors of results f against the FP64 checker, on the nodes given:
+    normwise max|df| / max|f64|; per node and component |df| / sabs (sabs: the
+    terms' magnitudes); and per result |df|inf / max(|f64|inf, 2^-10 sinf) at
+    the median, 99th percentile and worst node."""
+    f = np.asarray(f, np.float64).reshape(-1, 3)
+    g = np.asarray(f64, np.float64).reshape(-1, 3)
+    d = np.abs(f - g)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        pern = np.where(sabs > 0, d / np.where(sabs > 0, sabs, 1.0), np.where(d > 0, np.inf, 0.0))
+        den = np.maximum(np.abs(g).max(axis=1), np.asarray(sinf) / 1024.0)
+        res = np.where(den > 0, d.max(axis=1) / np.where(den > 0, den, 1.0), 0.0)
+    return {"normwise": float(d.max() / max(np.abs(g).max(), 1e-300)),
+            "per_node_S": float(pern.max()),
+            "per_result": {"p50": float(np.percentile(res, 50)), "p99": float(np.percentile(res, 99)),
+                           "max": float(res.max())},
+            "nodes": int(g.shape[0]),
+            "metric_note": "per_result = |df|inf / max(|f64|inf, 2^-10 sum_e |f_e|inf)"}
+
+
+def merge_err(errs):
+    """The worst of several force_err results."""
+    if not errs:
+        return None
+    return {"normwise": max(e["normwise"] for e in errs),
+            "per_node_S": max(e["per_node_S"] for e in errs),
+            "per_result": {k: max(e["per_result"][k] for e in errs) for k in ("p50", "p99", "max")},
+            "nodes": sum(e["nodes"] for e in errs), "metric_note": errs[0]["metric_note"]}
 
 
 class ClockSampler:
@@ -221,6 +304,19 @@ def run_reference(args, rank, world):
         "vs_baseline": None, "dtype": "f64 per edge, f32 accumulate", "data": "synthetic",
         "config": {"workload": workload_name(args.nodes), "nodes": args.nodes,
                    "edges_per_step": int(sample.shape[0]),
+                   "sample": f"rows [0, {rows}) of the workload's half list, every step; the "
+                             f"rate is the metric (edges/s), so the sample stands for the "
+                             f"whole list",
+                   "chunk_edges": CPU_CHUNK,
+                   "chunk_source": "CPU_BLOCK_SIZE of the reference's miniMD copy "
+                                   "(miniMD/irregular/parameters.h:7); the moldyn copy's "
+                                   "1,000,000 would leave most threads idle on the sample",
+                   "kind": "port",
+                   "why_port": "the reference's CPU code, compiled from its own sources, needs "
+                               "the reference tree, which the GPU box does not hold, and its "
+                               "1,048,577-bucket table overflows (its insert then spins) at "
+                               "4,194,304 nodes",
+                   "threads": threads,
                    "executor": "reference CPU executor (port of compute_cpu + Cobject)"},
         "cpu_baseline": {"value": rate, "unit": "edges/s", "cores": threads, "kind": "port",
                          "sample": desc},
@@ -288,6 +384,17 @@ def run_ours(args, rank, world, local):
                               "legs": "value only", "nodes": n, "edges": E,
                               "ms_per_step": ms / args.steps}), flush=True)
         return 0
+
+    # force error of the timed configuration on a seeded node sample (FP64 checker)
+    err = None
+    if rank == 0:
+        f_gpu = h.get_result(elm_size=12)
+        host_edges = edges.to_host()
+        smp = np.sort(np.random.Generator(np.random.PCG64(SEED + 1)).choice(
+            n, min(n, FORCE_SAMPLE), replace=False))
+        g, sabs, sinf = fp64_forces(pos, incident(host_edges, n, smp), float(side), CUTOFF)
+        err = force_err(f_gpu[smp], g[smp], sabs[smp], sinf[smp])
+        del host_edges
 
     # e2e through the public API with host buffers (pinned)
     pin_in = torch.empty((n, 3), dtype=torch.float32, pin_memory=True)
@@ -359,9 +466,18 @@ def run_ours(args, rank, world, local):
         "gpu_launches": args.steps,
         "variants_edges_per_s": variants,
     }
+    if err is not None:
+        line["force_err"] = err
     if cpu is not None:
         line["cpu_baseline"] = cpu
     h.close()
+    if rank == 0 and world == 1 and args.legs == "all":
+        # the other configurations of the metric, measured in the same run
+        line["md"] = run_md(args)
+        line["batched"] = run_batched(args)
+        line["served"] = run_served(args)
+    elif args.legs == "all":
+        line["legs"] = "md / batched / served run at N = 1 only"
     if rank == 0:
         print(json.dumps(line), flush=True)
     return 0
@@ -371,7 +487,8 @@ def run_batched(args):
     """Config 4: 512 instances, sizes log-uniform in [1,024, 262,144] atoms, each
     uniform-random in its own periodic box at density 0.8442, cutoff 2.5; one
     persistent launch per step (CUDA graph, autotuned shape) vs the same
-    instances one by one through the single-instance paths."""
+    instances one by one through the single-instance paths.  Returns the leg's
+    JSON object."""
     import torch
 
     import irregular_gb300 as irr
@@ -383,13 +500,18 @@ def run_batched(args):
     rng = np.random.Generator(np.random.PCG64(SEED + 2))
     count = args.instances
     sizes = np.floor(np.exp(rng.uniform(math.log(1024), math.log(262144), count))).astype(int)
+    checked = {int(np.argmax(sizes))}
+    checked |= set(int(k) for k in np.random.Generator(np.random.PCG64(SEED + 3)).choice(
+        count, min(3, count), replace=False))
     t_setup = time.perf_counter()
-    part, plain = [], []
+    part, plain, keep = [], [], {}
     E = 0
     for k, n in enumerate(sizes):
         pos, side = W.random_box(int(n), 0.8442, SEED + 100 + k)
         edges = irr.neighbor_build(pos, side, CUTOFF * CUTOFF, device=dev, stream=stream.cuda_stream)
         E += edges.count
+        if k in checked:
+            keep[k] = (pos, side, edges.to_host())
         for mode, bucket in ((irr.IRR_EXEC_PARTITIONED, part), (irr.IRR_EXEC_PLAIN, plain)):
             h = irr.Handle(irr.default_config(device=dev, map_idx=irr.IRR_MAP_LJ_MOLDYN, exec=mode))
             h.set_stream(stream.cuda_stream)
@@ -411,6 +533,14 @@ def run_batched(args):
     b.sync()
     ms_batch = time_steps(b, stream, args.batch_steps)
     b.sync()
+    errs = []
+    for k, (pos, side, host_edges) in sorted(keep.items()):
+        f_gpu = part[k].get_result(elm_size=12)
+        nk = pos.shape[0]
+        smp = np.sort(np.random.Generator(np.random.PCG64(SEED + 1000 + k)).choice(
+            nk, min(nk, 1000), replace=False))
+        g, sabs, sinf = fp64_forces(pos, incident(host_edges, nk, smp), side, CUTOFF)
+        errs.append(force_err(f_gpu[smp], g[smp], sabs[smp], sinf[smp]))
 
     class Serial:
         def __init__(self, hs):
@@ -431,6 +561,9 @@ def run_batched(args):
     batched = E * args.batch_steps / (ms_batch / 1e3)
     serial_part = E * args.batch_steps / (ms_part / 1e3)
     serial_plain = E * ser_steps / (ms_plain / 1e3)
+    alg = 8.0 * E + 24.0 * float(sizes.sum())
+    peak = measured_hbm_peak()[0]
+    achieved = alg / (ms_batch / 1e3 / args.batch_steps) / 1e9
     line = {"leg": "batched", "metric": "aggregate edges/s", "unit": "edges/s",
             "instances": int(count), "nodes": int(sizes.sum()), "edges_per_step": int(E),
             "steps": args.batch_steps, "batched": batched,
@@ -443,21 +576,22 @@ def run_batched(args):
             "shape": {"lanes_per_row": inf.lanes_per_row, "rows_per_item": inf.block_nodes,
                       "work_items": int(inf.num_items), "cuda_graph": bool(inf.graph)},
             "setup_s": setup_s,
-            "roofline": {"algorithmic_bytes_per_step": 8.0 * E + 24.0 * float(sizes.sum()),
-                         "achieved_GBs": (8.0 * E + 24.0 * float(sizes.sum())) /
-                         (ms_batch / 1e3 / args.batch_steps) / 1e9,
-                         "peak_GBs": measured_hbm_peak()[0]},
+            "roofline": {"algorithmic_bytes_per_step": alg, "achieved_GBs": achieved,
+                         "peak_GBs": peak, "frac": achieved / peak},
+            "force_err": merge_err(errs),
+            "force_err_instances": sorted(int(k) for k in keep),
             "data": "synthetic (seeded sizes and positions; lists built on the GPU)"}
     b.close()
-    print(json.dumps(line), flush=True)
-    return 0
+    for h in part + plain:
+        h.close()
+    return line
 
 
 def run_md(args):
     """Config 3: miniMD-style LJ MD, FCC 4 x 64^3 = 1,048,576 atoms at density
     0.8442, Maxwell velocities at T = 1.44, cutoff 2.5, skin 0.3, rebuild every
     20 steps, velocity Verlet dt = 0.005, 1000 steps; FP32 forces, FP64
-    integration and energies."""
+    integration and energies.  Returns the leg's JSON object."""
     import torch
 
     import irregular_gb300 as irr
@@ -483,6 +617,17 @@ def run_md(args):
     ke1, pe1, vir1 = md.energy()
     n = pos.shape[0]
     info = md.info()
+    # forces at the end against the FP64 checker (x48: the MD's force units)
+    gp, _ = md.state()
+    f_gpu = md.forces()
+    p32 = gp.astype(np.float32)
+    lst = irr.neighbor_build(p32, float(np.float32(side)), 2.8 ** 2)
+    host_edges = lst.to_host()
+    lst.close()
+    smp = np.sort(np.random.Generator(np.random.PCG64(SEED + 4)).choice(n, FORCE_SAMPLE,
+                                                                      replace=False))
+    g, sabs, sinf = fp64_forces(p32, incident(host_edges, n, smp), side, 2.5)
+    err = force_err(f_gpu[smp], 48.0 * g[smp], 48.0 * sabs[smp], 48.0 * sinf[smp])
     line = {"leg": "md", "metric": "ms per MD step", "unit": "ms", "atoms": n,
             "steps": steps, "ms_per_step": ms / steps, "atom_steps_per_s": n * steps / (ms / 1e3),
             "pairs_in_list": int(info.num_edges), "rebuilds": int(info.rebuilds),
@@ -491,11 +636,16 @@ def run_md(args):
             "energy_drift_rel": abs((ke1 + pe1) - (ke_w + pe_w)) / abs(ke_w + pe_w),
             "temperature_end": 2.0 * ke1 / (3 * n - 3),
             "pressure_end": (2.0 * ke1 / 3.0 + vir1 / 3.0) / side ** 3,
+            "force_err": err,
             "precision": "FP32 per-edge forces (compensated sums), FP64 integration and energies",
             "data": "synthetic (miniMD FCC lattice, seeded Maxwell velocities)"}
     md.close()
-    print(json.dumps(line), flush=True)
-    return 0
+    return line
+
+
+# Served capacity: the p99 job latency a rate must keep to count as sustained.
+P99_BOUND_S = 1.0
+CAPACITY_RATES = (200.0, 400.0, 800.0, 1600.0, 3200.0, 1e9)
 
 
 def run_served(args):
@@ -505,7 +655,11 @@ def run_served(args):
     execution (one job at a time through the partitioned force kernel) and
     serial plain execution (one job at a time, every force by the plain
     edge-parallel kernel), all admitting in arrival order, and continuous
-    batching admitting the smallest waiting job first."""
+    batching admitting the smallest waiting job first.  Then the capacity: the
+    same stream offered at rising rates (1e9/s: every job waiting at t = 0),
+    the highest rate whose p99 latency stays within P99_BOUND_S, and the
+    throughput there against serial plain execution's at the same rate.
+    Returns the leg's JSON object."""
     import irregular_gb300 as irr
 
     out = {"leg": "served", "jobs": args.jobs, "arrival_rate_per_s": 200.0,
@@ -515,21 +669,42 @@ def run_served(args):
     # kernels loaded; without it the first measured schedule would pay for both
     irr.serve(num_jobs=max(1, args.jobs // 4), mode=irr.IRR_SERVE_CONTINUOUS, arrival_rate=200.0,
               steps_per_job=50, budget_bytes=120e9, seed=SEED + 6)
+
+    def one(mode, policy, rate):
+        st, _ = irr.serve(num_jobs=args.jobs, mode=mode, policy=policy, arrival_rate=rate,
+                          steps_per_job=50, budget_bytes=120e9, seed=SEED + 5)
+        return {"p50_ms": st.p50_ms, "p99_ms": st.p99_ms, "mean_ms": st.mean_ms,
+                "max_ms": st.max_ms, "makespan_s": st.makespan_s,
+                "edges_per_s": st.edges_per_s, "jobs_done": int(st.jobs_done),
+                "max_resident": int(st.max_resident)}
+
     runs = ((irr.IRR_SERVE_CONTINUOUS, irr.IRR_SERVE_FIFO, "continuous"),
             (irr.IRR_SERVE_SERIAL, irr.IRR_SERVE_FIFO, "serial"),
             (irr.IRR_SERVE_SERIAL_PLAIN, irr.IRR_SERVE_FIFO, "serial_plain"),
             (irr.IRR_SERVE_CONTINUOUS, irr.IRR_SERVE_SJF, "continuous_sjf"))
     for mode, policy, name in runs:
-        st, _ = irr.serve(num_jobs=args.jobs, mode=mode, policy=policy, arrival_rate=200.0,
-                          steps_per_job=50, budget_bytes=120e9, seed=SEED + 5)
-        out[name] = {"p50_ms": st.p50_ms, "p99_ms": st.p99_ms, "mean_ms": st.mean_ms,
-                     "max_ms": st.max_ms, "makespan_s": st.makespan_s,
-                     "edges_per_s": st.edges_per_s, "jobs_done": int(st.jobs_done),
-                     "max_resident": int(st.max_resident)}
+        out[name] = one(mode, policy, 200.0)
     out["speedup_edges_per_s"] = out["continuous"]["edges_per_s"] / out["serial"]["edges_per_s"]
     out["speedup_vs_serial_plain"] = out["continuous"]["edges_per_s"] / out["serial_plain"]["edges_per_s"]
-    print(json.dumps(out), flush=True)
-    return 0
+    if args.capacity:
+        sweep = []
+        for rate in CAPACITY_RATES:
+            r = one(irr.IRR_SERVE_CONTINUOUS, irr.IRR_SERVE_FIFO, rate)
+            r["rate_per_s"] = rate
+            sweep.append(r)
+        ok = [r for r in sweep if r["p99_ms"] <= 1e3 * P99_BOUND_S]
+        best = max(ok, key=lambda r: r["rate_per_s"]) if ok else None
+        cap = {"p99_bound_s": P99_BOUND_S, "sweep": sweep,
+               "sustained_rate_per_s": best["rate_per_s"] if best else None}
+        if best:
+            plain = one(irr.IRR_SERVE_SERIAL_PLAIN, irr.IRR_SERVE_FIFO, best["rate_per_s"])
+            cap["at_sustained_rate"] = {"continuous_edges_per_s": best["edges_per_s"],
+                                        "continuous_p99_ms": best["p99_ms"],
+                                        "serial_plain_edges_per_s": plain["edges_per_s"],
+                                        "serial_plain_p99_ms": plain["p99_ms"],
+                                        "speedup_vs_serial_plain": best["edges_per_s"] / plain["edges_per_s"]}
+        out["capacity"] = cap
+    return out
 
 
 def main():
@@ -549,6 +724,8 @@ def main():
     ap.add_argument("--md-steps", type=int, default=1000)
     ap.add_argument("--jobs", type=int, default=200)
     ap.add_argument("--batch-steps", type=int, default=200)
+    ap.add_argument("--capacity", type=int, default=1,
+                    help="1: the served leg also sweeps the arrival rate for its capacity")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -556,12 +733,10 @@ def main():
         world = int(os.environ.get("WORLD_SIZE", "1"))
         rank = int(os.environ.get("RANK", "0"))
         return run_reference(args, rank, world)
-    if args.legs == "batched":
-        return run_batched(args)
-    if args.legs == "md":
-        return run_md(args)
-    if args.legs == "served":
-        return run_served(args)
+    if args.legs in ("batched", "md", "served"):
+        leg = {"batched": run_batched, "md": run_md, "served": run_served}[args.legs](args)
+        print(json.dumps(leg), flush=True)
+        return 0
     rank, world, local = dist_init(args)
     rc = run_ours(args, rank, world, local)
     if world > 1:

@@ -134,7 +134,10 @@ typedef struct irr_config {
                           them from global memory; -1 = tuned default               */
     int layout;        /* partitioned: enum irr_layout                               */
     int order;         /* partitioned with reorder: enum irr_order                   */
-    int reserved[6];
+    int wait_limit_us; /* partitioned: a device-side wait (a work item's entries, a free
+                          ring stage) gives up after this many microseconds and the
+                          next synchronising call returns IRR_ERR_DEVICE; 0 = 2 s    */
+    int reserved[5];
 } irr_config;
 
 typedef struct irr_handle irr_handle;
@@ -219,6 +222,15 @@ IRR_API int irr_get_result_device(irr_handle *h, void *d_out, int elm_size);
 
 /* Waits for the handle's stream and reports any device-side fault. */
 IRR_API int irr_sync(irr_handle *h);
+/* The limit of the partitioned kernel's device-side waits (irr_config
+ * wait_limit_us; limit_us <= 0 restores the 2 s default).  withhold_once != 0
+ * tests the time-out path: in the next irr_step the kernel's producers publish
+ * no work, so every consumer's wait runs out after the limit, the launch ends
+ * with nothing in flight, and the next synchronising call returns
+ * IRR_ERR_DEVICE; the step after that runs normally.  No counterpart in the
+ * reference, whose bucket-lock spins have no limit (moldyn/irregular/ros.cu:
+ * 10-68). */
+IRR_API int irr_set_wait_limit(irr_handle *h, int64_t limit_us, int withhold_once);
 IRR_API int irr_get_info(const irr_handle *h, irr_info *info);
 
 /* Partition outputs (partitioned mode, after irr_init), copied to host:
@@ -436,6 +448,15 @@ typedef struct irr_serve_job {
 } irr_serve_job;
 
 IRR_API void irr_serve_config_default(irr_serve_config *cfg);
+/* Job `job` of the stream that cfg describes, as irr_serve_run makes it (host
+ * code; no GPU): its atom count, box side, and initial state -- 3n FP64
+ * positions and 3n velocities, the job's own atom order; any output may be
+ * NULL.  A job's result can be replayed alone (irr_md_* on this state with
+ * cfg's dt, cutforce, skin and rebuild_every gives the same trajectory bit for
+ * bit) and checked against another implementation.  No counterpart in the
+ * reference. */
+IRR_API int irr_serve_job_state(const irr_serve_config *cfg, int job, int64_t *atoms,
+                                double *side, double *pos, double *vel);
 /* Runs the stream to completion; jobs_out (optional) has num_jobs records. */
 IRR_API int irr_serve_run(const irr_serve_config *cfg, irr_serve_stats *stats,
                           irr_serve_job *jobs_out);

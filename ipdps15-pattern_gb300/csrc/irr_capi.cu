@@ -328,6 +328,7 @@ int irr_create(const irr_config* cfg, irr_handle** out)
         return IRR_ERR_ARG;
     if (c.layout < IRR_LAYOUT_AUTO || c.layout > IRR_LAYOUT_SLICED) return IRR_ERR_ARG;
     if (c.order != IRR_ORDER_HILBERT && c.order != IRR_ORDER_MORTON) return IRR_ERR_ARG;
+    if (c.wait_limit_us < 0) return IRR_ERR_ARG;
     if (c.lanes_per_row != 0 && c.lanes_per_row != 1 && c.lanes_per_row != 2 && c.lanes_per_row != 4 &&
         c.lanes_per_row != 8 && c.lanes_per_row != 16 && c.lanes_per_row != 32)
         return IRR_ERR_ARG;
@@ -356,6 +357,7 @@ int irr_create(const irr_config* cfg, irr_handle** out)
         return IRR_ERR_CUDA;
     }
     h->stream = h->own_stream;
+    if (c.wait_limit_us > 0) h->wait.wait_ns = 1000ull * (uint64_t)c.wait_limit_us;
     h->shape.lanes_per_row = c.lanes_per_row ? c.lanes_per_row : 4;
     h->shape.block_nodes = c.block_nodes ? c.block_nodes : 1024;
     h->shape.stage_smem = c.stage_smem < 0 ? 1 : (c.stage_smem ? 1 : 0);
@@ -533,8 +535,10 @@ int irr_step(irr_handle* h)
         return IRR_OK;
     }
     H_CUDA(h, cudaMemsetAsync(h->d_queue, 0, sizeof(int), h->stream), "clear work queue");
+    const WaitPolicy wp = h->wait;
+    h->wait.withhold = 0;  // one step only
     H_CUDA(h, launch_tiled(h->shape, h->d_inst, h->d_items, h->num_items, h->d_queue,
-                           h->sms * kCtasPerSm, h->d_status, h->stream, &h->inst, 1),
+                           h->sms * kCtasPerSm, h->d_status, h->stream, &h->inst, 1, wp),
            "tiled kernel");
     return IRR_OK;
 }
@@ -587,6 +591,15 @@ int irr_sync(irr_handle* h)
     if (!h) return IRR_ERR_ARG;
     DeviceGuard dev_guard(h->device);
     return check_status(h);
+}
+
+int irr_set_wait_limit(irr_handle* h, int64_t limit_us, int withhold_once)
+{
+    if (!h) return IRR_ERR_ARG;
+    if (limit_us > (int64_t)1 << 40) return fail(h, IRR_ERR_ARG, "wait limit above 2^40 us");
+    h->wait.wait_ns = limit_us > 0 ? 1000ull * (uint64_t)limit_us : kDefaultWaitNs;
+    h->wait.withhold = withhold_once ? 1 : 0;
+    return IRR_OK;
 }
 
 int irr_get_info(const irr_handle* h, irr_info* info)

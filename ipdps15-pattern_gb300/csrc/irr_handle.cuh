@@ -48,6 +48,7 @@ struct irr_handle {
     int num_items = 0;
     int* d_status = nullptr;
     int* d_queue = nullptr;      // work-queue cursor, cleared before each launch
+    irr::WaitPolicy wait{};      // device-side wait limit; withhold: the next step only
     void* d_out = nullptr;       // result staging for host reads
     size_t out_cap = 0;
     int64_t dev_bytes = 0;

@@ -165,6 +165,15 @@ inline cudaError_t irr_malloc_async(T** p, size_t bytes, cudaStream_t s)
     return irr_malloc_async(reinterpret_cast<void**>(p), bytes, s);
 }
 
+// How long a kernel's device-side waits may last before it gives up
+// (kStatusWaitTimeout), and the one-shot test of that path: withhold != 0
+// makes the producers publish nothing, so every consumer wait runs out.
+constexpr uint64_t kDefaultWaitNs = 2000000000ull;  // 2 s: far above any work item's time
+struct WaitPolicy {
+    uint64_t wait_ns = kDefaultWaitNs;
+    int withhold = 0;
+};
+
 // -- reduction kernels (irr_reduce.cu) --
 cudaError_t launch_plain(const float4* pos, const int2* edges, int64_t e, float4* force,
                          const LawParams& law, cudaStream_t s);
@@ -176,7 +185,7 @@ cudaError_t launch_plain(const float4* pos, const int2* edges, int64_t e, float4
 cudaError_t launch_tiled(const TiledShape& shape, const InstDesc* d_insts,
                          const WorkItem* d_items, int num_items, int* d_queue, int grid,
                          int* d_status, cudaStream_t s, const InstDesc* host_insts = nullptr,
-                         int num_insts = 0);
+                         int num_insts = 0, const WaitPolicy& wp = WaitPolicy{});
 
 // -- data movement (irr_partition.cu) --
 // Raw node records (12/16/24 bytes) -> float4, optionally gathered: dst[k] =

@@ -118,7 +118,6 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
     }
 }
 
-constexpr uint64_t kWaitNs = 2000000000ull;  // 2 s: far above any item's time
 
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar)
 {
@@ -468,13 +467,17 @@ __device__ __forceinline__ void consume_sliced(const WorkItem& w, const InstHot&
 // rows, arrive on `empty` (kConsumerWarps arrivals free the stage).  Waits
 // suspend the thread until the phase completes (mbar_try_wait).  Every
 // wait is bounded; a wait that gives up sets kStatusWaitTimeout, waits once
-// more (bounded) for a copy that may be in flight, and leaves.
+// more (bounded) for a copy that may be in flight, and leaves.  wait_ns
+// bounds each wait; withhold != 0 (a test of that path) makes every producer
+// leave before publishing its first stage, so every consumer's first wait
+// runs out and the launch ends with kStatusWaitTimeout and nothing in flight.
 //
 // Src (SrcGlobal, SrcOne, SrcTable): where the instance fields come from.
 template <bool PERIODIC, int G, class Src>
 __global__ void __launch_bounds__(kPipeThreads, kCtasPerSm) tiled_kernel(
     const InstDesc* __restrict__ insts, const WorkItem* __restrict__ items, int num_items,
-    int* queue, int* status, int use_stages, const __grid_constant__ Src src)
+    int* queue, int* status, int use_stages, uint64_t wait_ns, int withhold,
+    const __grid_constant__ Src src)
 {
     constexpr bool ONE = std::is_same<Src, SrcOne>::value;
     constexpr bool TABLE = std::is_same<Src, SrcTable>::value;
@@ -497,12 +500,12 @@ __global__ void __launch_bounds__(kPipeThreads, kCtasPerSm) tiled_kernel(
     __syncthreads();
 
     if (warp == kConsumerWarps) {
-        if (lane != 0) return;
+        if (lane != 0 || withhold) return;
         int next_item = 0, chunk_left = 0;
         for (int k = 0;; k++) {
             const int s = k % kStages;
             const int use = k / kStages;
-            if (use > 0 && !mbar_wait_bounded(&empty[s], (uint32_t)(use - 1) & 1u, kWaitNs)) {
+            if (use > 0 && !mbar_wait_bounded(&empty[s], (uint32_t)(use - 1) & 1u, wait_ns)) {
                 atomicOr(status, kStatusWaitTimeout);
                 return;  // nothing of this stage is in flight: its last copy was consumed
             }
@@ -541,9 +544,9 @@ __global__ void __launch_bounds__(kPipeThreads, kCtasPerSm) tiled_kernel(
     InstHot hot{};
     for (int k = 0;; k++) {
         const int s = k % kStages;
-        if (!mbar_wait_bounded(&full[s], (uint32_t)(k / kStages) & 1u, kWaitNs)) {
+        if (!mbar_wait_bounded(&full[s], (uint32_t)(k / kStages) & 1u, wait_ns)) {
             if (lane == 0) atomicOr(status, kStatusWaitTimeout);
-            mbar_wait_bounded(&full[s], (uint32_t)(k / kStages) & 1u, kWaitNs);
+            mbar_wait_bounded(&full[s], (uint32_t)(k / kStages) & 1u, wait_ns);
             return;
         }
         const int it = s_item[s];
@@ -582,7 +585,7 @@ __global__ void __launch_bounds__(kPipeThreads, kCtasPerSm) tiled_kernel(
 template <bool PERIODIC, int G, class Src>
 cudaError_t launch_tiled_src(const TiledShape& shape, const InstDesc* d_insts,
                              const WorkItem* d_items, int num_items, int* d_queue, int grid,
-                             int* d_status, cudaStream_t s, const Src& src)
+                             int* d_status, cudaStream_t s, const Src& src, const WaitPolicy& wp)
 {
     auto kern = tiled_kernel<PERIODIC, G, Src>;
     const size_t smem =
@@ -592,7 +595,7 @@ cudaError_t launch_tiled_src(const TiledShape& shape, const InstDesc* d_insts,
                                           (int)smem));
     if (grid <= 0 || num_items <= 0) return cudaSuccess;
     kern<<<grid, kPipeThreads, smem, s>>>(d_insts, d_items, num_items, d_queue, d_status,
-                                          shape.stage_smem, src);
+                                          shape.stage_smem, wp.wait_ns, wp.withhold, src);
     return cudaGetLastError();
 }
 
@@ -600,11 +603,11 @@ template <bool PERIODIC, int G>
 cudaError_t launch_tiled_g(const TiledShape& shape, const InstDesc* d_insts,
                            const WorkItem* d_items, int num_items, int* d_queue, int grid,
                            int* d_status, cudaStream_t s, const InstDesc* host_insts,
-                           int num_insts)
+                           int num_insts, const WaitPolicy& wp)
 {
     if (host_insts && num_insts == 1)
         return launch_tiled_src<PERIODIC, G>(shape, d_insts, d_items, num_items, d_queue, grid,
-                                             d_status, s, SrcOne{host_insts[0]});
+                                             d_status, s, SrcOne{host_insts[0]}, wp);
     if (host_insts && num_insts > 1 && num_insts <= kTableInsts) {
         static thread_local SrcTable t;  // 28 KB: kept off the stack
         for (int k = 0; k < num_insts; k++) {
@@ -612,23 +615,24 @@ cudaError_t launch_tiled_g(const TiledShape& shape, const InstDesc* d_insts,
             t.h[k] = HotEntry{d.pos, HotLaw{d.law.half2, d.law.rc2, d.law.band}, 0.f};
         }
         return launch_tiled_src<PERIODIC, G>(shape, d_insts, d_items, num_items, d_queue, grid,
-                                             d_status, s, t);
+                                             d_status, s, t, wp);
     }
     return launch_tiled_src<PERIODIC, G>(shape, d_insts, d_items, num_items, d_queue, grid,
-                                         d_status, s, SrcGlobal{0});
+                                         d_status, s, SrcGlobal{0}, wp);
 }
 
 template <bool PERIODIC>
 cudaError_t launch_tiled_p(const TiledShape& sh, const InstDesc* a, const WorkItem* b, int n,
-                           int* q, int grid, int* st, cudaStream_t s, const InstDesc* hi, int ni)
+                           int* q, int grid, int* st, cudaStream_t s, const InstDesc* hi, int ni,
+                           const WaitPolicy& wp)
 {
     switch (sh.lanes_per_row) {
-    case 1: return launch_tiled_g<PERIODIC, 1>(sh, a, b, n, q, grid, st, s, hi, ni);
-    case 2: return launch_tiled_g<PERIODIC, 2>(sh, a, b, n, q, grid, st, s, hi, ni);
-    case 4: return launch_tiled_g<PERIODIC, 4>(sh, a, b, n, q, grid, st, s, hi, ni);
-    case 8: return launch_tiled_g<PERIODIC, 8>(sh, a, b, n, q, grid, st, s, hi, ni);
-    case 16: return launch_tiled_g<PERIODIC, 16>(sh, a, b, n, q, grid, st, s, hi, ni);
-    case 32: return launch_tiled_g<PERIODIC, 32>(sh, a, b, n, q, grid, st, s, hi, ni);
+    case 1: return launch_tiled_g<PERIODIC, 1>(sh, a, b, n, q, grid, st, s, hi, ni, wp);
+    case 2: return launch_tiled_g<PERIODIC, 2>(sh, a, b, n, q, grid, st, s, hi, ni, wp);
+    case 4: return launch_tiled_g<PERIODIC, 4>(sh, a, b, n, q, grid, st, s, hi, ni, wp);
+    case 8: return launch_tiled_g<PERIODIC, 8>(sh, a, b, n, q, grid, st, s, hi, ni, wp);
+    case 16: return launch_tiled_g<PERIODIC, 16>(sh, a, b, n, q, grid, st, s, hi, ni, wp);
+    case 32: return launch_tiled_g<PERIODIC, 32>(sh, a, b, n, q, grid, st, s, hi, ni, wp);
     default: return cudaErrorInvalidValue;
     }
 }
@@ -653,13 +657,14 @@ cudaError_t launch_plain(const float4* pos, const int2* edges, int64_t e, float4
 
 cudaError_t launch_tiled(const TiledShape& shape, const InstDesc* d_insts,
                          const WorkItem* d_items, int num_items, int* d_queue, int grid,
-                         int* d_status, cudaStream_t s, const InstDesc* host_insts, int num_insts)
+                         int* d_status, cudaStream_t s, const InstDesc* host_insts, int num_insts,
+                         const WaitPolicy& wp)
 {
     if (!d_queue) return cudaErrorInvalidValue;
     return shape.periodic ? launch_tiled_p<true>(shape, d_insts, d_items, num_items, d_queue, grid,
-                                                 d_status, s, host_insts, num_insts)
+                                                 d_status, s, host_insts, num_insts, wp)
                           : launch_tiled_p<false>(shape, d_insts, d_items, num_items, d_queue,
-                                                  grid, d_status, s, host_insts, num_insts);
+                                                  grid, d_status, s, host_insts, num_insts, wp);
 }
 
 void make_work_items(const uint32_t* row_off, int64_t n, int inst, int max_rows, int staged,

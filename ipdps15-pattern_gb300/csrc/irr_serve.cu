@@ -455,6 +455,25 @@ void irr_serve_config_default(irr_serve_config* c)
     c->seed = 20260005;
 }
 
+int irr_serve_job_state(const irr_serve_config* cfg, int job, int64_t* atoms, double* side,
+                        double* pos, double* vel)
+{
+    if (!cfg || job < 0 || job >= cfg->num_jobs || cfg->min_atoms < 32 ||
+        cfg->max_atoms < cfg->min_atoms || !(cfg->density > 0) || !(cfg->temperature > 0))
+        return IRR_ERR_ARG;
+    const std::vector<JobSpec> jobs = make_jobs(cfg);
+    const JobSpec& j = jobs[(size_t)job];
+    if (atoms) *atoms = j.atoms;
+    if (side) *side = j.side;
+    if (pos || vel) {
+        std::vector<double> p, v;
+        initial_state(j, cfg, p, v);
+        if (pos) std::copy(p.begin(), p.end(), pos);
+        if (vel) std::copy(v.begin(), v.end(), vel);
+    }
+    return IRR_OK;
+}
+
 int irr_serve_run(const irr_serve_config* cfg, irr_serve_stats* st, irr_serve_job* out)
 {
     if (!cfg || !st) return IRR_ERR_ARG;

@@ -53,7 +53,7 @@ class Config(C.Structure):
     _fields_ = [("device", C.c_int), ("exec", C.c_int), ("map_idx", C.c_int),
                 ("reduce_idx", C.c_int), ("block_nodes", C.c_int), ("lanes_per_row", C.c_int),
                 ("reorder", C.c_int), ("stage_smem", C.c_int), ("layout", C.c_int),
-                ("order", C.c_int), ("reserved", C.c_int * 6)]
+                ("order", C.c_int), ("wait_limit_us", C.c_int), ("reserved", C.c_int * 5)]
 
 
 class Info(C.Structure):
@@ -135,6 +135,7 @@ _SIGS = {
     "irr_get_result": (C.c_int, [P, P, C.c_int]),
     "irr_get_result_device": (C.c_int, [P, P, C.c_int]),
     "irr_sync": (C.c_int, [P]),
+    "irr_set_wait_limit": (C.c_int, [P, I64, C.c_int]),
     "irr_get_info": (C.c_int, [P, C.POINTER(Info)]),
     "irr_get_partition": (C.c_int, [P, P, P, P]),
     "irr_neighbor_build": (C.c_int, [C.c_int, P, P, C.c_int, C.c_int, I64, C.c_float, C.c_float,
@@ -158,6 +159,8 @@ _SIGS = {
     "irr_autotune": (C.c_int, [P]),
     "irr_serve_config_default": (None, [C.POINTER(ServeConfig)]),
     "irr_serve_run": (C.c_int, [C.POINTER(ServeConfig), C.POINTER(ServeStats), P]),
+    "irr_serve_job_state": (C.c_int, [C.POINTER(ServeConfig), C.c_int, C.POINTER(I64),
+                                      C.POINTER(C.c_double), P, P]),
     "irr_md_config_default": (None, [C.POINTER(MDConfig)]),
     "irr_md_create": (C.c_int, [C.POINTER(MDConfig), P, P, I64, C.POINTER(P)]),
     "irr_md_destroy": (C.c_int, [P]),
@@ -382,6 +385,12 @@ class Handle:
     def sync(self):
         self._check(load().irr_sync(self._h), "irr_sync")
 
+    def set_wait_limit(self, limit_us: int, withhold_once: bool = False):
+        """irr_set_wait_limit: the device-side wait limit, and (withhold_once)
+        a next step whose waits all run out, to test the time-out path."""
+        self._check(load().irr_set_wait_limit(self._h, int(limit_us), int(withhold_once)),
+                    "irr_set_wait_limit")
+
     def get_result(self, out: Optional[np.ndarray] = None, elm_size: int = 12) -> np.ndarray:
         info = self.info()
         n = info.num_nodes
@@ -403,15 +412,18 @@ class Handle:
     def autotune(self):
         self._check(load().irr_autotune(self._h), "irr_autotune")
 
-    def partition(self):
+    def partition(self, with_entries: bool = True):
+        """(perm, row_off, col) of a partitioned handle; col is None when
+        with_entries is False (the entries are not copied)."""
         inf = self.info()
         n, m = inf.num_nodes, inf.num_entries
         perm = np.zeros(n, np.int32)
         row_off = np.zeros(n + 1, np.int64)
-        col = np.zeros(max(m, 1), np.int32)
-        self._check(load().irr_get_partition(self._h, _ptr(perm), _ptr(row_off), _ptr(col)),
+        col = np.zeros(max(m, 1), np.int32) if with_entries else None
+        self._check(load().irr_get_partition(self._h, _ptr(perm), _ptr(row_off),
+                                             _ptr(col) if with_entries else None),
                     "irr_get_partition")
-        return perm, row_off, col[:m]
+        return perm, row_off, (col[:m] if with_entries else None)
 
 
 def read_graph(path: str, one_based: bool = False) -> np.ndarray:
@@ -516,6 +528,58 @@ def serve(**kw):
     if rc != IRR_OK:
         raise IrregularError(rc, f"irr_serve_run: {L.irr_status_string(rc).decode()}")
     return stats, list(jobs)[: cfg.num_jobs]
+
+
+def serve_job_state(job: int, **kw):
+    """Job `job` of the stream the serve() keywords describe (irr_serve_job_state,
+    host only): (atoms, side, positions (n, 3), velocities (n, 3))."""
+    L = load()
+    cfg = ServeConfig()
+    L.irr_serve_config_default(C.byref(cfg))
+    for k, v in kw.items():
+        setattr(cfg, k, v)
+    n, side = I64(), C.c_double()
+    rc = L.irr_serve_job_state(C.byref(cfg), int(job), C.byref(n), C.byref(side), None, None)
+    if rc != IRR_OK:
+        raise IrregularError(rc, f"irr_serve_job_state: {L.irr_status_string(rc).decode()}")
+    pos = np.zeros((n.value, 3), np.float64)
+    vel = np.zeros((n.value, 3), np.float64)
+    rc = L.irr_serve_job_state(C.byref(cfg), int(job), None, None, _ptr(pos), _ptr(vel))
+    if rc != IRR_OK:
+        raise IrregularError(rc, "irr_serve_job_state")
+    return n.value, side.value, pos, vel
+
+
+def serve_job_sizes(**kw):
+    """Atom counts of every job of the stream the serve() keywords describe."""
+    L = load()
+    cfg = ServeConfig()
+    L.irr_serve_config_default(C.byref(cfg))
+    for k, v in kw.items():
+        setattr(cfg, k, v)
+    out = []
+    for j in range(cfg.num_jobs):
+        n = I64()
+        rc = L.irr_serve_job_state(C.byref(cfg), j, C.byref(n), None, None, None)
+        if rc != IRR_OK:
+            raise IrregularError(rc, "irr_serve_job_state")
+        out.append(n.value)
+    return out
+
+
+def state_digest(pos) -> int:
+    """The digest irr_serve_job.state_hash reports, computed on the host: the sum
+    mod 2^64, over atoms k (the caller's order) and components c, of
+    mix64(bits(x_kc) + 0x9e3779b97f4a7c15 * (3k + c + 1)), mix64 being
+    SplitMix64's finaliser."""
+    x = np.ascontiguousarray(pos, np.float64).reshape(-1).view(np.uint64)
+    k = np.arange(x.shape[0], dtype=np.uint64)
+    with np.errstate(over="ignore"):
+        z = x + np.uint64(0x9E3779B97F4A7C15) * (k + np.uint64(1))
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+        return int(z.sum(dtype=np.uint64))
 
 
 class MD:

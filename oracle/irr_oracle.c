@@ -91,6 +91,26 @@ void orc_lj_reduce_f64(int64_t n, const double *pos, int64_t e, const int32_t *e
     }
 }
 
+/* The scale of the per-result error metric: per node, the sum over its
+ * in-cutoff edges of the FP64 edge force's largest component |f_e|inf. */
+void orc_lj_edge_scale_inf(int64_t n, const double *pos, int64_t e, const int32_t *edges,
+                           const orc_lj_param *p, double *sinf)
+{
+    memset(sinf, 0, sizeof(double) * (size_t)n);
+    for (int64_t t = 0; t < e; t++) {
+        int32_t i = edges[2 * t], j = edges[2 * t + 1];
+        double d[3], s;
+        if (!lj_edge_f64(pos, i, j, p, d, &s, NULL)) continue;
+        double m = 0.0;
+        for (int c = 0; c < 3; c++) {
+            const double a = fabs(d[c] * s);
+            if (a > m) m = a;
+        }
+        sinf[i] += m;
+        sinf[j] += m;
+    }
+}
+
 void orc_lj_reduce_refnum_f32(int64_t n, const double *pos, int64_t e, const int32_t *edges,
                               const orc_lj_param *p, float *f)
 {
@@ -714,8 +734,27 @@ static double wrap_box(double x, double L)
     return x;
 }
 
+/* The MD's work is split over `threads` host threads: the list by row ranges
+ * (each range's pairs in the serial list's order, ranges concatenated in
+ * order: the serial list exactly), the forces by edge ranges into per-thread
+ * FP64 arrays summed in thread order (the FP64 result of another summation
+ * order: ~1e-16 relative). */
+typedef struct {
+    int64_t n, r0, r1, cap, count;
+    const float *fp;
+    float box, cut2;
+    int32_t *out;
+} md_list_arg;
+
+static void *md_list_worker(void *v)
+{
+    md_list_arg *a = (md_list_arg *)v;
+    a->count = orc_neighbor_half_list_rows(a->n, a->fp, a->box, a->cut2, a->r0, a->r1, a->out, a->cap);
+    return NULL;
+}
+
 static int64_t md_list(int64_t n, const double *pos, double side, double lc, float **fpos,
-                       int32_t **edges)
+                       int32_t **edges, int threads)
 {
     float *fp = *fpos;
     float Lf = (float)side;
@@ -723,22 +762,52 @@ static int64_t md_list(int64_t n, const double *pos, double side, double lc, flo
         float v = (float)pos[k];
         fp[k] = v >= Lf ? 0.0f : v;
     }
-    int64_t e = orc_neighbor_half_list(n, fp, Lf, (float)(lc * lc), NULL, 0);
+    if (threads < 1) threads = 1;
+    if (threads > 64) threads = 64;
+    md_list_arg args[64];
+    pthread_t tids[64];
+    for (int t = 0; t < threads; t++) {
+        md_list_arg a = {n, n * t / threads, n * (t + 1) / threads, 0, 0, fp, Lf, (float)(lc * lc), NULL};
+        args[t] = a;
+    }
+    for (int t = 1; t < threads; t++) pthread_create(&tids[t], NULL, md_list_worker, &args[t]);
+    md_list_worker(&args[0]);
+    for (int t = 1; t < threads; t++) pthread_join(tids[t], NULL);
+    int64_t e = 0;
+    for (int t = 0; t < threads; t++) e += args[t].count;
     free(*edges);
     *edges = (int32_t *)malloc(sizeof(int32_t) * 2 * (size_t)(e > 0 ? e : 1));
-    orc_neighbor_half_list(n, fp, Lf, (float)(lc * lc), *edges, e);
+    int64_t off = 0;
+    for (int t = 0; t < threads; t++) {
+        args[t].out = *edges + 2 * off;
+        args[t].cap = args[t].count;
+        off += args[t].count;
+    }
+    for (int t = 1; t < threads; t++) pthread_create(&tids[t], NULL, md_list_worker, &args[t]);
+    md_list_worker(&args[0]);
+    for (int t = 1; t < threads; t++) pthread_join(tids[t], NULL);
     return e;
 }
 
-static void md_forces(int64_t n, const double *pos, int64_t e, const int32_t *edges,
-                      const orc_lj_param *p, double *f, double *pe)
+typedef struct {
+    int64_t n, e0, e1;
+    const double *pos;
+    const int32_t *edges;
+    const orc_lj_param *p;
+    double *f;
+    double u;
+} md_force_arg;
+
+static void *md_force_worker(void *v)
 {
-    memset(f, 0, sizeof(double) * 3 * (size_t)n);
+    md_force_arg *a = (md_force_arg *)v;
+    double *f = a->f;
+    memset(f, 0, sizeof(double) * 3 * (size_t)a->n);
     double u = 0.0;
-    for (int64_t t = 0; t < e; t++) {
-        int32_t i = edges[2 * t], j = edges[2 * t + 1];
+    for (int64_t t = a->e0; t < a->e1; t++) {
+        int32_t i = a->edges[2 * t], j = a->edges[2 * t + 1];
         double d[3], s;
-        if (!lj_edge_f64(pos, i, j, p, d, &s, NULL)) continue;
+        if (!lj_edge_f64(a->pos, i, j, a->p, d, &s, NULL)) continue;
         double rd = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
         double r6 = 1.0 / (rd * rd * rd);
         u += 4.0 * r6 * (r6 - 1.0);
@@ -747,25 +816,72 @@ static void md_forces(int64_t n, const double *pos, int64_t e, const int32_t *ed
             f[3 * (int64_t)j + c] -= 48.0 * d[c] * s;
         }
     }
+    a->u = u;
+    return NULL;
+}
+
+/* part: threads - 1 scratch force arrays of 3n doubles (thread 0 writes f). */
+static void md_forces(int64_t n, const double *pos, int64_t e, const int32_t *edges,
+                      const orc_lj_param *p, double *f, double *pe, int threads, double *part)
+{
+    if (threads < 1) threads = 1;
+    if (threads > 64) threads = 64;
+    md_force_arg args[64];
+    pthread_t tids[64];
+    for (int t = 0; t < threads; t++) {
+        md_force_arg a = {n, e * t / threads, e * (t + 1) / threads, pos, edges, p,
+                          t == 0 ? f : part + (size_t)(t - 1) * 3 * (size_t)n, 0.0};
+        args[t] = a;
+    }
+    for (int t = 1; t < threads; t++) pthread_create(&tids[t], NULL, md_force_worker, &args[t]);
+    md_force_worker(&args[0]);
+    for (int t = 1; t < threads; t++) pthread_join(tids[t], NULL);
+    double u = args[0].u;
+    for (int t = 1; t < threads; t++) {
+        const double *g = args[t].f;
+        for (int64_t k = 0; k < 3 * n; k++) f[k] += g[k];
+        u += args[t].u;
+    }
     if (pe) *pe = u;
 }
 
-int orc_md_run(int64_t n, double *pos, double *vel, double side, double cutforce, double skin,
-               double dt, int steps, int rebuild_every, double *ke, double *pe)
+/* The positions the forces are evaluated at: the FP64 state itself, or (as
+ * the GPU evaluates them) its float copy, a value that rounds up to the box
+ * side wrapping to 0, widened back to double. */
+static const double *md_force_positions(int64_t n, const double *pos, double side, double *copy)
+{
+    if (!copy) return pos;
+    const float Lf = (float)side;
+    for (int64_t k = 0; k < 3 * n; k++) {
+        const float v = (float)pos[k];
+        copy[k] = (double)(v >= Lf ? 0.0f : v);
+    }
+    return copy;
+}
+
+int orc_md_run_mt(int64_t n, double *pos, double *vel, double side, double cutforce, double skin,
+                  double dt, int steps, int rebuild_every, double *ke, double *pe, int threads,
+                  int float_forces)
 {
     if (n < 2 || !(side > 0) || rebuild_every < 1) return -1;
+    if (threads < 1) threads = 1;
+    if (threads > 64) threads = 64;
     orc_lj_param p = {side, cutforce * cutforce, 1};
     float *fpos = (float *)malloc(sizeof(float) * 3 * (size_t)n);
     double *f = (double *)malloc(sizeof(double) * 3 * (size_t)n);
+    double *part = threads > 1 ? (double *)malloc(sizeof(double) * 3 * (size_t)n * (size_t)(threads - 1)) : NULL;
+    double *copy = float_forces ? (double *)malloc(sizeof(double) * 3 * (size_t)n) : NULL;
     int32_t *edges = NULL;
-    if (!fpos || !f) {
+    if (!fpos || !f || (threads > 1 && !part) || (float_forces && !copy)) {
         free(fpos);
         free(f);
+        free(part);
+        free(copy);
         return -1;
     }
     for (int64_t k = 0; k < 3 * n; k++) pos[k] = wrap_box(pos[k], side);
-    int64_t e = md_list(n, pos, side, cutforce + skin, &fpos, &edges);
-    md_forces(n, pos, e, edges, &p, f, NULL);
+    int64_t e = md_list(n, pos, side, cutforce + skin, &fpos, &edges, threads);
+    md_forces(n, md_force_positions(n, pos, side, copy), e, edges, &p, f, NULL, threads, part);
     int since = 0;
     for (int t = 0; t < steps; t++) {
         for (int64_t k = 0; k < 3 * n; k++) {
@@ -773,13 +889,13 @@ int orc_md_run(int64_t n, double *pos, double *vel, double side, double cutforce
             pos[k] = wrap_box(pos[k] + dt * vel[k], side);
         }
         if (++since >= rebuild_every) {
-            e = md_list(n, pos, side, cutforce + skin, &fpos, &edges);
+            e = md_list(n, pos, side, cutforce + skin, &fpos, &edges, threads);
             since = 0;
         }
-        md_forces(n, pos, e, edges, &p, f, NULL);
+        md_forces(n, md_force_positions(n, pos, side, copy), e, edges, &p, f, NULL, threads, part);
         for (int64_t k = 0; k < 3 * n; k++) vel[k] += 0.5 * dt * f[k];
     }
-    if (pe) md_forces(n, pos, e, edges, &p, f, pe);
+    if (pe) md_forces(n, md_force_positions(n, pos, side, copy), e, edges, &p, f, pe, threads, part);
     if (ke) {
         double s = 0.0;
         for (int64_t k = 0; k < 3 * n; k++) s += vel[k] * vel[k];
@@ -787,6 +903,14 @@ int orc_md_run(int64_t n, double *pos, double *vel, double side, double cutforce
     }
     free(fpos);
     free(f);
+    free(part);
+    free(copy);
     free(edges);
     return 0;
+}
+
+int orc_md_run(int64_t n, double *pos, double *vel, double side, double cutforce, double skin,
+               double dt, int steps, int rebuild_every, double *ke, double *pe)
+{
+    return orc_md_run_mt(n, pos, vel, side, cutforce, skin, dt, steps, rebuild_every, ke, pe, 1, 0);
 }

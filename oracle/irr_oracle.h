@@ -48,6 +48,8 @@ typedef struct {
  * sabs (optional): per node and component, the sum over incident in-cutoff
  * edges of |d_c| * (r^-14 + r^-8/2) -- the magnitude of the terms before
  * cancellation, used as the per-node error scale. */
+void orc_lj_edge_scale_inf(int64_t n, const double *pos, int64_t e, const int32_t *edges,
+                           const orc_lj_param *p, double *sinf);
 void orc_lj_reduce_f64(int64_t n, const double *pos, int64_t e, const int32_t *edges,
                        const orc_lj_param *p, double *f, double *sabs);
 
@@ -103,6 +105,9 @@ int64_t orc_neighbor_half_list_rows(int64_t n, const float *pos, float box, floa
  * cutforce + skin) rebuilt after the drift of every rebuild_every-th step.
  * pos, vel: 3n doubles, updated in place.  ke / pe (optional) receive the
  * final kinetic and potential (4(r^-12 - r^-6) inside the cutoff) energy. */
+int orc_md_run_mt(int64_t n, double *pos, double *vel, double side, double cutforce, double skin,
+                  double dt, int steps, int rebuild_every, double *ke, double *pe, int threads,
+                  int float_forces);
 int orc_md_run(int64_t n, double *pos, double *vel, double side, double cutforce, double skin,
                double dt, int steps, int rebuild_every, double *ke, double *pe);
 

@@ -64,6 +64,7 @@ def lib():
         i64 = C.c_int64
         L.orc_lj_reduce_f64.argtypes = [i64, P, i64, P, C.POINTER(LJParam), P, P]
         L.orc_lj_reduce_refnum_f32.argtypes = [i64, P, i64, P, C.POINTER(LJParam), P]
+        L.orc_lj_edge_scale_inf.argtypes = [i64, P, i64, P, C.POINTER(LJParam), P]
         L.orc_cpu_executor.argtypes = [i64, P, i64, P, C.POINTER(LJParam), C.c_int, i64, P,
                                        C.POINTER(C.c_double)]
         L.orc_cpu_executor.restype = C.c_int
@@ -79,6 +80,10 @@ def lib():
         L.orc_md_run.argtypes = [i64, P, P, C.c_double, C.c_double, C.c_double, C.c_double,
                                  C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.orc_md_run.restype = C.c_int
+        L.orc_md_run_mt.argtypes = [i64, P, P, C.c_double, C.c_double, C.c_double, C.c_double,
+                                    C.c_int, C.c_int, C.POINTER(C.c_double),
+                                    C.POINTER(C.c_double), C.c_int, C.c_int]
+        L.orc_md_run_mt.restype = C.c_int
         L.orc_fcc_moldyn.argtypes = [C.c_int, C.c_double, P]
         L.orc_fcc_minimd.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, P, i64]
         L.orc_fcc_minimd.restype = i64
@@ -117,6 +122,17 @@ def lj_reduce_f64(pos, edges, param: LJParam):
     s = np.zeros((n, 3), np.float64)
     lib().orc_lj_reduce_f64(n, _p(pos), edges.shape[0], _p(edges), C.byref(param), _p(f), _p(s))
     return f, s
+
+
+def lj_edge_scale_inf(pos, edges, param: LJParam) -> np.ndarray:
+    """Per node: the sum over its in-cutoff edges of max_c |f_e,c| (FP64), the
+    scale of the per-result error metric (helpers.result_error)."""
+    pos = _pos64(pos)
+    edges = _edges(edges)
+    n = pos.shape[0]
+    s = np.zeros(n, np.float64)
+    lib().orc_lj_edge_scale_inf(n, _p(pos), edges.shape[0], _p(edges), C.byref(param), _p(s))
+    return s
 
 
 def lj_reduce_refnum(pos, edges, param: LJParam) -> np.ndarray:
@@ -214,13 +230,20 @@ def neighbor_count(pos32, box: float, list_cut2: float) -> int:
 
 
 def md_run(pos, vel, side: float, cutforce: float, skin: float, dt: float, steps: int,
-           rebuild_every: int):
-    """FP64 reference MD; returns (pos, vel, kinetic, potential)."""
+           rebuild_every: int, threads: int = 0, float_forces: bool = False):
+    """FP64 reference MD; returns (pos, vel, kinetic, potential).  threads = 0:
+    all host cores (the list is the serial one; forces are summed per thread
+    in a fixed order, FP64 to ~1e-16).  float_forces: evaluate the (FP64) forces
+    at the float copy of the positions, as the GPU's FP32 reduction does, so
+    that a comparison isolates the per-edge FP32 arithmetic."""
     p = np.array(pos, np.float64).reshape(-1, 3).copy()
     v = np.array(vel, np.float64).reshape(-1, 3).copy()
     ke, pe = C.c_double(), C.c_double()
-    rc = lib().orc_md_run(p.shape[0], _p(p), _p(v), float(side), float(cutforce), float(skin),
-                          float(dt), int(steps), int(rebuild_every), C.byref(ke), C.byref(pe))
+    if threads <= 0:
+        threads = min(os.cpu_count() or 1, 32)
+    rc = lib().orc_md_run_mt(p.shape[0], _p(p), _p(v), float(side), float(cutforce), float(skin),
+                             float(dt), int(steps), int(rebuild_every), C.byref(ke), C.byref(pe),
+                             int(threads), int(bool(float_forces)))
     if rc != 0:
         raise ValueError("orc_md_run failed")
     return p, v, ke.value, pe.value

@@ -7,14 +7,19 @@ full size is checked through what does not depend on size:
     reference's numerics and the FP64 oracle within the stated tolerances;
   * CSR and sliced layouts give the same bits, and a second step repeats them;
   * Newton's third law: the total force vanishes to FP32 rounding;
-  * the plain (atomic) path agrees with the partitioned path on the sample.
+  * the plain (atomic) path agrees with the partitioned path on the sample;
+  * the caller's random node order (reorder = 0, no curve order) gives the
+    same parity on the sample;
+  * the per-result error against FP64 (helpers.result_errors) is stated per
+    quantile.
 """
 import math
 
 import numpy as np
 import pytest
 
-from helpers import TOL_NORMWISE_F64, TOL_PERNODE_F64, TOL_VS_REFERENCE, scaled_error
+from helpers import (TOL_NORMWISE_F64, TOL_PERNODE_F64, TOL_RESULT_MAX, TOL_RESULT_P50,
+                     TOL_VS_REFERENCE, result_error_summary, scaled_error)
 
 pytestmark = pytest.mark.gpu
 
@@ -59,9 +64,10 @@ def full(built_lib, oracle_lib):
     pos64 = pos.astype(np.float64)
     p = O.lj_param(CUTOFF * CUTOFF, float(side), True)
     f64, sabs = O.lj_reduce_f64(pos64, incident, p)
+    sinf = O.lj_edge_scale_inf(pos64, incident, p)
     fref = O.lj_reduce_refnum(pos64, incident, p)
     yield dict(irr=irr, O=O, pos=pos, side=side, d_edges=d_edges, edges=edges, sample=sample,
-               f64=f64[sample], sabs=sabs[sample], fref=fref[sample])
+               f64=f64[sample], sabs=sabs[sample], sinf=sinf[sample], fref=fref[sample])
     d_edges.close()
 
 
@@ -83,6 +89,8 @@ def test_sample_parity_layouts_and_reproducibility(full):
     assert scaled_error(fs, fref, sabs) <= TOL_VS_REFERENCE
     assert np.abs(fs - f64).max() / np.abs(f64).max() <= TOL_NORMWISE_F64
     assert scaled_error(fs, f64, sabs) <= TOL_PERNODE_F64
+    err = result_error_summary(fs, f64, full["sinf"])
+    assert err["p50"] <= TOL_RESULT_P50 and err["max"] <= TOL_RESULT_MAX, err
     # a second step repeats the bits
     h_sl.step()
     assert np.array_equal(h_sl.get_result(elm_size=12).view(np.uint32), f_sl.view(np.uint32))
@@ -101,6 +109,27 @@ def test_sample_parity_layouts_and_reproducibility(full):
     total = np.abs(f64sum.sum(axis=0))
     assert np.all(np.isfinite(total))
     assert np.all(total <= 1e-6 * np.abs(f64sum).sum(axis=0))
+
+
+def test_caller_random_order(full):
+    """reorder = 0, the workload's other node order (it is measured in both):
+    blocks cut from the caller's random order, no curve order.  Each row sums
+    the same terms (in the order of the caller's column ids), so the sample
+    meets the same bounds, and a second step repeats the bits."""
+    irr, pos, side, d_edges = full["irr"], full["pos"], full["side"], full["d_edges"]
+    s, f64, sabs, fref = full["sample"], full["f64"], full["sabs"], full["fref"]
+    f, h = run(irr, pos, side, d_edges, exec=irr.IRR_EXEC_PARTITIONED, reorder=0)
+    perm, _, _ = h.partition(with_entries=False)
+    assert np.array_equal(perm, np.arange(N, dtype=np.int32))
+    fs = f[s]
+    assert scaled_error(fs, fref, sabs) <= TOL_VS_REFERENCE
+    assert np.abs(fs - f64).max() / np.abs(f64).max() <= TOL_NORMWISE_F64
+    assert scaled_error(fs, f64, sabs) <= TOL_PERNODE_F64
+    err = result_error_summary(fs, f64, full["sinf"])
+    assert err["p50"] <= TOL_RESULT_P50 and err["max"] <= TOL_RESULT_MAX, err
+    h.step()
+    assert np.array_equal(h.get_result(elm_size=12).view(np.uint32), f.view(np.uint32))
+    h.close()
 
 
 def test_plain_path_agrees(full):
