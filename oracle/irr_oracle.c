@@ -914,3 +914,166 @@ int orc_md_run(int64_t n, double *pos, double *vel, double side, double cutforce
 {
     return orc_md_run_mt(n, pos, vel, side, cutforce, skin, dt, steps, rebuild_every, ke, pe, 1, 0);
 }
+
+/* ------------------------------------------------------------------------ */
+/* Staged ("halo") layout (the library's own; see irr_oracle.h).             */
+/* ------------------------------------------------------------------------ */
+
+static int64_t staged_table(int64_t n, const int64_t *row_off, const int32_t *col, int64_t r0,
+                            int64_t r1, int32_t *buf)
+{
+    int64_t m = 0;
+    for (int64_t r = r0; r < r1 && r < n; r++) {
+        buf[m++] = (int32_t)r;
+        for (int64_t k = row_off[r]; k < row_off[r + 1]; k++) buf[m++] = col[k];
+    }
+    qsort(buf, (size_t)m, sizeof(int32_t), cmp_i32);
+    int64_t u = 0;
+    for (int64_t k = 0; k < m; k++)
+        if (u == 0 || buf[u - 1] != buf[k]) buf[u++] = buf[k];
+    return u;
+}
+
+static int64_t staged_slot(const int32_t *tab, int64_t ntab, int32_t id)
+{
+    int64_t lo = 0, hi = ntab;  /* first index with tab[idx] >= id */
+    while (lo < hi) {
+        int64_t mid = (lo + hi) / 2;
+        if (tab[mid] < id) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+int orc_staged_layout(int64_t n, const int64_t *row_off, const int32_t *col, int slices_per_item,
+                      int tab_max, int stream_max, int64_t *num_items, int64_t *num_words,
+                      int64_t *num_ids, int32_t *items, uint32_t *slice_off, uint32_t *words,
+                      int32_t *ids)
+{
+    if (n < 0 || slices_per_item < 1 || tab_max < 1 || stream_max < 64) return -2;
+    const int64_t S = (n + 7) / 8;
+    int64_t *soff = (int64_t *)malloc(sizeof(int64_t) * (size_t)(S + 1));
+    int64_t maxent = 0;
+    for (int64_t r = 0; r < n; r++)
+        if (row_off[r + 1] - row_off[r] > maxent) maxent = row_off[r + 1] - row_off[r];
+    int32_t *buf = (int32_t *)malloc(sizeof(int32_t) * (size_t)((int64_t)slices_per_item * 8 * (maxent + 1) + 8));
+    uint16_t *rs = (uint16_t *)malloc(sizeof(uint16_t) * (size_t)(maxent + 1));
+    if (!soff || !buf || !rs) {
+        free(soff);
+        free(buf);
+        free(rs);
+        return -2;
+    }
+    soff[0] = 0;
+    for (int64_t q = 0; q < S; q++) {
+        int64_t T = 0;
+        for (int64_t r = 8 * q; r < 8 * q + 8 && r < n; r++) {
+            int64_t t = (row_off[r + 1] - row_off[r] + 7) / 8;
+            if (t > T) T = t;
+        }
+        if (32 * (T + 1) > stream_max) {
+            free(soff);
+            free(buf);
+            free(rs);
+            return -1;
+        }
+        soff[q + 1] = soff[q] + 32 * (T + 1);
+    }
+    if (slice_off)
+        for (int64_t q = 0; q <= S; q++) slice_off[q] = (uint32_t)soff[q];
+    int64_t it = 0, tab0 = 0;
+    int64_t q0 = 0;
+    while (q0 < S) {
+        /* tentative run: at most slices_per_item slices and stream_max words */
+        int64_t q1 = q0 + 1;
+        while (q1 < S && q1 - q0 < slices_per_item && soff[q1 + 1] - soff[q0] <= stream_max) q1++;
+        /* cut into the longest prefixes whose tables fit */
+        int64_t a = q0;
+        while (a < q1) {
+            int64_t b = a + 1, ntab = staged_table(n, row_off, col, 8 * a, 8 * b, buf);
+            if (ntab > tab_max) {
+                free(soff);
+                free(buf);
+                free(rs);
+                return -1;
+            }
+            while (b < q1) {
+                int64_t t2 = staged_table(n, row_off, col, 8 * a, 8 * (b + 1), buf);
+                if (t2 > tab_max) break;
+                b++;
+                ntab = t2;
+            }
+            ntab = staged_table(n, row_off, col, 8 * a, 8 * b, buf);
+            if (items) {
+                int32_t *w = items + 6 * it;
+                w[0] = (int32_t)(8 * a);
+                w[1] = (int32_t)((8 * b < n ? 8 * b : n) - 8 * a);
+                w[2] = (int32_t)soff[a];
+                w[3] = (int32_t)(soff[b] - soff[a]);
+                w[4] = (int32_t)tab0;
+                w[5] = (int32_t)ntab;
+            }
+            if (ids) memcpy(ids + tab0, buf, sizeof(int32_t) * (size_t)ntab);
+            if (words) {
+                for (int64_t q = a; q < b; q++) {
+                    const int64_t T = (soff[q + 1] - soff[q]) / 32 - 1;
+                    uint32_t *sw = words + soff[q];
+                    for (int i = 0; i < 8; i++) {
+                        const int64_t r = 8 * q + i;
+                        int64_t len = 0, own = 0;
+                        int64_t cnt[8] = {0}, cur[8] = {0}, beg[8] = {0};
+                        if (r < n) {
+                            len = row_off[r + 1] - row_off[r];
+                            own = staged_slot(buf, ntab, (int32_t)r);
+                            /* the row's slots bucketed by bank group, ascending */
+                            for (int64_t k = 0; k < len; k++) cnt[staged_slot(buf, ntab, col[row_off[r] + k]) & 7]++;
+                            int64_t acc = 0;
+                            for (int g = 0; g < 8; g++) {
+                                beg[g] = acc;
+                                acc += cnt[g];
+                            }
+                            int64_t fill[8];
+                            for (int g = 0; g < 8; g++) fill[g] = beg[g];
+                            for (int64_t k = 0; k < len; k++) {
+                                const int64_t sl = staged_slot(buf, ntab, col[row_off[r] + k]);
+                                rs[fill[sl & 7]++] = (uint16_t)sl;
+                            }
+                        }
+                        for (int l = 0; l < 4; l++) sw[4 * i + l] = (uint32_t)(own * 16) | ((uint32_t)len << 16);
+                        const int p = i & 1;
+                        for (int64_t t = 0; t < T; t++) {
+                            uint32_t pk[2][4];
+                            for (int h = 0; h < 2; h++)
+                                for (int l = 0; l < 4; l++) {
+                                    int g = (int)((2 * t + h + 4 * p + l) & 7);
+                                    if (cur[g] >= cnt[g]) {
+                                        int best = -1;
+                                        for (int x = 0; x < 8; x++)
+                                            if (cnt[x] - cur[x] > 0 && (best < 0 || cnt[x] - cur[x] > cnt[best] - cur[best]))
+                                                best = x;
+                                        g = best;
+                                    }
+                                    int64_t slot = own;
+                                    if (g >= 0) slot = rs[beg[g] + cur[g]++];
+                                    pk[h][l] = (uint32_t)(slot * 16);
+                                }
+                            for (int l = 0; l < 4; l++)
+                                sw[32 * (t + 1) + 4 * i + l] = pk[0][l] | (pk[1][l] << 16);
+                        }
+                    }
+                }
+            }
+            it++;
+            tab0 += ntab;
+            a = b;
+        }
+        q0 = q1;
+    }
+    if (num_items) *num_items = it;
+    if (num_words) *num_words = soff[S];
+    if (num_ids) *num_ids = tab0;
+    free(soff);
+    free(buf);
+    free(rs);
+    return 0;
+}

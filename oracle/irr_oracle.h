@@ -140,6 +140,34 @@ int orc_partition_curve(int64_t n, const float *pos, const float lo[3], const fl
                         int curve, int64_t e, const int32_t *edges, int32_t *perm, int32_t *inv,
                         int64_t *row_off, int32_t *col);
 
+/* Staged ("halo") entry layout of a CSR (rows in execution order, columns
+ * ascending), for 4 lanes per row and slices of 8 rows -- the GPU builder's
+ * output, bit for bit.  No reference counterpart: it restates the library's
+ * own layout so that the GPU pass is checked as integer work.
+ *   Slices: slice q is rows [8q, 8q + 8) (clipped to n); T_q = the longest
+ *     row's entries / 8 rounded up; it takes 32 (T_q + 1) words.
+ *   Items: the slices are cut greedily into runs of at most slices_per_item
+ *     slices and stream_max words; each run is then cut greedily into the
+ *     longest prefixes whose table -- the sorted distinct ids of the item's
+ *     rows and of all their columns -- holds at most tab_max ids.
+ *   Words of a slice: word 4i + l (row i, lane l) of its first 32 is the
+ *     header own | len << 16 (own: the byte offset 16 * slot of the row's own
+ *     id in the item's table; a row past n has own 0 and len 0); word
+ *     32 (t + 1) + 4i + l is b0 | b1 << 16, the byte offsets of the row's picks
+ *     (t, 0, l) and (t, 1, l).  Row i (parity p = i & 1) picks in the order
+ *     (t, h, l): from bank group g = (2t + h + 4p + l) mod 8 (a slot's group is
+ *     slot mod 8) its lowest remaining entry; if that group is empty, from the
+ *     group with the most remaining entries (the lowest such group); when
+ *     none remain, its own slot (padding, masked by len in the kernel).
+ * Outputs may be NULL (sizes only).  items: 6 int32 per item (row0, nrows,
+ * word0, nwords, tab0, ntab).  Returns 0, or -1 when a slice alone exceeds
+ * stream_max words or tab_max ids (the layout does not apply), -2 on bad
+ * arguments. */
+int orc_staged_layout(int64_t n, const int64_t *row_off, const int32_t *col, int slices_per_item,
+                      int tab_max, int stream_max, int64_t *num_items, int64_t *num_words,
+                      int64_t *num_ids, int32_t *items, uint32_t *slice_off, uint32_t *words,
+                      int32_t *ids);
+
 #ifdef __cplusplus
 }
 #endif

@@ -93,6 +93,10 @@ def lib():
         L.orc_hilbert_keys.argtypes = [i64, P, P, P, P]
         L.orc_partition_curve.argtypes = [i64, P, P, P, C.c_int, i64, P, P, P, P, P]
         L.orc_partition_curve.restype = C.c_int
+        L.orc_staged_layout.argtypes = [i64, P, P, C.c_int, C.c_int, C.c_int,
+                                        C.POINTER(i64), C.POINTER(i64), C.POINTER(i64),
+                                        P, P, P, P]
+        L.orc_staged_layout.restype = C.c_int
         _lib = L
     return _lib
 
@@ -299,6 +303,35 @@ def partition(pos32, lo, scale, edges, curve: str = "morton"):
     if rc != 0:
         raise ValueError(f"orc_partition failed ({rc})")
     return perm, inv, row_off, col[: 2 * e]
+
+
+def staged_layout(row_off, col, slices_per_item: int = 8, tab_max: int = 640,
+                  stream_max: int = 3584):
+    """The staged ("halo") layout of a CSR (orc_staged_layout): a dict of items
+    (k, 6: row0, nrows, word0, nwords, tab0, ntab), slice_off, words and ids, or
+    None when a slice alone does not fit the limits."""
+    row_off = np.ascontiguousarray(row_off, np.int64)
+    col = np.ascontiguousarray(col, np.int32)
+    n = row_off.shape[0] - 1
+    ni, nw, nd = C.c_int64(), C.c_int64(), C.c_int64()
+    L = lib()
+    rc = L.orc_staged_layout(n, _p(row_off), _p(col), slices_per_item, tab_max, stream_max,
+                             C.byref(ni), C.byref(nw), C.byref(nd), None, None, None, None)
+    if rc == -1:
+        return None
+    if rc != 0:
+        raise ValueError(f"orc_staged_layout failed ({rc})")
+    items = np.zeros((max(ni.value, 1), 6), np.int32)
+    slice_off = np.zeros((n + 7) // 8 + 1, np.uint32)
+    words = np.zeros(max(nw.value, 1), np.uint32)
+    ids = np.zeros(max(nd.value, 1), np.int32)
+    rc = L.orc_staged_layout(n, _p(row_off), _p(col), slices_per_item, tab_max, stream_max,
+                             C.byref(ni), C.byref(nw), C.byref(nd), _p(items), _p(slice_off),
+                             _p(words), _p(ids))
+    if rc != 0:
+        raise ValueError(f"orc_staged_layout failed ({rc})")
+    return {"items": items[: ni.value], "slice_off": slice_off, "words": words[: nw.value],
+            "ids": ids[: nd.value]}
 
 
 def morton_frame(pos32):
