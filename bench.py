@@ -57,6 +57,7 @@ import numpy as np  # noqa: E402
 
 N_NODES = 4194304
 FORCE_SAMPLE = 2000   # nodes whose results the FP64 checker recomputes
+LAYOUTS = {"auto": 0, "csr": 1, "sliced": 2, "staged": 3}  # enum irr_layout
 CUTOFF = 2.5
 DENSITY = 64.0 / (4.0 / 3.0 * math.pi * CUTOFF ** 3)
 SEED = 20260002
@@ -361,7 +362,7 @@ def run_ours(args, rank, world, local):
         h.init()
         return h
 
-    h = handle(exec=irr.IRR_EXEC_PARTITIONED)
+    h = handle(exec=irr.IRR_EXEC_PARTITIONED, layout=LAYOUTS[args.layout])
     for _ in range(args.warmup):
         h.step()
     h.sync()
@@ -382,7 +383,7 @@ def run_ours(args, rank, world, local):
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "unit": "edges/s",
                               "legs": "value only", "nodes": n, "edges": E,
-                              "ms_per_step": ms / args.steps}), flush=True)
+                              "layout": args.layout, "ms_per_step": ms / args.steps}), flush=True)
         return 0
 
     # force error of the timed configuration on a seeded node sample (FP64 checker)
@@ -724,6 +725,8 @@ def main():
     ap.add_argument("--md-steps", type=int, default=1000)
     ap.add_argument("--jobs", type=int, default=200)
     ap.add_argument("--batch-steps", type=int, default=200)
+    ap.add_argument("--layout", choices=sorted(LAYOUTS), default="auto",
+                    help="entry layout of the timed partitioned handle (irr_config.layout)")
     ap.add_argument("--capacity", type=int, default=1,
                     help="1: the served leg also sweeps the arrival rate for its capacity")
     args = ap.parse_args()

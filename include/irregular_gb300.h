@@ -101,7 +101,17 @@ enum irr_layout {
      * slice's entries interleaved so that one warp's lanes read one
      * contiguous, bank-conflict-free 256-byte line per step.  Same sums, in
      * the same order, as CSR. */
-    IRR_LAYOUT_SLICED = 2
+    IRR_LAYOUT_SLICED = 2,
+    /* Staged ("halo"): work items of up to 64 consecutive rows, each with a
+     * table of the node ids its rows touch; the kernel gathers the table's
+     * positions into shared memory once per item and reads every entry's
+     * neighbour from there, by a 16-bit table offset.  Each row's entries are
+     * summed in an order chosen to spread shared-memory banks (not the CSR
+     * order), so results differ from CSR / sliced in the last bits; 4 lanes
+     * per row.  Applies when every 8 consecutive rows touch at most 640
+     * distinct nodes and no row exceeds ~440 entries; else IRR_ERR_CAPACITY
+     * (AUTO falls back). */
+    IRR_LAYOUT_STAGED = 3
 };
 
 /* Node-data formats: the node_data_elm_size the reference passes. */
@@ -239,6 +249,15 @@ IRR_API int irr_get_info(const irr_handle *h, irr_info *info);
  * entries within a row in edge-list order, idx0 side first).  Any pointer may
  * be NULL. */
 IRR_API int irr_get_partition(irr_handle *h, int32_t *perm, int64_t *row_off, int32_t *col);
+
+/* The staged layout of a handle that uses it (IRR_ERR_STATE otherwise),
+ * copied to host so that it can be checked as integer work: counts[3] =
+ * {items, words, table ids}; items: 6 int32 per item (first row, rows, first
+ * word, words, first table id, table ids); slice_off: one uint32 per slice of
+ * 8 rows, plus one; words; ids.  Any array may be NULL (counts alone size
+ * them).  No reference counterpart. */
+IRR_API int irr_get_staged(irr_handle *h, int64_t *counts, int32_t *items, uint32_t *slice_off,
+                           uint32_t *words, int32_t *ids);
 
 /* ---------------------------------------------------------- file formats
  * The drivers' input files (host code; no GPU needed).

@@ -16,6 +16,10 @@ using namespace irr;
 
 namespace {
 
+// IRR_LAYOUT_AUTO takes the staged layout where it applies (4 lanes per row,
+// shared-memory stages, every 8 rows within the table limit).
+constexpr bool kAutoStaged = false;
+
 int fail(irr_handle* h, int code, const char* fmt, ...)
 {
     if (h) {
@@ -58,6 +62,8 @@ void free_layout(irr_handle* h)
     dfree(h->part.row_off);
     dfree(h->part.col);
     free_sliced(&h->sl);
+    free_staged(&h->st);
+    h->shape.staged = 0;
     h->host_row_off.clear();
     dfree(h->d_inst);
     dfree(h->d_items);
@@ -128,8 +134,10 @@ int upload_inst(irr_handle* h)
     d.row_off = h->part.row_off;
     d.col = h->part.col;
     d.force = h->d_force;
-    d.slice_off = h->sl.lanes ? h->sl.slice_off : nullptr;
+    d.slice_off = h->shape.staged ? h->st.slice_off : (h->sl.lanes ? h->sl.slice_off : nullptr);
     d.scol = h->sl.lanes ? h->sl.col : nullptr;
+    d.words = h->shape.staged ? h->st.words : nullptr;
+    d.tab = h->shape.staged ? h->st.ids : nullptr;
     d.law = h->law;
     d.n = h->n;
     h->inst = d;
@@ -142,7 +150,10 @@ int upload_inst(irr_handle* h)
 int upload_items(irr_handle* h)
 {
     std::vector<WorkItem> items;
-    make_instance_items(h->host_row_off.data(), h->sl, h->n, 0, h->shape, items);
+    if (h->shape.staged)
+        items = h->st.items;
+    else
+        make_instance_items(h->host_row_off.data(), h->sl, h->n, 0, h->shape, items);
     dfree(h->d_items);
     h->num_items = 0;
     H_CUDA(h, cudaMalloc(&h->d_items, sizeof(WorkItem) * (items.size() ? items.size() : 1)), "allocate work items");
@@ -255,19 +266,47 @@ int irr_ensure_layout(irr_handle* h, int lanes_per_row, int block_nodes)
     h->shape.lanes_per_row = lanes_per_row;
     h->shape.block_nodes = block_nodes;
     const int want = h->cfg.layout;
-    if (want == IRR_LAYOUT_CSR) {
+    bool staged = false;
+    if (want == IRR_LAYOUT_STAGED || (want == IRR_LAYOUT_AUTO && kAutoStaged)) {
+        if (lanes_per_row == 4 && h->shape.stage_smem) {
+            if (!h->st.words) {
+                const cudaError_t se = build_staged(h->part.row_off, h->part.col, h->host_row_off.data(),
+                                                    n, &h->st, h->stream);
+                if (se != cudaSuccess) {
+                    cudaGetLastError();
+                    free_staged(&h->st);
+                    if (want == IRR_LAYOUT_STAGED)
+                        return se == cudaErrorNotSupported
+                                   ? fail(h, IRR_ERR_CAPACITY,
+                                          "staged layout: 8 rows touch more than %d nodes, or a row is too long",
+                                          kHaloTabMax)
+                                   : cuda_fail(h, se, "build staged layout");
+                }
+            }
+            staged = h->st.words != nullptr || (n == 0 && want == IRR_LAYOUT_STAGED);
+        } else if (want == IRR_LAYOUT_STAGED) {
+            return fail(h, IRR_ERR_ARG, "the staged layout needs 4 lanes per row and stage_smem");
+        }
+    }
+    h->shape.staged = staged ? 1 : 0;
+    if (staged) {
         free_sliced(&h->sl);
-    } else if (h->sl.lanes != lanes_per_row) {
-        const cudaError_t se = build_sliced(h->part.row_off, h->part.col, n, lanes_per_row, &h->sl, h->stream);
-        if (se != cudaSuccess) {
-            cudaGetLastError();
+    } else {
+        free_staged(&h->st);
+        if (want == IRR_LAYOUT_CSR) {
             free_sliced(&h->sl);
-            if (want == IRR_LAYOUT_SLICED)
-                return se == cudaErrorInvalidValue
-                           ? fail(h, IRR_ERR_CAPACITY, "sliced layout above 2^32 words")
-                           : cuda_fail(h, se, "build sliced layout");
-        } else if (want == IRR_LAYOUT_AUTO && !sliced_pays(h->sl, 2 * e)) {
-            free_sliced(&h->sl);
+        } else if (h->sl.lanes != lanes_per_row) {
+            const cudaError_t se = build_sliced(h->part.row_off, h->part.col, n, lanes_per_row, &h->sl, h->stream);
+            if (se != cudaSuccess) {
+                cudaGetLastError();
+                free_sliced(&h->sl);
+                if (want == IRR_LAYOUT_SLICED)
+                    return se == cudaErrorInvalidValue
+                               ? fail(h, IRR_ERR_CAPACITY, "sliced layout above 2^32 words")
+                               : cuda_fail(h, se, "build sliced layout");
+            } else if (want != IRR_LAYOUT_SLICED && !sliced_pays(h->sl, 2 * e)) {
+                free_sliced(&h->sl);
+            }
         }
     }
     int rc = upload_inst(h);
@@ -276,7 +315,8 @@ int irr_ensure_layout(irr_handle* h, int lanes_per_row, int block_nodes)
     if (rc) return rc;
     h->dev_bytes = 2 * (int64_t)(n > 0 ? n : 1) * (int64_t)sizeof(float4) + (int64_t)h->raw_cap +
                    (int64_t)(2 * n + n + 1) * 4 + 2 * e * 4 +
-                   (h->sl.lanes ? 4 * (h->sl.words + h->sl.slices + 1) : 0);
+                   (h->sl.lanes ? 4 * (h->sl.words + h->sl.slices + 1) : 0) +
+                   (h->shape.staged ? 4 * (h->st.nwords + h->st.nids + h->st.slices + 1) : 0);
     return IRR_OK;
 }
 
@@ -326,7 +366,7 @@ int irr_create(const irr_config* cfg, irr_handle** out)
     if (c.map_idx < IRR_MAP_LJ_MOLDYN || c.map_idx > IRR_MAP_LJ_MINIMD_PBC) return IRR_ERR_ARG;
     if (c.block_nodes != 0 && (c.block_nodes < 64 || c.block_nodes > 4096 || (c.block_nodes & (c.block_nodes - 1))))
         return IRR_ERR_ARG;
-    if (c.layout < IRR_LAYOUT_AUTO || c.layout > IRR_LAYOUT_SLICED) return IRR_ERR_ARG;
+    if (c.layout < IRR_LAYOUT_AUTO || c.layout > IRR_LAYOUT_STAGED) return IRR_ERR_ARG;
     if (c.order != IRR_ORDER_HILBERT && c.order != IRR_ORDER_MORTON) return IRR_ERR_ARG;
     if (c.wait_limit_us < 0) return IRR_ERR_ARG;
     if (c.lanes_per_row != 0 && c.lanes_per_row != 1 && c.lanes_per_row != 2 && c.lanes_per_row != 4 &&
@@ -615,9 +655,10 @@ int irr_get_info(const irr_handle* h, irr_info* info)
     info->lanes_per_row = h->shape.lanes_per_row;
     info->stage_smem = h->shape.stage_smem;
     info->exec = h->cfg.exec;
-    info->layout = h->sl.lanes ? IRR_LAYOUT_SLICED : IRR_LAYOUT_CSR;
+    info->layout = h->shape.staged ? IRR_LAYOUT_STAGED : (h->sl.lanes ? IRR_LAYOUT_SLICED : IRR_LAYOUT_CSR);
     info->order = h->cfg.order;
-    info->num_slots = h->sl.lanes ? h->sl.words : info->num_entries;
+    info->num_slots = h->shape.staged ? 2 * (h->st.nwords - 32 * h->st.slices)
+                                      : (h->sl.lanes ? h->sl.words : info->num_entries);
     return IRR_OK;
 }
 
@@ -640,6 +681,35 @@ int irr_get_partition(irr_handle* h, int32_t* perm, int64_t* row_off, int32_t* c
     H_CUDA(h, cudaStreamSynchronize(h->stream), "copy partition");
     if (row_off)
         for (int64_t i = 0; i <= n; i++) row_off[i] = ro[(size_t)i];
+    return IRR_OK;
+}
+
+int irr_get_staged(irr_handle* h, int64_t* counts, int32_t* items, uint32_t* slice_off,
+                   uint32_t* words, int32_t* ids)
+{
+    if (!h) return IRR_ERR_ARG;
+    if (!h->inited || !h->shape.staged) return fail(h, IRR_ERR_STATE, "the handle does not use the staged layout");
+    DeviceGuard dev_guard(h->device);
+    const Staged& st = h->st;
+    if (counts) {
+        counts[0] = (int64_t)st.items.size();
+        counts[1] = st.nwords;
+        counts[2] = st.nids;
+    }
+    if (items)
+        for (size_t k = 0; k < st.items.size(); k++) {
+            const WorkItem& w = st.items[k];
+            const int32_t v[6] = {w.row0, w.nrows, (int32_t)w.ent0, (int32_t)w.nent, (int32_t)w.tab0,
+                                  (int32_t)w.ntab};
+            memcpy(items + 6 * k, v, sizeof(v));
+        }
+    if (slice_off && !st.host_off.empty())
+        memcpy(slice_off, st.host_off.data(), sizeof(uint32_t) * st.host_off.size());
+    if (words && st.nwords > 0)
+        H_CUDA(h, cudaMemcpyAsync(words, st.words, sizeof(uint32_t) * st.nwords, cudaMemcpyDeviceToHost, h->stream), "copy words");
+    if (ids && st.nids > 0)
+        H_CUDA(h, cudaMemcpyAsync(ids, st.ids, sizeof(int32_t) * st.nids, cudaMemcpyDeviceToHost, h->stream), "copy tables");
+    H_CUDA(h, cudaStreamSynchronize(h->stream), "copy staged layout");
     return IRR_OK;
 }
 

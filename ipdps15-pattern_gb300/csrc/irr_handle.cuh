@@ -42,6 +42,7 @@ struct irr_handle {
     PartitionOut part{};
     std::vector<uint32_t> host_row_off;  // host copy of part.row_off (cuts work items)
     irr::Sliced sl{};                    // sliced layout, when in use
+    irr::Staged st{};                    // staged layout, when in use
     InstDesc* d_inst = nullptr;
     InstDesc inst{};             // host copy of *d_inst (the single-instance launch parameter)
     WorkItem* d_items = nullptr;

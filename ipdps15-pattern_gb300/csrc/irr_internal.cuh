@@ -51,8 +51,10 @@ struct InstDesc {
     const uint32_t* row_off;  // n + 1 entry offsets
     const int32_t* col;       // neighbour of each directed entry (instance-local id)
     float4* force;            // per-node result, execution order
-    const uint32_t* slice_off;  // sliced layout: word offset of each slice (or null)
+    const uint32_t* slice_off;  // sliced or staged layout: word offset of each slice (or null)
     const int32_t* scol;        // sliced layout: interleaved, padded entries
+    const uint32_t* words;      // staged layout: headers and 16-bit table offsets
+    const int32_t* tab;         // staged layout: the items' tables (node ids), concatenated
     LawParams law;
     int64_t n;
 };
@@ -60,7 +62,8 @@ struct InstDesc {
 // One node block: rows [row0, row0 + nrows) of instance `inst`, whose
 // directed entries are [ent0, ent0 + nent) of the instance's col array (or,
 // with kItemSliced, words [ent0, ent0 + nent) of its sliced array: whole
-// slices, so row0 is a multiple of the slice height).
+// slices, so row0 is a multiple of the slice height; with kItemStaged, words
+// of its staged array, and its table is ids [tab0, tab0 + ntab) of tab).
 struct WorkItem {
     int32_t inst;
     int32_t row0;
@@ -68,9 +71,11 @@ struct WorkItem {
     int32_t flags;       // kItemDirect: read entries from global memory
     uint32_t ent0;
     uint32_t nent;
+    uint32_t tab0;
+    uint32_t ntab;
 };
 
-enum : int { kItemDirect = 1, kItemSliced = 2 };
+enum : int { kItemDirect = 1, kItemSliced = 2, kItemStaged = 4 };
 
 // Sliced entry layout of one instance, for G lanes per row.  A slice is
 // R = 32 / G consecutive rows; each row is padded to the slice's longest row
@@ -94,7 +99,35 @@ struct TiledShape {
     int stage_smem;      // 1: entry segments bulk-copied into a shared-memory ring
     int block_nodes;     // max rows per work item
     int periodic;
+    int staged = 0;      // 1: staged layout (the halo kernel; 4 lanes per row)
 };
+
+// Staged ("halo") layout of one instance, for 4 lanes per row and slices of 8
+// rows (irr_staged.cu): per work item a table of node ids whose positions the
+// kernel gathers into shared memory, and per slice 32 header words and 32
+// words per step of 16-bit byte offsets into that table.
+constexpr int kHaloSlicesPerItem = 8;   // 64 rows per item at most
+constexpr int kHaloTabMax = 640;        // table ids per item (10 KB of positions)
+constexpr int kHaloStreamMax = 3584;    // words per item (14 KB)
+constexpr int kHaloStages = 2;          // shared-memory ring depth
+struct Staged {
+    uint32_t* slice_off = nullptr;   // [slices + 1] word offsets (multiples of 32)
+    uint32_t* words = nullptr;       // [nwords]
+    int32_t* ids = nullptr;          // [nids] the items' tables, concatenated
+    int64_t slices = 0;
+    int64_t nwords = 0;
+    int64_t nids = 0;
+    std::vector<uint32_t> host_off;  // host copy of slice_off
+    std::vector<WorkItem> items;     // the items (instance 0), flags kItemStaged
+};
+// Builds st from a CSR (rows in execution order, columns ascending) on the
+// device; host_row_off is the host copy of row_off.  Synchronises s.
+// cudaErrorNotSupported (nothing allocated) when a slice alone exceeds the
+// limits above -- a row of more than ~440 entries, or 8 rows touching more
+// than kHaloTabMax distinct nodes.
+cudaError_t build_staged(const uint32_t* row_off, const int32_t* col, const uint32_t* host_row_off,
+                         int64_t n, Staged* st, cudaStream_t s);
+void free_staged(Staged* st, cudaStream_t s = nullptr);
 
 // Shape of the owner-computes kernel; each can be set at build time
 // (-DIRR_STAGES=... etc.) to build and time variants.

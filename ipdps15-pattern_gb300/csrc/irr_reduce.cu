@@ -582,6 +582,213 @@ __global__ void __launch_bounds__(kPipeThreads, kCtasPerSm) tiled_kernel(
     }
 }
 
+// ---- staged ("halo") layout: positions staged in shared memory ----
+//
+// halo_kernel: the same persistent, warp-specialised owner-computes reduction
+// over the staged layout (irr_staged.cu).  Per work item the producer warp
+// bulk-copies the item's words (headers and 16-bit table offsets) into the
+// stage, and its 32 lanes gather the item's table -- the positions of every
+// node its rows touch, ~465 for 64 rows -- with 16-byte cp.async copies into
+// the stage's table; the stage's `full` barrier completes when the bulk copy's
+// bytes and all 32 lanes' copies have landed (1 + 32 arrivals).  The
+// consumers read each entry's position from shared memory (a 128-bit load at
+// a table offset), so the law's operands arrive in tens of cycles instead of
+// an L1 miss's hundreds, and the entry order of the layout spreads each
+// quarter-warp's 8 loads over the 8 bank groups.  G = 4 lanes per row.
+constexpr int kHaloStageWords = kHaloStreamMax + 4 * kHaloTabMax;  // 32-bit words per stage
+
+__device__ __forceinline__ void cp_async16(uint32_t dst_smem, const void* src)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst_smem), "l"(src) : "memory");
+}
+
+// One arrival on `bar` once every cp.async this thread issued before has
+// landed (noinc: the barrier's expected count includes it).
+__device__ __forceinline__ void cp_async_arrive(uint64_t* bar)
+{
+    asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// Shared loads kept after the stage's barrier wait (volatile, like load_pair).
+__device__ __forceinline__ uint32_t lds32(uint32_t addr)
+{
+    uint32_t v;
+    asm volatile("ld.shared.u32 %0, [%1];" : "=r"(v) : "r"(addr));
+    return v;
+}
+
+__device__ __forceinline__ float4 lds128(uint32_t addr)
+{
+    float4 v;
+    asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+                 : "r"(addr));
+    return v;
+}
+
+// The slices of a staged work item that belong to consumer warp `cw`; `sw`
+// is the stage (words, then the table at word kHaloStreamMax).
+template <bool PERIODIC>
+__device__ __forceinline__ void consume_halo(const WorkItem& w, const InstHot& I, const uint32_t* sw,
+                                             int cw, int lane32)
+{
+    const int lane = lane32 & 3;
+    const uint32_t* __restrict__ slice_off = I.slice_off;
+    float4* __restrict__ force = I.force;
+    const LawParams* __restrict__ cold = I.cold;
+    const int64_t n = I.n;
+    const HotLaw H = I.H;
+    const uint32_t words_u32 = smem_u32(sw);
+    const uint32_t tab_u32 = smem_u32(sw + kHaloStreamMax);
+    const int s0 = w.row0 / 8;
+    const int ns = (w.nrows + 7) / 8;
+    for (int q = cw; q < ns; q += kConsumerWarps) {
+        const uint32_t o0 = __ldg(slice_off + s0 + q);
+        const uint32_t steps = ((__ldg(slice_off + s0 + q + 1) - o0) >> 5) - 1;
+        uint32_t addr = words_u32 + 4u * (o0 - w.ent0 + (uint32_t)lane32);
+        const uint32_t hdr = lds32(addr);
+        const float4 a = lds128(tab_u32 + (hdr & 0xffffu));
+        const uint32_t len = hdr >> 16;
+        const int64_t r = (int64_t)(s0 + q) * 8 + lane32 / 4;
+        float2 ax = make_float2(0.f, 0.f), ay = ax, az = ax;
+        for (uint32_t t = 0; t < steps; t++) {
+            addr += 128u;
+            const uint32_t wd = lds32(addr);
+            const float4 b0 = lds128(tab_u32 + (wd & 0xffffu));
+            const float4 b1 = lds128(tab_u32 + (wd >> 16));
+            const uint32_t k0 = 8 * t + lane;
+            lj_pair<PERIODIC>(a, b0, b1, k0 < len, k0 + 4 < len, H, cold, ax, ay, az);
+        }
+        const float3 f = join_partials<4>(ax, ay, az);
+        if (r < n && lane == 0) force[r] = make_float4(f.x, f.y, f.z, 0.f);
+    }
+}
+
+template <bool PERIODIC, class Src>
+__global__ void __launch_bounds__(kPipeThreads, kCtasPerSm) halo_kernel(
+    const InstDesc* __restrict__ insts, const WorkItem* __restrict__ items, int num_items,
+    int* queue, int* status, uint64_t wait_ns, int withhold, const __grid_constant__ Src src)
+{
+    constexpr bool ONE = std::is_same<Src, SrcOne>::value;
+    constexpr bool TABLE = std::is_same<Src, SrcTable>::value;
+    extern __shared__ int4 smem_raw[];
+    uint32_t* stage_base = reinterpret_cast<uint32_t*>(smem_raw);
+    __shared__ uint64_t full[kHaloStages];
+    __shared__ uint64_t empty[kHaloStages];
+    __shared__ int s_item[kHaloStages];
+    const int warp = threadIdx.x / 32;
+    const int lane = threadIdx.x % 32;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kHaloStages; s++) {
+            mbar_init(&full[s], 33);  // the bulk copy's arrive + one per producer lane
+            mbar_init(&empty[s], kConsumerWarps);
+        }
+    }
+    __syncthreads();
+
+    if (warp == kConsumerWarps) {
+        if (withhold) return;
+        for (int k = 0;; k++) {
+            const int s = k % kHaloStages;
+            const int use = k / kHaloStages;
+            int it = 0;
+            if (lane == 0) {
+                if (use > 0 && !mbar_wait_bounded(&empty[s], (uint32_t)(use - 1) & 1u, wait_ns)) {
+                    atomicOr(status, kStatusWaitTimeout);
+                    it = -1;
+                } else {
+                    const int got = atomicAdd(queue, 1);
+                    it = got < num_items ? got : num_items;
+                    s_item[s] = it;
+                }
+            }
+            it = __shfl_sync(0xffffffffu, it, 0);
+            if (it < 0) {  // a wait gave up: leave with none of this lane's copies in flight
+                asm volatile("cp.async.wait_all;" ::: "memory");
+                return;
+            }
+            if (it >= num_items) {  // no more work: complete the stage's phase for the consumers
+                if (lane == 0) mbar_arrive(&full[s]);
+                mbar_arrive(&full[s]);
+                asm volatile("cp.async.wait_all;" ::: "memory");
+                return;
+            }
+            const WorkItem w = items[it];
+            const InstDesc* I;
+            if constexpr (ONE) I = &src.d;
+            else I = insts + w.inst;
+            uint32_t* sw = stage_base + s * kHaloStageWords;
+            if (lane == 0) bulk_load(sw, I->words + w.ent0, w.nent * 4u, &full[s]);
+            const uint32_t tab_u32 = smem_u32(sw + kHaloStreamMax);
+            const int32_t* __restrict__ ids = I->tab + w.tab0;
+            const float4* __restrict__ pos = I->pos;
+            for (uint32_t j = lane; j < w.ntab; j += 32) cp_async16(tab_u32 + 16u * j, pos + __ldg(ids + j));
+            cp_async_arrive(&full[s]);
+        }
+    }
+
+    int cur = -1;
+    InstHot hot{};
+    for (int k = 0;; k++) {
+        const int s = k % kHaloStages;
+        if (!mbar_wait_bounded(&full[s], (uint32_t)(k / kHaloStages) & 1u, wait_ns)) {
+            if (lane == 0) atomicOr(status, kStatusWaitTimeout);
+            mbar_wait_bounded(&full[s], (uint32_t)(k / kHaloStages) & 1u, wait_ns);
+            return;
+        }
+        const int it = s_item[s];
+        if (it >= num_items) return;
+        const WorkItem w = items[it];
+        if constexpr (ONE) {
+            hot = load_hot(&src.d);
+        } else if constexpr (TABLE) {
+            hot = hot_from(src, insts, w.inst);
+        } else if (w.inst != cur) {
+            hot = load_hot(insts + w.inst);
+            cur = w.inst;
+        }
+        consume_halo<PERIODIC>(w, hot, stage_base + s * kHaloStageWords, warp, lane);
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[s]);
+    }
+}
+
+template <bool PERIODIC, class Src>
+cudaError_t launch_halo_src(const InstDesc* d_insts, const WorkItem* d_items, int num_items,
+                            int* d_queue, int grid, int* d_status, cudaStream_t s, const Src& src,
+                            const WaitPolicy& wp)
+{
+    auto kern = halo_kernel<PERIODIC, Src>;
+    const size_t smem = (size_t)kHaloStages * kHaloStageWords * sizeof(uint32_t);
+    IRR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (grid <= 0 || num_items <= 0) return cudaSuccess;
+    kern<<<grid, kPipeThreads, smem, s>>>(d_insts, d_items, num_items, d_queue, d_status,
+                                          wp.wait_ns, wp.withhold, src);
+    return cudaGetLastError();
+}
+
+template <bool PERIODIC>
+cudaError_t launch_halo_p(const InstDesc* d_insts, const WorkItem* d_items, int num_items,
+                          int* d_queue, int grid, int* d_status, cudaStream_t s,
+                          const InstDesc* host_insts, int num_insts, const WaitPolicy& wp)
+{
+    if (host_insts && num_insts == 1)
+        return launch_halo_src<PERIODIC>(d_insts, d_items, num_items, d_queue, grid, d_status, s,
+                                         SrcOne{host_insts[0]}, wp);
+    if (host_insts && num_insts > 1 && num_insts <= kTableInsts) {
+        static thread_local SrcTable t;
+        for (int k = 0; k < num_insts; k++) {
+            const InstDesc& d = host_insts[k];
+            t.h[k] = HotEntry{d.pos, HotLaw{d.law.half2, d.law.rc2, d.law.band}, 0.f};
+        }
+        return launch_halo_src<PERIODIC>(d_insts, d_items, num_items, d_queue, grid, d_status, s, t,
+                                         wp);
+    }
+    return launch_halo_src<PERIODIC>(d_insts, d_items, num_items, d_queue, grid, d_status, s,
+                                     SrcGlobal{0}, wp);
+}
+
 template <bool PERIODIC, int G, class Src>
 cudaError_t launch_tiled_src(const TiledShape& shape, const InstDesc* d_insts,
                              const WorkItem* d_items, int num_items, int* d_queue, int grid,
@@ -661,6 +868,13 @@ cudaError_t launch_tiled(const TiledShape& shape, const InstDesc* d_insts,
                          const WaitPolicy& wp)
 {
     if (!d_queue) return cudaErrorInvalidValue;
+    if (shape.staged) {
+        if (shape.lanes_per_row != 4) return cudaErrorInvalidValue;
+        return shape.periodic ? launch_halo_p<true>(d_insts, d_items, num_items, d_queue, grid,
+                                                    d_status, s, host_insts, num_insts, wp)
+                              : launch_halo_p<false>(d_insts, d_items, num_items, d_queue, grid,
+                                                     d_status, s, host_insts, num_insts, wp);
+    }
     return shape.periodic ? launch_tiled_p<true>(shape, d_insts, d_items, num_items, d_queue, grid,
                                                  d_status, s, host_insts, num_insts, wp)
                           : launch_tiled_p<false>(shape, d_insts, d_items, num_items, d_queue,

@@ -41,6 +41,7 @@ IRR_ORDER_MORTON = 1
 IRR_LAYOUT_AUTO = 0
 IRR_LAYOUT_CSR = 1
 IRR_LAYOUT_SLICED = 2
+IRR_LAYOUT_STAGED = 3
 
 
 class IrregularError(RuntimeError):
@@ -138,6 +139,7 @@ _SIGS = {
     "irr_set_wait_limit": (C.c_int, [P, I64, C.c_int]),
     "irr_get_info": (C.c_int, [P, C.POINTER(Info)]),
     "irr_get_partition": (C.c_int, [P, P, P, P]),
+    "irr_get_staged": (C.c_int, [P, P, P, P, P, P]),
     "irr_neighbor_build": (C.c_int, [C.c_int, P, P, C.c_int, C.c_int, I64, C.c_float, C.c_float,
                                      C.POINTER(P), C.POINTER(I64)]),
     "irr_device_free": (C.c_int, [C.c_int, P]),
@@ -412,6 +414,10 @@ class Handle:
     def autotune(self):
         self._check(load().irr_autotune(self._h), "irr_autotune")
 
+    def staged(self) -> dict:
+        """The staged layout (irr_get_staged): items (k, 6), slice_off, words, ids."""
+        return _staged_of(self)
+
     def partition(self, with_entries: bool = True):
         """(perm, row_off, col) of a partitioned handle; col is None when
         with_entries is False (the entries are not copied)."""
@@ -424,6 +430,21 @@ class Handle:
                                              _ptr(col) if with_entries else None),
                     "irr_get_partition")
         return perm, row_off, (col[:m] if with_entries else None)
+
+
+def _staged_of(handle) -> dict:
+    L = load()
+    counts = np.zeros(3, np.int64)
+    handle._check(L.irr_get_staged(handle._h, _ptr(counts), None, None, None, None), "irr_get_staged")
+    ni, nw, nd = (int(x) for x in counts)
+    n = handle.info().num_nodes
+    items = np.zeros((max(ni, 1), 6), np.int32)
+    slice_off = np.zeros((n + 7) // 8 + 1, np.uint32)
+    words = np.zeros(max(nw, 1), np.uint32)
+    ids = np.zeros(max(nd, 1), np.int32)
+    handle._check(L.irr_get_staged(handle._h, _ptr(counts), _ptr(items), _ptr(slice_off),
+                                   _ptr(words), _ptr(ids)), "irr_get_staged")
+    return {"items": items[:ni], "slice_off": slice_off, "words": words[:nw], "ids": ids[:nd]}
 
 
 def read_graph(path: str, one_based: bool = False) -> np.ndarray:
