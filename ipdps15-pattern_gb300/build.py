@@ -21,6 +21,9 @@ ROOT = os.path.dirname(HERE)
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                      "-Xcompiler", "-fvisibility=hidden", "-I", os.path.join(ROOT, "include")]
+# Extra nvcc flags, e.g. "-DIRR_STAGES=3" to build a variant of the kernels'
+# compile-time shape (see csrc/irr_internal.cuh).
+NVCC_FLAGS += os.environ.get("IRR_NVCC_EXTRA", "").split()
 
 
 def nvcc() -> str:

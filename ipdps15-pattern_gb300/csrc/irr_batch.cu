@@ -84,8 +84,10 @@ int upload_insts(irr_batch* b)
         d.row_off = h->part.row_off;
         d.col = h->part.col;
         d.force = h->d_force;
-        d.slice_off = h->sl.lanes ? h->sl.slice_off : nullptr;
+        d.slice_off = h->shape.staged ? h->st.slice_off : (h->sl.lanes ? h->sl.slice_off : nullptr);
         d.scol = h->sl.lanes ? h->sl.col : nullptr;
+        d.words = h->shape.staged ? h->st.words : nullptr;
+        d.tab = h->shape.staged ? h->st.ids : nullptr;
         d.law = h->law;
         d.n = h->n;
         insts.push_back(d);
@@ -98,14 +100,17 @@ int upload_insts(irr_batch* b)
     return IRR_OK;
 }
 
-// Every instance's layout for G lanes per row (each handle rebuilds its own
-// descriptor and items with it), then the batch's instance table.
-int set_lanes(irr_batch* b, int lanes)
+// Every instance's layout for G lanes per row, staged or not (each handle
+// rebuilds its own descriptor and items with it), then the batch's instance
+// table.  IRR_ERR_CAPACITY (no failure recorded) when the staged layout was
+// asked for and some instance's graph does not fit it.
+int set_lanes(irr_batch* b, int lanes, int staged)
 {
     for (irr_handle* h : b->handles) {
-        if (h->shape.lanes_per_row == lanes) continue;  // already laid out for G
-        const int rc = irr_ensure_layout(h, lanes, h->shape.block_nodes);
+        if (h->shape.lanes_per_row == lanes && h->shape.staged == staged) continue;  // already laid out
+        const int rc = irr_ensure_layout(h, lanes, h->shape.block_nodes, staged);
         if (rc) return bfail(b, rc, std::string("instance layout: ") + irr_last_error(h));
+        if (h->shape.staged != staged) return IRR_ERR_CAPACITY;
     }
     return upload_insts(b);
 }
@@ -116,7 +121,14 @@ int upload_items(irr_batch* b, const TiledShape& shape)
     std::vector<WorkItem> items;
     for (size_t k = 0; k < b->handles.size(); k++) {
         const irr_handle* h = b->handles[k];
-        make_instance_items(h->host_row_off.data(), h->sl, h->n, (int)k, shape, items);
+        if (shape.staged) {
+            for (WorkItem w : h->st.items) {
+                w.inst = (int32_t)k;
+                items.push_back(w);
+            }
+        } else {
+            make_instance_items(h->host_row_off.data(), h->sl, h->n, (int)k, shape, items);
+        }
     }
     if (b->d_items) cudaFree(b->d_items);
     b->d_items = nullptr;
@@ -185,7 +197,7 @@ int autotune(irr_batch* b)
         auto it = g_tune_cache.find(key);
         if (it != g_tune_cache.end()) b->shape = it->second;
         if (it != g_tune_cache.end()) {
-            const int rc = set_lanes(b, b->shape.lanes_per_row);
+            const int rc = set_lanes(b, b->shape.lanes_per_row, b->shape.staged);
             return rc ? rc : upload_items(b, b->shape);
         }
     }
@@ -193,13 +205,29 @@ int autotune(irr_batch* b)
     const int rows[] = {64, 256, 1024};
     TiledShape best = b->shape;
     double best_ms = 1e30;
+    // the staged layout first (4 lanes per row; items are its own), where every instance takes it
+    {
+        int rc = set_lanes(b, 4, 1);
+        if (rc == IRR_OK) {
+            TiledShape s = b->shape;
+            s.lanes_per_row = 4;
+            s.staged = 1;
+            const double ms = time_shape(b, s, 3);
+            if (ms < 0) return bfail(b, IRR_ERR_CUDA, "autotune launch");
+            best_ms = ms;
+            best = s;
+        } else if (rc != IRR_ERR_CAPACITY) {
+            return rc;
+        }
+    }
     for (int g : lanes) {
-        const int rc = set_lanes(b, g);
+        const int rc = set_lanes(b, g, 0);
         if (rc) return rc;
         for (int r : rows) {
             TiledShape s = b->shape;
             s.lanes_per_row = g;
             s.block_nodes = r;
+            s.staged = 0;
             const double ms = time_shape(b, s, 3);
             if (ms < 0) return bfail(b, IRR_ERR_CUDA, "autotune launch");
             if (ms < best_ms) {
@@ -213,7 +241,7 @@ int autotune(irr_batch* b)
         std::lock_guard<std::mutex> lock(g_tune_mutex);
         g_tune_cache[key] = best;
     }
-    const int rc = set_lanes(b, b->shape.lanes_per_row);
+    const int rc = set_lanes(b, b->shape.lanes_per_row, b->shape.staged);
     return rc ? rc : upload_items(b, b->shape);
 }
 
@@ -303,8 +331,19 @@ int irr_batch_finalize(irr_batch* b, int autotune_shape)
         b->nodes += h->n;
         b->edges += h->e;
     }
-    int rc = autotune_shape ? autotune(b) : set_lanes(b, b->shape.lanes_per_row);
-    if (!rc && !autotune_shape) rc = upload_items(b, b->shape);
+    int rc = IRR_OK;
+    if (autotune_shape) {
+        rc = autotune(b);
+    } else {
+        // the staged layout where every instance takes it (4 lanes per row), else sliced / CSR
+        b->shape.staged = b->shape.lanes_per_row == 4 ? 1 : 0;
+        rc = set_lanes(b, b->shape.lanes_per_row, b->shape.staged);
+        if (rc == IRR_ERR_CAPACITY) {
+            b->shape.staged = 0;
+            rc = set_lanes(b, b->shape.lanes_per_row, 0);
+        }
+        if (!rc) rc = upload_items(b, b->shape);
+    }
     if (rc) return rc;
     b->finalized = true;
     return IRR_OK;
@@ -392,7 +431,7 @@ int irr_autotune(irr_handle* h)
     if (!rc) rc = irr_batch_finalize(b, 1);
     if (!rc) {
         // the handle's own layout and work items for the chosen shape
-        rc = irr_ensure_layout(h, b->shape.lanes_per_row, b->shape.block_nodes);
+        rc = irr_ensure_layout(h, b->shape.lanes_per_row, b->shape.block_nodes, b->shape.staged);
     } else {
         h->err = std::string("autotune: ") + b->err;
     }

@@ -56,6 +56,8 @@ struct irr_handle {
 };
 
 // (Re)builds the handle's entry layout for G lanes per row as its config asks
-// (sliced or CSR), then its instance descriptor and work items, so that the
-// three always agree.  Partitioned, initialised handles only.
-int irr_ensure_layout(irr_handle* h, int lanes_per_row, int block_nodes);
+// (staged, sliced or CSR), then its instance descriptor and work items, so
+// that the three always agree.  staged_ok = 0 keeps an AUTO handle off the
+// staged layout (a handle configured IRR_LAYOUT_STAGED then fails with
+// IRR_ERR_STATE).  Partitioned, initialised handles only.
+int irr_ensure_layout(irr_handle* h, int lanes_per_row, int block_nodes, int staged_ok = 1);

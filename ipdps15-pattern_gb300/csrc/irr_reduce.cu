@@ -118,6 +118,24 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
     }
 }
 
+// The same bound, polling with a growing sleep (32 ns doubling up to MAX_NS)
+// between tests: a warp that waits long -- the producer, waiting for the
+// consumers to free a stage -- then takes few issue slots from the warps
+// that work on its SM sub-partition (without the sleep a waiting producer
+// polled ~450 times per work item).
+template <uint32_t MAX_NS>
+__device__ __forceinline__ bool mbar_wait_backoff(uint64_t* bar, uint32_t parity, uint64_t limit_ns)
+{
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = global_ns();
+    uint32_t ns = 32;
+    for (;;) {
+        __nanosleep(ns);
+        if (mbar_try_wait(bar, parity)) return true;
+        if (global_ns() - t0 > limit_ns) return false;
+        if (ns < MAX_NS) ns <<= 1;
+    }
+}
 
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar)
 {
@@ -596,6 +614,12 @@ __global__ void __launch_bounds__(kPipeThreads, kCtasPerSm) tiled_kernel(
 // an L1 miss's hundreds, and the entry order of the layout spreads each
 // quarter-warp's 8 loads over the 8 bank groups.  G = 4 lanes per row.
 constexpr int kHaloStageWords = kHaloStreamMax + 4 * kHaloTabMax;  // 32-bit words per stage
+// The consumers add a table's address to both 16-bit halves of a word at once,
+// which needs every shared address of the CTA below 2^16: the stages, the id
+// buffers, the barriers and the system's reserved kilobyte.
+static_assert(kHaloStages * kHaloStageWords * 4 + kHaloStages * (kHaloTabMax + 8) * 4 + 1024 + 1024 <
+                  65536,
+              "shared addresses fit 16 bits");
 
 __device__ __forceinline__ void cp_async16(uint32_t dst_smem, const void* src)
 {
@@ -626,36 +650,94 @@ __device__ __forceinline__ float4 lds128(uint32_t addr)
     return v;
 }
 
-// The slices of a staged work item that belong to consumer warp `cw`; `sw`
-// is the stage (words, then the table at word kHaloStreamMax).
+// The slices of a staged work item (first row row0, nrows rows) that consumer
+// warp `lane32`'s warp claims from the stage's counter *claim (a warp done
+// with one slice takes the next unclaimed one, so the item's slices of
+// different lengths spread over the warps); `sw` is the stage (words, then
+// the table at word kHaloStreamMax) and soff the slices' word offsets within
+// it.  Two 16-bit table offsets of a word become shared addresses with one
+// add: every address of the CTA's shared window is below 2^16, so the low
+// half cannot carry into the high one.
+// Build-time variants (each an equal amount of work):
+//   IRR_HALO_DYNAMIC   1: warps claim slices from the stage's counter;
+//                      0: warp w takes slices w, w + 8, ...
+//   IRR_HALO_PAIR_ADDR 1: one add forms both table addresses of a word;
+//   IRR_HALO_UNROLL    the step loop's unroll factor;
+//   IRR_HALO_CWAIT     the consumers' stage wait polls with a sleep of up to
+//                      this many ns (0: suspend-hinted polls, no sleep);
+//   IRR_HALO_PWAIT     the same for the producer's wait for a free stage.
+// On the 4M-node workload (ms per step): static 0.396 vs dynamic 0.414 slice
+// claims; pair addresses 0.391 vs 0.396; 7 consumer warps 0.455 and 3 CTAs
+// per SM 0.415 vs 8 warps x 4 CTAs 0.396.
+#ifndef IRR_HALO_DYNAMIC
+#define IRR_HALO_DYNAMIC 0
+#endif
+#ifndef IRR_HALO_PAIR_ADDR
+#define IRR_HALO_PAIR_ADDR 1
+#endif
+#ifndef IRR_HALO_UNROLL
+#define IRR_HALO_UNROLL 1
+#endif
+constexpr int kHaloUnroll = IRR_HALO_UNROLL;
+#ifndef IRR_HALO_CWAIT
+#define IRR_HALO_CWAIT 128
+#endif
+#ifndef IRR_HALO_PWAIT
+#define IRR_HALO_PWAIT 256
+#endif
+
+// A bounded wait that sleeps up to MAX_NS between polls, or (MAX_NS == 0)
+// polls with the suspend hint only.
+template <uint32_t MAX_NS>
+__device__ __forceinline__ bool mbar_wait_policy(uint64_t* bar, uint32_t parity, uint64_t limit_ns)
+{
+    if constexpr (MAX_NS == 0) return mbar_wait_bounded(bar, parity, limit_ns);
+    else return mbar_wait_backoff<MAX_NS>(bar, parity, limit_ns);
+}
+
 template <bool PERIODIC>
-__device__ __forceinline__ void consume_halo(const WorkItem& w, const InstHot& I, const uint32_t* sw,
-                                             int cw, int lane32)
+__device__ __forceinline__ void consume_halo(int row0, int nrows, const uint32_t* soff, int* claim,
+                                             const InstHot& I, const uint32_t* sw, int lane32,
+                                             int warp)
 {
     const int lane = lane32 & 3;
-    const uint32_t* __restrict__ slice_off = I.slice_off;
     float4* __restrict__ force = I.force;
     const LawParams* __restrict__ cold = I.cold;
     const int64_t n = I.n;
     const HotLaw H = I.H;
     const uint32_t words_u32 = smem_u32(sw);
     const uint32_t tab_u32 = smem_u32(sw + kHaloStreamMax);
-    const int s0 = w.row0 / 8;
-    const int ns = (w.nrows + 7) / 8;
-    for (int q = cw; q < ns; q += kConsumerWarps) {
-        const uint32_t o0 = __ldg(slice_off + s0 + q);
-        const uint32_t steps = ((__ldg(slice_off + s0 + q + 1) - o0) >> 5) - 1;
-        uint32_t addr = words_u32 + 4u * (o0 - w.ent0 + (uint32_t)lane32);
+    const uint32_t tab_pair = tab_u32 * 0x10001u;  // the table's address in both halves
+    const int s0 = row0 / 8;
+    const int ns = (nrows + 7) / 8;
+    for (int qs = warp;; qs += kConsumerWarps) {
+        int q = qs;
+        if (IRR_HALO_DYNAMIC) {
+            if (lane32 == 0) q = atomicAdd(claim, 1);
+            q = __shfl_sync(0xffffffffu, q, 0);
+        }
+        if (q >= ns) break;
+        const uint32_t o0 = soff[q];
+        const uint32_t steps = ((soff[q + 1] - o0) >> 5) - 1;
+        uint32_t addr = words_u32 + 4u * (o0 + (uint32_t)lane32);
         const uint32_t hdr = lds32(addr);
         const float4 a = lds128(tab_u32 + (hdr & 0xffffu));
         const uint32_t len = hdr >> 16;
         const int64_t r = (int64_t)(s0 + q) * 8 + lane32 / 4;
         float2 ax = make_float2(0.f, 0.f), ay = ax, az = ax;
+#pragma unroll kHaloUnroll
         for (uint32_t t = 0; t < steps; t++) {
             addr += 128u;
-            const uint32_t wd = lds32(addr);
-            const float4 b0 = lds128(tab_u32 + (wd & 0xffffu));
-            const float4 b1 = lds128(tab_u32 + (wd >> 16));
+            float4 b0, b1;
+            if (IRR_HALO_PAIR_ADDR) {
+                const uint32_t wd = lds32(addr) + tab_pair;
+                b0 = lds128(wd & 0xffffu);
+                b1 = lds128(wd >> 16);
+            } else {
+                const uint32_t wd = lds32(addr);
+                b0 = lds128(tab_u32 + (wd & 0xffffu));
+                b1 = lds128(tab_u32 + (wd >> 16));
+            }
             const uint32_t k0 = 8 * t + lane;
             lj_pair<PERIODIC>(a, b0, b1, k0 < len, k0 + 4 < len, H, cold, ax, ay, az);
         }
@@ -676,6 +758,15 @@ __global__ void __launch_bounds__(kPipeThreads, kCtasPerSm) halo_kernel(
     __shared__ uint64_t full[kHaloStages];
     __shared__ uint64_t empty[kHaloStages];
     __shared__ int s_item[kHaloStages];
+    // per stage: the item's (instance, first row, rows) and its slices' word
+    // offsets within the stage, so that the consumers read no global memory
+    __shared__ int4 s_meta[kHaloStages];
+    __shared__ uint32_t s_soff[kHaloStages][kHaloSlicesPerItem + 1];
+    // per stage: the item's table ids (bulk-copied in whole 16-byte words, so
+    // up to 3 ids before and after them), read by the producer's lanes
+    __shared__ __align__(16) int32_t s_ids[kHaloStages][kHaloTabMax + 8];
+    __shared__ uint64_t idsbar[kHaloStages];
+    __shared__ int s_claim[kHaloStages];  // the next unclaimed slice of the stage's item
     const int warp = threadIdx.x / 32;
     const int lane = threadIdx.x % 32;
 
@@ -683,48 +774,90 @@ __global__ void __launch_bounds__(kPipeThreads, kCtasPerSm) halo_kernel(
         for (int s = 0; s < kHaloStages; s++) {
             mbar_init(&full[s], 33);  // the bulk copy's arrive + one per producer lane
             mbar_init(&empty[s], kConsumerWarps);
+            mbar_init(&idsbar[s], 1);
         }
     }
     __syncthreads();
 
     if (warp == kConsumerWarps) {
         if (withhold) return;
+        // Item k + 1 is prepared while item k's copies are in flight: its
+        // claim, its descriptor, its slices' word offsets (lane j holds the
+        // j-th) and the bulk copy of its table ids into s_ids, so that the
+        // lanes can issue item k + 1's position copies without waiting on
+        // memory once its stage is free.
+        int nxt = 0;
+        WorkItem wn{};
+        uint32_t soff_n = 0;
+        auto prepare = [&](int stage) {
+            nxt = __shfl_sync(0xffffffffu, nxt, 0);
+            if (nxt >= num_items) return;
+            wn = items[nxt];
+            const InstDesc* In;
+            if constexpr (ONE) In = &src.d;
+            else In = insts + wn.inst;
+            const int ns = (wn.nrows + 7) / 8;
+            soff_n = (lane <= ns && lane <= kHaloSlicesPerItem)
+                         ? __ldg(In->slice_off + wn.row0 / 8 + lane) - wn.ent0
+                         : 0u;
+            if (lane == 0) {  // whole 16-byte words around the item's ids
+                const uint32_t a0 = wn.tab0 & ~3u;
+                const uint32_t cnt = ((wn.tab0 & 3u) + wn.ntab + 3u) & ~3u;
+                bulk_load(s_ids[stage], In->tab + a0, cnt * 4u, &idsbar[stage]);
+            }
+        };
+        if (lane == 0) nxt = atomicAdd(queue, 1);
+        prepare(0);
         for (int k = 0;; k++) {
             const int s = k % kHaloStages;
             const int use = k / kHaloStages;
-            int it = 0;
-            if (lane == 0) {
-                if (use > 0 && !mbar_wait_bounded(&empty[s], (uint32_t)(use - 1) & 1u, wait_ns)) {
-                    atomicOr(status, kStatusWaitTimeout);
-                    it = -1;
-                } else {
-                    const int got = atomicAdd(queue, 1);
-                    it = got < num_items ? got : num_items;
-                    s_item[s] = it;
-                }
-            }
-            it = __shfl_sync(0xffffffffu, it, 0);
-            if (it < 0) {  // a wait gave up: leave with none of this lane's copies in flight
+            const int it = nxt < num_items ? nxt : num_items;
+            const WorkItem w = wn;
+            const uint32_t so = soff_n;
+            int ok = 1;
+            if (lane == 0 && use > 0)
+                ok = mbar_wait_policy<IRR_HALO_PWAIT>(&empty[s], (uint32_t)(use - 1) & 1u, wait_ns) ? 1 : 0;
+            ok = __shfl_sync(0xffffffffu, ok, 0);
+            if (!ok) {  // a wait gave up: leave with none of this lane's copies in flight
+                if (lane == 0) atomicOr(status, kStatusWaitTimeout);
+                mbar_wait_backoff<256>(&idsbar[s], (uint32_t)use & 1u, wait_ns);
                 asm volatile("cp.async.wait_all;" ::: "memory");
                 return;
             }
+            if (lane == 0) s_item[s] = it;
             if (it >= num_items) {  // no more work: complete the stage's phase for the consumers
                 if (lane == 0) mbar_arrive(&full[s]);
                 mbar_arrive(&full[s]);
                 asm volatile("cp.async.wait_all;" ::: "memory");
                 return;
             }
-            const WorkItem w = items[it];
+            if (lane == 0) nxt = atomicAdd(queue, 1);  // item k + 1: the claim is in flight
             const InstDesc* I;
             if constexpr (ONE) I = &src.d;
             else I = insts + w.inst;
             uint32_t* sw = stage_base + s * kHaloStageWords;
+            // the metadata, written before the stage is published: lane 0's
+            // arrive (release) follows every lane's writes through __syncwarp
+            const int ns = (w.nrows + 7) / 8;
+            if (lane <= ns && lane <= kHaloSlicesPerItem) s_soff[s][lane] = so;
+            if (lane == 0) {
+                s_meta[s] = make_int4(w.inst, w.row0, w.nrows, 0);
+                s_claim[s] = 0;  // every consumer has left the stage's previous item
+            }
+            __syncwarp();
             if (lane == 0) bulk_load(sw, I->words + w.ent0, w.nent * 4u, &full[s]);
+            // the table: its ids arrived by the bulk copy of the iteration before
+            if (!mbar_wait_backoff<64>(&idsbar[s], (uint32_t)use & 1u, wait_ns)) {
+                if (lane == 0) atomicOr(status, kStatusWaitTimeout);
+                asm volatile("cp.async.wait_all;" ::: "memory");
+                return;  // the consumers' wait for this stage runs out too
+            }
             const uint32_t tab_u32 = smem_u32(sw + kHaloStreamMax);
-            const int32_t* __restrict__ ids = I->tab + w.tab0;
+            const int32_t* ids = s_ids[s] + (w.tab0 & 3u);
             const float4* __restrict__ pos = I->pos;
-            for (uint32_t j = lane; j < w.ntab; j += 32) cp_async16(tab_u32 + 16u * j, pos + __ldg(ids + j));
+            for (uint32_t j = lane; j < w.ntab; j += 32) cp_async16(tab_u32 + 16u * j, pos + ids[j]);
             cp_async_arrive(&full[s]);
+            prepare((k + 1) % kHaloStages);
         }
     }
 
@@ -732,23 +865,24 @@ __global__ void __launch_bounds__(kPipeThreads, kCtasPerSm) halo_kernel(
     InstHot hot{};
     for (int k = 0;; k++) {
         const int s = k % kHaloStages;
-        if (!mbar_wait_bounded(&full[s], (uint32_t)(k / kHaloStages) & 1u, wait_ns)) {
+        if (!mbar_wait_policy<IRR_HALO_CWAIT>(&full[s], (uint32_t)(k / kHaloStages) & 1u, wait_ns)) {
             if (lane == 0) atomicOr(status, kStatusWaitTimeout);
-            mbar_wait_bounded(&full[s], (uint32_t)(k / kHaloStages) & 1u, wait_ns);
+            mbar_wait_policy<IRR_HALO_CWAIT>(&full[s], (uint32_t)(k / kHaloStages) & 1u, wait_ns);
             return;
         }
         const int it = s_item[s];
         if (it >= num_items) return;
-        const WorkItem w = items[it];
+        const int4 m = s_meta[s];  // instance, first row, rows
         if constexpr (ONE) {
             hot = load_hot(&src.d);
         } else if constexpr (TABLE) {
-            hot = hot_from(src, insts, w.inst);
-        } else if (w.inst != cur) {
-            hot = load_hot(insts + w.inst);
-            cur = w.inst;
+            hot = hot_from(src, insts, m.x);
+        } else if (m.x != cur) {
+            hot = load_hot(insts + m.x);
+            cur = m.x;
         }
-        consume_halo<PERIODIC>(w, hot, stage_base + s * kHaloStageWords, warp, lane);
+        consume_halo<PERIODIC>(m.y, m.z, s_soff[s], &s_claim[s], hot, stage_base + s * kHaloStageWords, lane,
+                               warp);
         __syncwarp();
         if (lane == 0) mbar_arrive(&empty[s]);
     }

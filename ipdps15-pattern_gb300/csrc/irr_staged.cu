@@ -332,7 +332,8 @@ cudaError_t build_staged(const uint32_t* row_off, const int32_t* col, const uint
     int* d_status = nullptr;
     e = alloc_n(&out.slice_off, S + 1, s);
     if (e == cudaSuccess) e = alloc_n(&out.words, out.nwords, s);
-    if (e == cudaSuccess) e = alloc_n(&out.ids, out.nids, s);
+    // 4 ids of slack: the kernel bulk-copies each item's ids in whole 16-byte words
+    if (e == cudaSuccess) e = alloc_n(&out.ids, out.nids + 4, s);
     if (e == cudaSuccess) e = alloc_n(&d_items, (int64_t)items.size(), s);
     if (e == cudaSuccess) e = alloc_n(&d_status, 1, s);
     if (e == cudaSuccess)

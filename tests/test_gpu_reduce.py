@@ -169,12 +169,18 @@ def test_sliced_layout_gives_the_csr_sums(built_lib, name, lanes):
 
 
 def test_auto_layout_choice(built_lib):
-    """AUTO takes the sliced layout for near-uniform rows and keeps CSR when
-    one long row would make the padding dominate."""
+    """AUTO takes the staged layout where it applies (4 lanes per row, the
+    shared-memory stages, tables within their limit), else the sliced layout
+    for near-uniform rows, and keeps CSR when long rows would make the padding
+    dominate."""
     import irregular_gb300 as irr
     c = load_golden("moldyn_random_2048")
     _, h = run_case(irr, c, exec=1)
-    assert h.info().layout == irr.IRR_LAYOUT_SLICED
+    assert h.info().layout == irr.IRR_LAYOUT_STAGED
+    for cfg in (dict(lanes_per_row=8), dict(stage_smem=0)):
+        _, hs = run_case(irr, c, exec=1, **cfg)
+        assert hs.info().layout == irr.IRR_LAYOUT_SLICED, cfg
+        hs.close()
     n = c["pos"].shape[0]
     # 32 hub nodes joined to every other node: their slices pad 8 rows each
     # to ~n entries, far more than half the entries
