@@ -106,10 +106,24 @@ struct TiledShape {
 // rows (irr_staged.cu): per work item a table of node ids whose positions the
 // kernel gathers into shared memory, and per slice 32 header words and 32
 // words per step of 16-bit byte offsets into that table.
-constexpr int kHaloSlicesPerItem = 8;   // 64 rows per item at most
-constexpr int kHaloTabMax = 640;        // table ids per item (10 KB of positions)
-constexpr int kHaloStreamMax = 3584;    // words per item (14 KB)
-constexpr int kHaloStages = 2;          // shared-memory ring depth
+// (each can be set at build time, -DIRR_HALO_SLICES=... etc., to build and
+// time variants; the oracle's layout takes the same three limits)
+#ifndef IRR_HALO_SLICES
+#define IRR_HALO_SLICES 8
+#endif
+#ifndef IRR_HALO_TABMAX
+#define IRR_HALO_TABMAX 640
+#endif
+#ifndef IRR_HALO_STREAMMAX
+#define IRR_HALO_STREAMMAX 3584
+#endif
+#ifndef IRR_HALO_STAGES
+#define IRR_HALO_STAGES 2
+#endif
+constexpr int kHaloSlicesPerItem = IRR_HALO_SLICES;  // 64 rows per item at most
+constexpr int kHaloTabMax = IRR_HALO_TABMAX;         // table ids per item (~10 KB of positions)
+constexpr int kHaloStreamMax = IRR_HALO_STREAMMAX;   // words per item (14 KB)
+constexpr int kHaloStages = IRR_HALO_STAGES;         // shared-memory ring depth
 struct Staged {
     uint32_t* slice_off = nullptr;   // [slices + 1] word offsets (multiples of 32)
     uint32_t* words = nullptr;       // [nwords]

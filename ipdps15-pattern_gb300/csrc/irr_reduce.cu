@@ -617,9 +617,14 @@ constexpr int kHaloStageWords = kHaloStreamMax + 4 * kHaloTabMax;  // 32-bit wor
 // The consumers add a table's address to both 16-bit halves of a word at once,
 // which needs every shared address of the CTA below 2^16: the stages, the id
 // buffers, the barriers and the system's reserved kilobyte.
-static_assert(kHaloStages * kHaloStageWords * 4 + kHaloStages * (kHaloTabMax + 8) * 4 + 1024 + 1024 <
-                  65536,
+#ifndef IRR_HALO_PAIR_ADDR
+#define IRR_HALO_PAIR_ADDR 1
+#endif
+static_assert(!IRR_HALO_PAIR_ADDR ||
+                  kHaloStages * kHaloStageWords * 4 + kHaloStages * (kHaloTabMax + 8) * 4 + 1024 + 1024 <
+                      65536,
               "shared addresses fit 16 bits");
+static_assert(8 * kHaloSlicesPerItem <= 64, "a row's index in its item fits the header's 6 bits");
 
 __device__ __forceinline__ void cp_async16(uint32_t dst_smem, const void* src)
 {
@@ -668,13 +673,33 @@ __device__ __forceinline__ float4 lds128(uint32_t addr)
 //   IRR_HALO_PWAIT     the same for the producer's wait for a free stage.
 // On the 4M-node workload (ms per step): static 0.396 vs dynamic 0.414 slice
 // claims; pair addresses 0.391 vs 0.396; 7 consumer warps 0.455 and 3 CTAs
-// per SM 0.415 vs 8 warps x 4 CTAs 0.396.
+// per SM 0.415 vs 8 warps x 4 CTAs 0.396; rotated claims 0.3877 vs 0.3899;
+// the step loop unrolled by 2 (spills) 0.421; sleep-free waits 0.393; 3-stage
+// rings (3 CTAs per SM, or smaller items at 4) 0.395-0.431; 4 or 6 consumer
+// warps with 6 or 7 CTAs per SM 0.413-0.418; each item's steps cut evenly
+// across the warps (slices split between warps, piece sums joined in shared
+// memory) 0.722: the extra state around the step loop doubled its
+// instructions.  The words prefetched into L2 one item ahead: 0.3907 vs
+// 0.3873.  What the warps still lose is the ring's coupling: a stage is
+// refilled only when its slowest warp is done (~4.3K cycles after the first),
+// and the refill takes ~3.6K cycles, so the first warps wait ~1.2K of each
+// item's ~7.6K cycles.
 #ifndef IRR_HALO_DYNAMIC
 #define IRR_HALO_DYNAMIC 0
 #endif
-#ifndef IRR_HALO_PAIR_ADDR
-#define IRR_HALO_PAIR_ADDR 1
+// IRR_HALO_ROTATE 1: with static claims, warp w takes slice (w + k) mod 8 of
+// the CTA's k-th item (slice 0 holds an item's longest rows, so a fixed
+// assignment would always give warp 0 the longest slice).
+#ifndef IRR_HALO_ROTATE
+#define IRR_HALO_ROTATE 1
 #endif
+// IRR_HALO_PREFETCH 1: when the producer claims an item (one item ahead), it
+// also prefetches the item's words into L2, so that their bulk copy, issued
+// once a stage is free, reads L2 rather than DRAM.
+#ifndef IRR_HALO_PREFETCH
+#define IRR_HALO_PREFETCH 0
+#endif
+
 #ifndef IRR_HALO_UNROLL
 #define IRR_HALO_UNROLL 1
 #endif
@@ -698,19 +723,17 @@ __device__ __forceinline__ bool mbar_wait_policy(uint64_t* bar, uint32_t parity,
 template <bool PERIODIC>
 __device__ __forceinline__ void consume_halo(int row0, int nrows, const uint32_t* soff, int* claim,
                                              const InstHot& I, const uint32_t* sw, int lane32,
-                                             int warp)
+                                             int first)
 {
     const int lane = lane32 & 3;
     float4* __restrict__ force = I.force;
     const LawParams* __restrict__ cold = I.cold;
-    const int64_t n = I.n;
     const HotLaw H = I.H;
     const uint32_t words_u32 = smem_u32(sw);
     const uint32_t tab_u32 = smem_u32(sw + kHaloStreamMax);
     const uint32_t tab_pair = tab_u32 * 0x10001u;  // the table's address in both halves
-    const int s0 = row0 / 8;
     const int ns = (nrows + 7) / 8;
-    for (int qs = warp;; qs += kConsumerWarps) {
+    for (int qs = first;; qs += kConsumerWarps) {
         int q = qs;
         if (IRR_HALO_DYNAMIC) {
             if (lane32 == 0) q = atomicAdd(claim, 1);
@@ -720,10 +743,11 @@ __device__ __forceinline__ void consume_halo(int row0, int nrows, const uint32_t
         const uint32_t o0 = soff[q];
         const uint32_t steps = ((soff[q + 1] - o0) >> 5) - 1;
         uint32_t addr = words_u32 + 4u * (o0 + (uint32_t)lane32);
+        // header: own byte offset | len << 14 | row-in-item << 24 (1 << 31: padding)
         const uint32_t hdr = lds32(addr);
-        const float4 a = lds128(tab_u32 + (hdr & 0xffffu));
-        const uint32_t len = hdr >> 16;
-        const int64_t r = (int64_t)(s0 + q) * 8 + lane32 / 4;
+        const float4 a = lds128(tab_u32 + (hdr & 0x3fffu));
+        const uint32_t len = (hdr >> 14) & 0x3ffu;
+        const int64_t r = (int64_t)row0 + ((hdr >> 24) & 0x3fu);
         float2 ax = make_float2(0.f, 0.f), ay = ax, az = ax;
 #pragma unroll kHaloUnroll
         for (uint32_t t = 0; t < steps; t++) {
@@ -742,7 +766,7 @@ __device__ __forceinline__ void consume_halo(int row0, int nrows, const uint32_t
             lj_pair<PERIODIC>(a, b0, b1, k0 < len, k0 + 4 < len, H, cold, ax, ay, az);
         }
         const float3 f = join_partials<4>(ax, ay, az);
-        if (r < n && lane == 0) force[r] = make_float4(f.x, f.y, f.z, 0.f);
+        if (!(hdr >> 31) && lane == 0) force[r] = make_float4(f.x, f.y, f.z, 0.f);
     }
 }
 
@@ -804,6 +828,10 @@ __global__ void __launch_bounds__(kPipeThreads, kCtasPerSm) halo_kernel(
                 const uint32_t a0 = wn.tab0 & ~3u;
                 const uint32_t cnt = ((wn.tab0 & 3u) + wn.ntab + 3u) & ~3u;
                 bulk_load(s_ids[stage], In->tab + a0, cnt * 4u, &idsbar[stage]);
+                if (IRR_HALO_PREFETCH)
+                    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(In->words + wn.ent0),
+                                 "r"(wn.nent * 4u)
+                                 : "memory");
             }
         };
         if (lane == 0) nxt = atomicAdd(queue, 1);
@@ -882,7 +910,7 @@ __global__ void __launch_bounds__(kPipeThreads, kCtasPerSm) halo_kernel(
             cur = m.x;
         }
         consume_halo<PERIODIC>(m.y, m.z, s_soff[s], &s_claim[s], hot, stage_base + s * kHaloStageWords, lane,
-                               warp);
+                               IRR_HALO_ROTATE ? (warp + k) % kConsumerWarps : warp);
         __syncwarp();
         if (lane == 0) mbar_arrive(&empty[s]);
     }

@@ -952,62 +952,75 @@ int orc_staged_layout(int64_t n, const int64_t *row_off, const int32_t *col, int
 {
     if (n < 0 || slices_per_item < 1 || tab_max < 1 || stream_max < 64) return -2;
     const int64_t S = (n + 7) / 8;
-    int64_t *soff = (int64_t *)malloc(sizeof(int64_t) * (size_t)(S + 1));
+    int64_t *cut = (int64_t *)malloc(sizeof(int64_t) * (size_t)(S + 1));  /* the cut's word counts */
+    int64_t *soff = (int64_t *)malloc(sizeof(int64_t) * (size_t)(S + 1)); /* the slices' words */
     int64_t maxent = 0;
     for (int64_t r = 0; r < n; r++)
         if (row_off[r + 1] - row_off[r] > maxent) maxent = row_off[r + 1] - row_off[r];
     int32_t *buf = (int32_t *)malloc(sizeof(int32_t) * (size_t)((int64_t)slices_per_item * 8 * (maxent + 1) + 8));
     uint16_t *rs = (uint16_t *)malloc(sizeof(uint16_t) * (size_t)(maxent + 1));
-    if (!soff || !buf || !rs) {
-        free(soff);
-        free(buf);
-        free(rs);
+    int64_t *order = (int64_t *)malloc(sizeof(int64_t) * (size_t)(8 * slices_per_item));
+    if (!cut || !soff || !buf || !rs || !order) {
+        free(cut); free(soff); free(buf); free(rs); free(order);
         return -2;
     }
-    soff[0] = 0;
-    for (int64_t q = 0; q < S; q++) {
+    int rc = 0;
+    cut[0] = 0;
+    for (int64_t q = 0; q < S && rc == 0; q++) {
         int64_t T = 0;
         for (int64_t r = 8 * q; r < 8 * q + 8 && r < n; r++) {
             int64_t t = (row_off[r + 1] - row_off[r] + 7) / 8;
             if (t > T) T = t;
         }
-        if (32 * (T + 1) > stream_max) {
-            free(soff);
-            free(buf);
-            free(rs);
-            return -1;
-        }
-        soff[q + 1] = soff[q] + 32 * (T + 1);
+        if (32 * (T + 1) > stream_max) rc = -1;
+        cut[q + 1] = cut[q] + 32 * (T + 1);
     }
-    if (slice_off)
-        for (int64_t q = 0; q <= S; q++) slice_off[q] = (uint32_t)soff[q];
     int64_t it = 0, tab0 = 0;
     int64_t q0 = 0;
-    while (q0 < S) {
-        /* tentative run: at most slices_per_item slices and stream_max words */
+    soff[0] = 0;
+    while (q0 < S && rc == 0) {
+        /* tentative run: at most slices_per_item blocks and stream_max words */
         int64_t q1 = q0 + 1;
-        while (q1 < S && q1 - q0 < slices_per_item && soff[q1 + 1] - soff[q0] <= stream_max) q1++;
+        while (q1 < S && q1 - q0 < slices_per_item && cut[q1 + 1] - cut[q0] <= stream_max) q1++;
         /* cut into the longest prefixes whose tables fit */
         int64_t a = q0;
-        while (a < q1) {
+        while (a < q1 && rc == 0) {
             int64_t b = a + 1, ntab = staged_table(n, row_off, col, 8 * a, 8 * b, buf);
             if (ntab > tab_max) {
-                free(soff);
-                free(buf);
-                free(rs);
-                return -1;
+                rc = -1;
+                break;
             }
             while (b < q1) {
                 int64_t t2 = staged_table(n, row_off, col, 8 * a, 8 * (b + 1), buf);
                 if (t2 > tab_max) break;
                 b++;
-                ntab = t2;
             }
             ntab = staged_table(n, row_off, col, 8 * a, 8 * b, buf);
+            const int64_t r0 = 8 * a, m = (8 * b < n ? 8 * b : n) - 8 * a, ns = b - a;
+            /* the item's rows, longest first (ties by row id): insertion sort */
+            for (int64_t k = 0; k < m; k++) {
+                const int64_t r = r0 + k, len = row_off[r + 1] - row_off[r];
+                int64_t pos = k;
+                while (pos > 0) {
+                    const int64_t o = order[pos - 1], lo = row_off[o + 1] - row_off[o];
+                    if (lo >= len) break;
+                    order[pos] = o;
+                    pos--;
+                }
+                order[pos] = r;
+            }
+            for (int64_t j = 0; j < ns; j++) {
+                int64_t T = 0;
+                for (int64_t i = 8 * j; i < 8 * j + 8 && i < m; i++) {
+                    const int64_t t = (row_off[order[i] + 1] - row_off[order[i]] + 7) / 8;
+                    if (t > T) T = t;
+                }
+                soff[a + j + 1] = soff[a + j] + 32 * (T + 1);
+            }
             if (items) {
                 int32_t *w = items + 6 * it;
-                w[0] = (int32_t)(8 * a);
-                w[1] = (int32_t)((8 * b < n ? 8 * b : n) - 8 * a);
+                w[0] = (int32_t)r0;
+                w[1] = (int32_t)m;
                 w[2] = (int32_t)soff[a];
                 w[3] = (int32_t)(soff[b] - soff[a]);
                 w[4] = (int32_t)tab0;
@@ -1015,16 +1028,20 @@ int orc_staged_layout(int64_t n, const int64_t *row_off, const int32_t *col, int
             }
             if (ids) memcpy(ids + tab0, buf, sizeof(int32_t) * (size_t)ntab);
             if (words) {
-                for (int64_t q = a; q < b; q++) {
+                for (int64_t j = 0; j < ns; j++) {
+                    const int64_t q = a + j;
                     const int64_t T = (soff[q + 1] - soff[q]) / 32 - 1;
                     uint32_t *sw = words + soff[q];
                     for (int i = 0; i < 8; i++) {
-                        const int64_t r = 8 * q + i;
+                        const int64_t pos = 8 * j + i;
                         int64_t len = 0, own = 0;
                         int64_t cnt[8] = {0}, cur[8] = {0}, beg[8] = {0};
-                        if (r < n) {
+                        uint32_t hdr = 1u << 31;  /* a padding row */
+                        if (pos < m) {
+                            const int64_t r = order[pos];
                             len = row_off[r + 1] - row_off[r];
                             own = staged_slot(buf, ntab, (int32_t)r);
+                            hdr = (uint32_t)(own * 16) | ((uint32_t)len << 14) | ((uint32_t)(r - r0) << 24);
                             /* the row's slots bucketed by bank group, ascending */
                             for (int64_t k = 0; k < len; k++) cnt[staged_slot(buf, ntab, col[row_off[r] + k]) & 7]++;
                             int64_t acc = 0;
@@ -1039,7 +1056,7 @@ int orc_staged_layout(int64_t n, const int64_t *row_off, const int32_t *col, int
                                 rs[fill[sl & 7]++] = (uint16_t)sl;
                             }
                         }
-                        for (int l = 0; l < 4; l++) sw[4 * i + l] = (uint32_t)(own * 16) | ((uint32_t)len << 16);
+                        for (int l = 0; l < 4; l++) sw[4 * i + l] = hdr;
                         const int p = i & 1;
                         for (int64_t t = 0; t < T; t++) {
                             uint32_t pk[2][4];
@@ -1069,11 +1086,17 @@ int orc_staged_layout(int64_t n, const int64_t *row_off, const int32_t *col, int
         }
         q0 = q1;
     }
-    if (num_items) *num_items = it;
-    if (num_words) *num_words = soff[S];
-    if (num_ids) *num_ids = tab0;
+    if (rc == 0) {
+        if (slice_off)
+            for (int64_t q = 0; q <= S; q++) slice_off[q] = (uint32_t)soff[q];
+        if (num_items) *num_items = it;
+        if (num_words) *num_words = soff[S];
+        if (num_ids) *num_ids = tab0;
+    }
+    free(cut);
     free(soff);
     free(buf);
     free(rs);
-    return 0;
+    free(order);
+    return rc;
 }

@@ -144,17 +144,25 @@ int orc_partition_curve(int64_t n, const float *pos, const float lo[3], const fl
  * ascending), for 4 lanes per row and slices of 8 rows -- the GPU builder's
  * output, bit for bit.  No reference counterpart: it restates the library's
  * own layout so that the GPU pass is checked as integer work.
- *   Slices: slice q is rows [8q, 8q + 8) (clipped to n); T_q = the longest
- *     row's entries / 8 rounded up; it takes 32 (T_q + 1) words.
- *   Items: the slices are cut greedily into runs of at most slices_per_item
- *     slices and stream_max words; each run is then cut greedily into the
- *     longest prefixes whose table -- the sorted distinct ids of the item's
- *     rows and of all their columns -- holds at most tab_max ids.
+ *   Cut: the rows are taken 8 at a time in order (block q: rows [8q, 8q + 8),
+ *     clipped to n, taking 32 (T + 1) words with T = its longest row's entries
+ *     / 8 rounded up); the blocks are cut greedily into runs of at most
+ *     slices_per_item blocks and stream_max words; each run is then cut
+ *     greedily into the longest prefixes whose table -- the sorted distinct
+ *     ids of the item's rows and of all their columns -- holds at most tab_max
+ *     ids.  An item of rows [r0, r0 + m) covers ceil(m / 8) slices.
+ *   Slices: within an item the rows are ordered by entry count, longest
+ *     first (ties by row id), and slice j of the item takes rows 8j .. 8j + 7
+ *     of that order (positions past m are padding rows), so that rows of a
+ *     slice have similar lengths; slice j takes 32 (T_j + 1) words, T_j = its
+ *     longest row's entries / 8 rounded up (never more words than the cut
+ *     counted).  slice_off holds each slice's first word.
  *   Words of a slice: word 4i + l (row i, lane l) of its first 32 is the
- *     header own | len << 16 (own: the byte offset 16 * slot of the row's own
- *     id in the item's table; a row past n has own 0 and len 0); word
- *     32 (t + 1) + 4i + l is b0 | b1 << 16, the byte offsets of the row's picks
- *     (t, 0, l) and (t, 1, l).  Row i (parity p = i & 1) picks in the order
+ *     header own | len << 14 | lrow << 24 (own: the byte offset 16 * slot of
+ *     the row's own id in the item's table; len < 1024; lrow = row - r0); a
+ *     padding row's header is 1 << 31; word 32 (t + 1) + 4i + l is
+ *     b0 | b1 << 16, the byte offsets of the row's picks (t, 0, l) and
+ *     (t, 1, l).  Row i (parity p = i & 1) picks in the order
  *     (t, h, l): from bank group g = (2t + h + 4p + l) mod 8 (a slot's group is
  *     slot mod 8) its lowest remaining entry; if that group is empty, from the
  *     group with the most remaining entries (the lowest such group); when

@@ -4,9 +4,11 @@ properties the GPU kernel relies on, on a curve-ordered random box.
   * items cover the slices in order, each within the limits (8 slices, 3,584
     words, 640 table ids), and every prefix cut is the longest that fits;
   * each item's table is its rows' and their neighbours' ids, sorted, distinct;
-  * each row's header gives its own table slot and its length, its first
-    `len` picks are exactly its neighbours (as a multiset) and the rest are
-    its own slot;
+  * every row of an item appears in exactly one of its slices, longest rows
+    first, and the slices pad less than slices of 8 consecutive rows would;
+  * each row's header gives its own table slot, its length and its index in
+    the item, its first `len` picks are exactly its neighbours (as a
+    multiset) and the rest are its own slot;
   * the bank-group order keeps a quarter-warp's 8 128-bit table loads at ~5.4
     shared-memory wavefronts (8 at random would be ~9).
 """
@@ -59,27 +61,32 @@ def test_items_cover_and_cut(case):
 def test_rows_reconstruct_and_banks(case):
     O, row_off, col, L = case
     it, so, w, ids = L["items"], L["slice_off"].astype(np.int64), L["words"], L["ids"]
-    n = row_off.shape[0] - 1
+    deg = np.diff(row_off)
     wf = lds = 0
     for k in range(0, it.shape[0], 7):
         row0, nrows, w0, nw, t0, nt = it[k]
         tab = ids[t0:t0 + nt]
+        seen = []
         for q in range(row0 // 8, (row0 + nrows + 7) // 8):
             T = (so[q + 1] - so[q]) // 32 - 1
             sw = w[so[q]:so[q + 1]].reshape(T + 1, 32)
+            lens = []
             for i in range(8):
-                r = 8 * q + i
                 hdr = sw[0, 4 * i:4 * i + 4]
                 assert np.all(hdr == hdr[0])
-                own, ln = (int(hdr[0]) & 0xFFFF) // 16, int(hdr[0]) >> 16
-                if r >= n:
-                    assert own == 0 and ln == 0
+                h0 = int(hdr[0])
+                if h0 == 1 << 31:  # a padding row
                     continue
+                own, ln, lrow = (h0 & 0x3FFF) // 16, (h0 >> 14) & 0x3FF, (h0 >> 24) & 0x3F
+                r = row0 + lrow
+                seen.append(r)
+                lens.append(ln)
                 assert tab[own] == r and ln == row_off[r + 1] - row_off[r]
                 picks = [((int(sw[t + 1, 4 * i + l]) >> (16 * h)) & 0xFFFF) // 16
                          for t in range(T) for h in range(2) for l in range(4)]
                 assert sorted(tab[picks[:ln]].tolist()) == sorted(col[row_off[r]:row_off[r + 1]].tolist())
                 assert all(p == own for p in picks[ln:])
+            assert lens == sorted(lens, reverse=True) and T == (max(lens) + 7) // 8
             for t in range(T):
                 for h in range(2):
                     for ph in range(4):
@@ -87,7 +94,12 @@ def test_rows_reconstruct_and_banks(case):
                                        for j in range(8)]) // 16
                         wf += max(1, np.bincount(a % 8, minlength=8).max())
                     lds += 1
+        assert sorted(seen) == list(range(row0, row0 + nrows))
     assert wf / lds < 6.0, wf / lds
+    # padding: slots over entries, against slices of 8 consecutive rows
+    slots = 2 * (int(so[-1]) - 32 * (so.shape[0] - 1))
+    consecutive = sum(64 * ((deg[r:r + 8].max() + 7) // 8) for r in range(0, deg.shape[0], 8))
+    assert slots / deg.sum() < 1.12 and slots < 0.95 * consecutive, (slots / deg.sum(), consecutive / deg.sum())
 
 
 def test_layout_does_not_apply_to_a_hub(oracle_lib):
