@@ -259,6 +259,75 @@ IRR_API int irr_get_partition(irr_handle *h, int32_t *perm, int64_t *row_off, in
 IRR_API int irr_get_staged(irr_handle *h, int64_t *counts, int32_t *items, uint32_t *slice_off,
                            uint32_t *words, int32_t *ids);
 
+/* ------------------------------------------------- user per-edge functions
+ * The irregular.h plugin.  The reference compiles the application's
+ * irregular.h -- `map`, `reduce` and their __constant__ function tables
+ * (moldyn/irregular.h:9-118) -- into its executors and calls
+ * map_function_table[map_idx] once per edge (moldyn/irregular/gpu_kernel.cu:
+ * 44-58, irregular_runtime.cu:493-501).  Here the application compiles its
+ * irregular.h together with irregular_plugin.cuh, which turns the tables (or
+ * one map) into a kernel and a launch function of type irr_user_launch_fn;
+ * irr_set_user_map hands that function to a partitioned handle, and every
+ * irr_step calls it with the view below on the handle's stream.
+ *
+ * The kernel gives each node's row its own reduction object and presents
+ * each of the row's entries to `map` as the edge (row, neighbour): row is
+ * idx0, part_index[x] == part_id holds for x == row only, and the object
+ * keeps inserts keyed by the row (first insert copied, later ones combined
+ * by `reduce` in the row's entry order, as the reference's reduction objects
+ * do: moldyn/irregular/ros.cu:10-68).  Every listed edge is thus evaluated
+ * once from each end, and each end keeps the contribution the map gives its
+ * idx0: right for pair laws, whose idx1 contribution is the idx0
+ * contribution of the reversed edge (both reference maps).  Node ids are
+ * execution-order ids, consistent across point_data, part_index and keys. */
+typedef struct irr_user_view {
+    int64_t num_nodes;
+    const uint32_t *row_off;  /* [num_nodes + 1] device; rows in execution order  */
+    const int32_t *col;       /* [row_off[num_nodes]] neighbour ids, ascending     */
+    void *node_data;          /* [num_nodes] node records, execution order         */
+    int node_elm_size;        /* bytes per node record                             */
+    int value_size;           /* bytes per result record (sizeof(VALUE))           */
+    void *param;              /* device copy of the parameter block                */
+    int param_size;
+    int map_idx;              /* table entries chosen by irr_set_map / _reduce     */
+    int reduce_idx;
+    int *part_index;          /* [num_nodes] device, part_index[x] = x             */
+    void *values;             /* [num_nodes] result records, execution order       */
+    int *status;              /* device status word: nonzero reports IRR_ERR_DEVICE */
+    int num_sms;
+} irr_user_view;
+
+/* Launches the user kernel on `stream` (a cudaStream_t); returns an
+ * irr_status (IRR_ERR_ARG for a table index out of range). */
+typedef int (*irr_user_launch_fn)(const irr_user_view *view, void *stream, void *ctx);
+
+/* Result records of a user map. */
+enum irr_value_kind {
+    IRR_VALUE_BYTES = 0, /* opaque: read back at value_size bytes only          */
+    IRR_VALUE_F32 = 1    /* floats: also readable widened to doubles, at twice
+                            value_size (moldyn reads its float3 VALUEs into
+                            double f[][3], moldyn/moldyn.cu:391)                */
+};
+
+/* Binds a user map to a partitioned handle before irr_init (IRR_ERR_STATE
+ * after it, or on a plain handle at irr_init).  value_size: a multiple of 4
+ * in [4, 256].  While bound: irr_set_map / irr_set_reduce select table
+ * entries (map_idx / reduce_idx of the view; the launch function checks the
+ * range); irr_set_params keeps the block as given (any size up to 64 KiB);
+ * irr_set_nodes takes records of any multiple of 4 bytes up to 1024, and the
+ * node order comes from irr_set_coordinates when given, else from records of
+ * 12, 16 or 24 bytes read as positions, else the caller's order is kept;
+ * irr_get_result reads value_size-byte records (or, for IRR_VALUE_F32,
+ * 2 * value_size-byte doubles).  launch == NULL unbinds (before irr_init). */
+IRR_API int irr_set_user_map(irr_handle *h, irr_user_launch_fn launch, void *ctx, int value_size,
+                             int value_kind);
+/* The constructor's node_coordinates (irregular_runtime.cu:17-48):
+ * num_nodes points of num_dims (2 or 3) components of coord_size (4 = float,
+ * 8 = double) bytes, host memory, caller's order; copied.  Used to order the
+ * nodes of a handle with a user map (above); ignored otherwise. */
+IRR_API int irr_set_coordinates(irr_handle *h, const void *coords, int coord_size, int num_dims,
+                                int64_t num_nodes);
+
 /* ---------------------------------------------------------- file formats
  * The drivers' input files (host code; no GPU needed).
  * irr_read_graph: moldyn's adjacency format (moldyn/misc.c:62-146): '%'

@@ -10,10 +10,16 @@
 //    re-splits do not exist; IrregularBarrier is a stream synchronisation;
 //  * the caller's edge and coordinate arrays are never modified, and results
 //    come back in the caller's node order;
-//  * the per-edge user function is one of the library's built-ins: the map
-//    index given by IRR_COMPAT_MAP when defined, else chosen from the
-//    parameter block the driver passes (16 bytes, moldyn's struct para ->
-//    moldyn `map`; 8 bytes, miniMD's cutforcesq -> miniMD `map1`);
+//  * the per-edge user function is the application's own irregular.h,
+//    compiled by irregular/irr_user_map.cu (which the application adds to its
+//    build, as the reference compiles irregular.h into its executors) and
+//    bound by irr_compat_register_user_map; set_map_idx / set_reduce_idx pick
+//    entries of its tables.  Defining IRR_COMPAT_MAP (an enum irr_map value)
+//    instead selects one of the library's built-in laws, whose tiled kernel
+//    is the fast path.  Without either the program does not link;
+//  * the result buffer is read at reduction_elm_size bytes per node: VALUE
+//    records, or their floats widened to doubles when reduction_elm_size is
+//    twice sizeof(VALUE) (moldyn passes 3 doubles, moldyn/moldyn.cu:321);
 //  * failures print the library's message and abort (the reference exit()s).
 #ifndef IRREGULAR_IRREGULAR_RUNTIME_H_
 #define IRREGULAR_IRREGULAR_RUNTIME_H_
@@ -23,6 +29,11 @@
 #include <stdlib.h>
 
 #include "irregular_gb300.h"
+
+#ifndef IRR_COMPAT_MAP
+// irregular/irr_user_map.cu: binds the application's irregular.h tables.
+extern "C" int irr_compat_register_user_map(irr_handle *h);
+#endif
 
 typedef int64_t IRIndex;
 
@@ -53,19 +64,23 @@ public:
     {
         (void)edge_data;
         (void)edge_data_elm_size;
-        (void)node_num_dims;
-        (void)node_coordinates;
-        (void)coordinate_size;
         (void)num_procs;
         (void)num_iters;
         irr_config cfg;
         irr_config_default(&cfg);
 #ifdef IRR_COMPAT_MAP
+        (void)node_num_dims;
+        (void)node_coordinates;
+        (void)coordinate_size;
         cfg.map_idx = IRR_COMPAT_MAP;
-#else
-        cfg.map_idx = parameter_size >= 16 ? IRR_MAP_LJ_MOLDYN : IRR_MAP_LJ_MINIMD;
-#endif
         check(irr_create(&cfg, &h_), "create");
+#else
+        check(irr_create(&cfg, &h_), "create");
+        check(irr_compat_register_user_map(h_), "user map");
+        if (node_coordinates)
+            check(irr_set_coordinates(h_, node_coordinates, coordinate_size, node_num_dims, num_nodes),
+                  "coordinates");
+#endif
         check(irr_set_params(h_, parameter, parameter_size), "parameters");
         check(irr_set_edges(h_, (const int32_t *)edges, num_edges), "edges");
         check(irr_set_nodes(h_, node_data, node_data_elm_size, num_nodes), "node data");

@@ -26,6 +26,10 @@ namespace {
 constexpr bool kAutoStaged = true;
 constexpr int64_t kStagedMinReuse = 3;
 
+// User maps: largest parameter block and result record.
+constexpr int kUserParamMax = 65536;
+constexpr int kUserValueMax = 256;
+
 int fail(irr_handle* h, int code, const char* fmt, ...)
 {
     if (h) {
@@ -74,10 +78,20 @@ void free_layout(irr_handle* h)
     dfree(h->d_inst);
     dfree(h->d_items);
     h->num_items = 0;
+    dfree(h->d_rec);
+    dfree(h->d_vals);
+    dfree(h->d_iota);
+    dfree(h->d_param);
     h->inited = false;
 }
 
-bool valid_node_elm(int elm) { return elm == 12 || elm == 16 || elm == 24; }
+// Node records: positions (12/16/24 bytes) for the built-in laws; any
+// multiple of 4 bytes up to 1024 for a user map.
+bool valid_node_elm(const irr_handle* h, int elm)
+{
+    if (h->user_launch) return elm >= 4 && elm <= 1024 && (elm & 3) == 0;
+    return elm == 12 || elm == 16 || elm == 24;
+}
 
 // Law parameters from the reference's parameter block for the selected map.
 int make_law(irr_handle* h)
@@ -201,10 +215,15 @@ int ensure_raw(irr_handle* h, size_t bytes)
 int set_nodes_common(irr_handle* h, const void* src, int elm, int64_t n, cudaMemcpyKind kind)
 {
     if (!h || (!src && n > 0) || n < 0) return fail(h, IRR_ERR_ARG, "bad node data arguments");
-    if (!valid_node_elm(elm)) return fail(h, IRR_ERR_ARG, "node elm_size %d: use 12, 16 or 24", elm);
+    if (!valid_node_elm(h, elm))
+        return fail(h, IRR_ERR_ARG,
+                    h->user_launch ? "node elm_size %d: use a multiple of 4 up to 1024" : "node elm_size %d: use 12, 16 or 24",
+                    elm);
     if (n > 0x7fffffffLL) return fail(h, IRR_ERR_CAPACITY, "more than 2^31-1 nodes");
     if (h->inited && n != h->n) return fail(h, IRR_ERR_STATE, "node count changed after init (%lld -> %lld)", (long long)h->n, (long long)n);
-    if (kind == cudaMemcpyHostToDevice && h->inited && n > 0) {
+    if (h->inited && h->user_launch && elm != h->raw_elm)
+        return fail(h, IRR_ERR_STATE, "node record size changed after init (%d -> %d)", h->raw_elm, elm);
+    if (kind == cudaMemcpyHostToDevice && h->inited && n > 0 && !h->user_launch) {
         // reset_node_data from page-locked host memory: the kernel reads the
         // caller's records in order over the host link and scatters them into
         // execution order (no staging copy, no second pass)
@@ -225,8 +244,12 @@ int set_nodes_common(irr_handle* h, const void* src, int elm, int64_t n, cudaMem
     h->raw_pending = true;
     if (h->inited) {
         // reset_node_data: convert (and gather into partition order) now
-        H_CUDA(h, launch_load_nodes(h->d_raw, elm, h->part.perm, n, h->d_pos, h->stream),
-               "load node data");
+        if (h->user_launch)
+            H_CUDA(h, launch_gather_records(h->d_raw, elm, h->part.perm, n, h->d_rec, h->stream),
+                   "load node records");
+        else
+            H_CUDA(h, launch_load_nodes(h->d_raw, elm, h->part.perm, n, h->d_pos, h->stream),
+                   "load node data");
         h->raw_pending = false;
     }
     return IRR_OK;
@@ -248,7 +271,14 @@ int set_edges_common(irr_handle* h, const int32_t* src, int64_t e, cudaMemcpyKin
     if (h->inited) {
         // new edge list: the layout is rebuilt at the next init
         const int64_t n = h->n;
-        if (!h->raw_pending) {
+        if (!h->raw_pending && h->user_launch) {
+            // keep the current node records: back into the caller's order
+            int rc = ensure_raw(h, (size_t)(n > 0 ? n : 1) * h->raw_elm);
+            if (rc) return rc;
+            H_CUDA(h, launch_gather_records(h->d_rec, h->raw_elm, h->part.inv, n, h->d_raw, h->stream),
+                   "save node records");
+            h->raw_pending = true;
+        } else if (!h->raw_pending) {
             // keep the current node data: write it back in the caller's order
             int rc = ensure_raw(h, (size_t)(n > 0 ? n : 1) * 16);
             if (rc) return rc;
@@ -261,11 +291,109 @@ int set_edges_common(irr_handle* h, const int32_t* src, int64_t e, cudaMemcpyKin
     return IRR_OK;
 }
 
+// User map: positions for the partitioner (coordinates, else position-like
+// records, else none: the caller's order is kept), then the partition, the
+// node records in execution order, and the view's other arrays.
+int init_user(irr_handle* h)
+{
+    cudaStream_t s = h->stream;
+    const int64_t n = h->n, e = h->e;
+    const size_t nb = (size_t)(n > 0 ? n : 1);
+    H_CUDA(h, cudaMalloc(&h->d_pos, nb * sizeof(float4)), "allocate positions");
+    int reorder = h->cfg.reorder;
+    if (h->coord_n >= 0) {
+        if (h->coord_n != n)
+            return fail(h, IRR_ERR_STATE, "%lld coordinates for %lld nodes", (long long)h->coord_n, (long long)n);
+        H_CUDA(h, launch_coords_to_pos(h->d_coord, h->coord_size, h->coord_dims, n, h->d_pos, s), "coordinates");
+    } else if (h->raw_elm == 12 || h->raw_elm == 16 || h->raw_elm == 24) {
+        H_CUDA(h, launch_load_nodes(h->d_raw, h->raw_elm, nullptr, n, h->d_pos, s), "load node positions");
+    } else {
+        H_CUDA(h, cudaMemsetAsync(h->d_pos, 0, nb * sizeof(float4), s), "clear positions");
+        reorder = 0;
+    }
+    PartitionOut p;
+    cudaError_t pe = build_partition(h->d_pos, n, h->d_edges, e, reorder, &p, s, h->cfg.order);
+    h->part = p;
+    if (pe != cudaSuccess) {
+        free_layout(h);
+        return cuda_fail(h, pe, "build partition");
+    }
+    dfree(h->d_pos);  // the user kernel reads the records
+    H_CUDA(h, cudaMalloc(&h->d_rec, nb * h->raw_elm), "allocate node records");
+    H_CUDA(h, launch_gather_records(h->d_raw, h->raw_elm, h->part.perm, n, h->d_rec, s), "gather node records");
+    h->raw_pending = false;
+    H_CUDA(h, cudaMalloc(&h->d_vals, nb * h->value_size), "allocate results");
+    H_CUDA(h, cudaMemsetAsync(h->d_vals, 0, nb * h->value_size, s), "clear results");
+    H_CUDA(h, cudaMalloc(&h->d_iota, nb * sizeof(int32_t)), "allocate part index");
+    H_CUDA(h, launch_iota(h->d_iota, n, s), "part index");
+    H_CUDA(h, cudaMalloc(&h->d_param, h->param.size() > 0 ? h->param.size() : 16), "allocate parameters");
+    if (!h->param.empty())
+        H_CUDA(h, cudaMemcpyAsync(h->d_param, h->param.data(), h->param.size(), cudaMemcpyHostToDevice, s),
+               "copy parameters");
+    h->dev_bytes = (int64_t)nb * (h->raw_elm + h->value_size + 3 * 4) + (int64_t)h->raw_cap + 4 * (n + 1) +
+                   8 * e + (int64_t)h->coord_cap;
+    h->inited = true;
+    dfree(h->d_edges);
+    h->edges_cap = 0;
+    H_CUDA(h, cudaStreamSynchronize(s), "init");
+    return IRR_OK;
+}
+
+int step_user(irr_handle* h)
+{
+    if (h->raw_pending) {
+        H_CUDA(h, launch_gather_records(h->d_raw, h->raw_elm, h->part.perm, h->n, h->d_rec, h->stream),
+               "load node records");
+        h->raw_pending = false;
+    }
+    irr_user_view v{};
+    v.num_nodes = h->n;
+    v.row_off = h->part.row_off;
+    v.col = h->part.col;
+    v.node_data = h->d_rec;
+    v.node_elm_size = h->raw_elm;
+    v.value_size = h->value_size;
+    v.param = h->d_param;
+    v.param_size = (int)h->param.size();
+    v.map_idx = h->user_map_idx;
+    v.reduce_idx = h->user_reduce_idx;
+    v.part_index = h->d_iota;
+    v.values = h->d_vals;
+    v.status = h->d_status;
+    v.num_sms = h->sms;
+    const int rc = h->user_launch(&v, (void*)h->stream, h->user_ctx);
+    if (rc != IRR_OK) {
+        const cudaError_t ce = cudaGetLastError();
+        return fail(h, rc, "user map launch (map %d, reduce %d): %s", h->user_map_idx, h->user_reduce_idx,
+                    rc == IRR_ERR_ARG ? "table index out of range, or VALUE size differs"
+                                      : cudaGetErrorString(ce));
+    }
+    return IRR_OK;
+}
+
+// User-map results into d_out (device or page-locked host memory the device
+// addresses): value_size records, or widened doubles at 2 * value_size.
+int store_user(irr_handle* h, void* d_out, int elm_size)
+{
+    if (elm_size == h->value_size)
+        H_CUDA(h, launch_gather_records(h->d_vals, elm_size, h->part.inv, h->n, d_out, h->stream), "store results");
+    else
+        H_CUDA(h, launch_widen_records(h->d_vals, h->value_size, h->part.inv, h->n, d_out, h->stream),
+               "store results");
+    return IRR_OK;
+}
+
+bool user_result_ok(const irr_handle* h, int elm_size)
+{
+    return elm_size == h->value_size || (h->value_kind == IRR_VALUE_F32 && elm_size == 2 * h->value_size);
+}
+
 }  // namespace
 
 int irr_ensure_layout(irr_handle* h, int lanes_per_row, int block_nodes, int staged_ok)
 {
     if (!h || !h->inited || h->cfg.exec != IRR_EXEC_PARTITIONED) return IRR_ERR_STATE;
+    if (h->user_launch) return fail(h, IRR_ERR_STATE, "a handle with a user map runs its own kernel");
     DeviceGuard dev_guard(h->device);
     H_CUDA(h, cudaStreamSynchronize(h->stream), "layout");  // no launch may use the old layout
     const int64_t n = h->n, e = h->e;
@@ -433,6 +561,7 @@ int irr_destroy(irr_handle* h)
     dfree(h->d_status);
     dfree(h->d_queue);
     dfree(h->d_out);
+    dfree(h->d_coord);
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
     delete h;
     return IRR_OK;
@@ -450,6 +579,12 @@ int irr_set_stream(irr_handle* h, void* stream)
 int irr_set_map(irr_handle* h, int map_idx)
 {
     if (!h) return IRR_ERR_ARG;
+    if (h->user_launch) {
+        // an entry of the user's map table (range checked at launch)
+        if (map_idx < 0) return fail(h, IRR_ERR_ARG, "negative map index %d", map_idx);
+        h->user_map_idx = map_idx;
+        return IRR_OK;
+    }
     if (map_idx < IRR_MAP_LJ_MOLDYN || map_idx > IRR_MAP_LJ_MINIMD_PBC)
         return fail(h, IRR_ERR_ARG, "unknown map index %d", map_idx);
     h->map_idx = map_idx;
@@ -465,6 +600,11 @@ int irr_set_map(irr_handle* h, int map_idx)
 int irr_set_reduce(irr_handle* h, int reduce_idx)
 {
     if (!h) return IRR_ERR_ARG;
+    if (h->user_launch) {
+        if (reduce_idx < 0) return fail(h, IRR_ERR_ARG, "negative reduce index %d", reduce_idx);
+        h->user_reduce_idx = reduce_idx;
+        return IRR_OK;
+    }
     if (reduce_idx != IRR_REDUCE_SUM) return fail(h, IRR_ERR_ARG, "unknown reduce index %d", reduce_idx);
     h->reduce_idx = reduce_idx;
     return IRR_OK;
@@ -475,6 +615,23 @@ int irr_set_params(irr_handle* h, const void* param, int param_size)
     if (!h) return IRR_ERR_ARG;
     if (!param || param_size <= 0) return fail(h, IRR_ERR_ARG, "empty parameter block");
     DeviceGuard dev_guard(h->device);
+    if (h->user_launch) {
+        // kept as given; the user map reads it from device memory
+        if (param_size > kUserParamMax) return fail(h, IRR_ERR_CAPACITY, "parameter block above %d bytes", kUserParamMax);
+        const bool resize = h->inited && (size_t)param_size != h->param.size();
+        h->param.assign((const unsigned char*)param, (const unsigned char*)param + param_size);
+        h->have_law = true;
+        if (h->inited) {
+            if (resize) {
+                H_CUDA(h, cudaStreamSynchronize(h->stream), "parameters");
+                dfree(h->d_param);
+                H_CUDA(h, cudaMalloc(&h->d_param, h->param.size()), "allocate parameters");
+            }
+            H_CUDA(h, cudaMemcpyAsync(h->d_param, h->param.data(), h->param.size(), cudaMemcpyHostToDevice,
+                                      h->stream), "copy parameters");
+        }
+        return IRR_OK;
+    }
     std::vector<unsigned char> keep = h->param;
     h->param.assign((const unsigned char*)param, (const unsigned char*)param + param_size);
     int rc = make_law(h);
@@ -520,12 +677,15 @@ int irr_init(irr_handle* h)
     if (h->n < 0) return fail(h, IRR_ERR_STATE, "irr_init before irr_set_nodes");
     if (h->e < 0) return fail(h, IRR_ERR_STATE, "irr_init before irr_set_edges");
     if (!h->have_law) return fail(h, IRR_ERR_STATE, "irr_init before irr_set_params");
+    if (h->user_launch && h->cfg.exec != IRR_EXEC_PARTITIONED)
+        return fail(h, IRR_ERR_STATE, "a user map needs the partitioned executor");
     DeviceGuard dev_guard(h->device);
     cudaStream_t s = h->stream;
     const int64_t n = h->n, e = h->e;
     H_CUDA(h, launch_validate_edges(h->d_edges, e, n, h->d_status, s), "validate edges");
     int rc = check_status(h);
     if (rc) return rc;
+    if (h->user_launch) return init_user(h);
     const size_t nb = (size_t)(n > 0 ? n : 1) * sizeof(float4);
     H_CUDA(h, cudaMalloc(&h->d_pos, nb), "allocate positions");
     H_CUDA(h, cudaMalloc(&h->d_force, nb), "allocate results");
@@ -575,6 +735,7 @@ int irr_step(irr_handle* h)
         if (rc) return rc;
     }
     DeviceGuard dev_guard(h->device);
+    if (h->user_launch) return step_user(h);
     if (h->raw_pending) {
         H_CUDA(h, launch_load_nodes(h->d_raw, h->raw_elm, h->part.perm, h->n, h->d_pos, h->stream), "load node data");
         h->raw_pending = false;
@@ -596,6 +757,15 @@ int irr_step(irr_handle* h)
 int irr_get_result_device(irr_handle* h, void* d_out, int elm_size)
 {
     if (!h || !d_out) return fail(h, IRR_ERR_ARG, "null output");
+    if (h->user_launch) {
+        if (!user_result_ok(h, elm_size))
+            return fail(h, IRR_ERR_ARG, "result elm_size %d: the user map's records are %d bytes", elm_size, h->value_size);
+        if (!h->inited) return fail(h, IRR_ERR_STATE, "no result before irr_step");
+        if (reinterpret_cast<uintptr_t>(d_out) % (elm_size == h->value_size ? 4 : 8))
+            return fail(h, IRR_ERR_ARG, "result buffer not aligned to %d bytes", elm_size == h->value_size ? 4 : 8);
+        DeviceGuard dev_guard(h->device);
+        return store_user(h, d_out, elm_size);
+    }
     if (elm_size != 12 && elm_size != 16 && elm_size != 24) return fail(h, IRR_ERR_ARG, "result elm_size %d: use 12, 16 or 24", elm_size);
     if (!h->inited) return fail(h, IRR_ERR_STATE, "no result before irr_step");
     const uintptr_t align = elm_size == 12 ? 4 : (elm_size == 16 ? 16 : 8);
@@ -610,10 +780,11 @@ int irr_get_result_device(irr_handle* h, void* d_out, int elm_size)
 int irr_get_result(irr_handle* h, void* out, int elm_size)
 {
     if (!h || (!out && h->n > 0)) return fail(h, IRR_ERR_ARG, "null output");
-    if (elm_size != 12 && elm_size != 16 && elm_size != 24) return fail(h, IRR_ERR_ARG, "result elm_size %d: use 12, 16 or 24", elm_size);
+    if (h->user_launch ? !user_result_ok(h, elm_size) : (elm_size != 12 && elm_size != 16 && elm_size != 24))
+        return fail(h, IRR_ERR_ARG, "result elm_size %d: not a record size of this handle", elm_size);
     if (!h->inited) return fail(h, IRR_ERR_STATE, "no result before irr_step");
     DeviceGuard dev_guard(h->device);
-    if (h->n > 0) {
+    if (h->n > 0 && !h->user_launch) {
         // into page-locked host memory directly: written in order over the
         // host link, gathered from execution order on the device
         if (void* mapped = host_device_view(out)) {
@@ -666,6 +837,7 @@ int irr_get_info(const irr_handle* h, irr_info* info)
     info->stage_smem = h->shape.stage_smem;
     info->exec = h->cfg.exec;
     info->layout = h->shape.staged ? IRR_LAYOUT_STAGED : (h->sl.lanes ? IRR_LAYOUT_SLICED : IRR_LAYOUT_CSR);
+    if (h->user_launch) info->num_blocks = 0;
     info->order = h->cfg.order;
     info->num_slots = h->shape.staged ? 2 * (h->st.nwords - 32 * h->st.slices)
                                       : (h->sl.lanes ? h->sl.words : info->num_entries);
@@ -720,6 +892,56 @@ int irr_get_staged(irr_handle* h, int64_t* counts, int32_t* items, uint32_t* sli
     if (ids && st.nids > 0)
         H_CUDA(h, cudaMemcpyAsync(ids, st.ids, sizeof(int32_t) * st.nids, cudaMemcpyDeviceToHost, h->stream), "copy tables");
     H_CUDA(h, cudaStreamSynchronize(h->stream), "copy staged layout");
+    return IRR_OK;
+}
+
+int irr_set_user_map(irr_handle* h, irr_user_launch_fn launch, void* ctx, int value_size, int value_kind)
+{
+    if (!h) return IRR_ERR_ARG;
+    if (h->inited) return fail(h, IRR_ERR_STATE, "irr_set_user_map after irr_init");
+    if (launch && (value_size < 4 || value_size > kUserValueMax || (value_size & 3)))
+        return fail(h, IRR_ERR_ARG, "value_size %d: use a multiple of 4 in [4, %d]", value_size, kUserValueMax);
+    if (value_kind != IRR_VALUE_BYTES && value_kind != IRR_VALUE_F32)
+        return fail(h, IRR_ERR_ARG, "unknown value kind %d", value_kind);
+    if (h->n >= 0 && !(launch ? (h->raw_elm >= 4 && h->raw_elm <= 1024 && (h->raw_elm & 3) == 0)
+                              : (h->raw_elm == 12 || h->raw_elm == 16 || h->raw_elm == 24)))
+        return fail(h, IRR_ERR_STATE, "the node records already given (%d bytes) do not suit this map", h->raw_elm);
+    h->user_launch = launch;
+    h->user_ctx = launch ? ctx : nullptr;
+    h->value_size = launch ? value_size : 0;
+    h->value_kind = launch ? value_kind : IRR_VALUE_BYTES;
+    h->user_map_idx = h->user_reduce_idx = 0;
+    if (launch) {
+        if (h->param.size() > (size_t)kUserParamMax) return fail(h, IRR_ERR_CAPACITY, "parameter block above %d bytes", kUserParamMax);
+        h->have_law = true;  // a user map may take no parameter block
+        return IRR_OK;
+    }
+    h->have_law = false;
+    return h->param.empty() ? IRR_OK : make_law(h);
+}
+
+int irr_set_coordinates(irr_handle* h, const void* coords, int coord_size, int num_dims, int64_t num_nodes)
+{
+    if (!h) return IRR_ERR_ARG;
+    if ((!coords && num_nodes > 0) || num_nodes < 0) return fail(h, IRR_ERR_ARG, "bad coordinate arguments");
+    if (coord_size != 4 && coord_size != 8) return fail(h, IRR_ERR_ARG, "coord_size %d: use 4 or 8", coord_size);
+    if (num_dims != 2 && num_dims != 3) return fail(h, IRR_ERR_ARG, "num_dims %d: use 2 or 3", num_dims);
+    if (num_nodes > 0x7fffffffLL) return fail(h, IRR_ERR_CAPACITY, "more than 2^31-1 nodes");
+    DeviceGuard dev_guard(h->device);
+    const size_t bytes = (size_t)(num_nodes > 0 ? num_nodes : 1) * coord_size * num_dims;
+    if (bytes > h->coord_cap) {
+        H_CUDA(h, cudaStreamSynchronize(h->stream), "coordinates");
+        dfree(h->d_coord);
+        h->coord_cap = 0;
+        H_CUDA(h, cudaMalloc(&h->d_coord, bytes), "allocate coordinates");
+        h->coord_cap = bytes;
+    }
+    if (num_nodes > 0)
+        H_CUDA(h, cudaMemcpyAsync(h->d_coord, coords, (size_t)num_nodes * coord_size * num_dims,
+                                  cudaMemcpyHostToDevice, h->stream), "copy coordinates");
+    h->coord_size = coord_size;
+    h->coord_dims = num_dims;
+    h->coord_n = num_nodes;
     return IRR_OK;
 }
 

@@ -53,6 +53,23 @@ struct irr_handle {
     void* d_out = nullptr;       // result staging for host reads
     size_t out_cap = 0;
     int64_t dev_bytes = 0;
+
+    // user map (the irregular.h plugin): bound by irr_set_user_map
+    irr_user_launch_fn user_launch = nullptr;
+    void* user_ctx = nullptr;
+    int value_size = 0;
+    int value_kind = IRR_VALUE_BYTES;
+    int user_map_idx = 0;        // table entries the launch function is given
+    int user_reduce_idx = 0;
+    void* d_rec = nullptr;       // node records, execution order
+    void* d_vals = nullptr;      // result records, execution order
+    int32_t* d_iota = nullptr;   // part_index[x] = x
+    void* d_param = nullptr;     // device copy of param
+    void* d_coord = nullptr;     // irr_set_coordinates, caller's order
+    size_t coord_cap = 0;
+    int coord_size = 0;
+    int coord_dims = 0;
+    int64_t coord_n = -1;
 };
 
 // (Re)builds the handle's entry layout for G lanes per row as its config asks

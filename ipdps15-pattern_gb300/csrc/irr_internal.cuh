@@ -255,6 +255,20 @@ cudaError_t launch_store_result(const float4* force, const int32_t* inv, int64_t
 cudaError_t launch_validate_edges(const int2* edges, int64_t e, int64_t n, int* d_status,
                                   cudaStream_t s);
 
+// -- user-map records (irr_user.cu) --
+// dst record k = src record idx[k] (idx nullptr: k); elm_size a multiple of 4.
+cudaError_t launch_gather_records(const void* src, int elm_size, const int32_t* idx, int64_t n,
+                                  void* dst, cudaStream_t s);
+// Same, each float of a record widened to a double (dst records are
+// 2 * elm_size bytes).
+cudaError_t launch_widen_records(const void* src, int elm_size, const int32_t* idx, int64_t n,
+                                 void* dst, cudaStream_t s);
+// out[i] = i.
+cudaError_t launch_iota(int32_t* out, int64_t n, cudaStream_t s);
+// Points of dims (2 or 3) components of coord_size (4 or 8) bytes -> float4.
+cudaError_t launch_coords_to_pos(const void* coords, int coord_size, int dims, int64_t n, float4* dst,
+                                 cudaStream_t s);
+
 // -- partitioner (irr_partition.cu) --
 // Hilbert index of a cell on the 2^10-per-axis grid: Skilling's transform
 // (J. Skilling, "Programming the Hilbert curve", AIP Conf. Proc. 707, 2004)

@@ -140,6 +140,8 @@ _SIGS = {
     "irr_get_info": (C.c_int, [P, C.POINTER(Info)]),
     "irr_get_partition": (C.c_int, [P, P, P, P]),
     "irr_get_staged": (C.c_int, [P, P, P, P, P, P]),
+    "irr_set_user_map": (C.c_int, [P, P, P, C.c_int, C.c_int]),
+    "irr_set_coordinates": (C.c_int, [P, P, C.c_int, C.c_int, I64]),
     "irr_neighbor_build": (C.c_int, [C.c_int, P, P, C.c_int, C.c_int, I64, C.c_float, C.c_float,
                                      C.POINTER(P), C.POINTER(I64)]),
     "irr_device_free": (C.c_int, [C.c_int, P]),
@@ -345,6 +347,25 @@ class Handle:
 
     def set_map(self, idx: int):
         self._check(load().irr_set_map(self._h, int(idx)), "irr_set_map")
+
+    def set_reduce(self, idx: int):
+        self._check(load().irr_set_reduce(self._h, int(idx)), "irr_set_reduce")
+
+    def set_user_map(self, launch_fn: int, value_size: int, value_kind: int = 1, ctx: int = 0):
+        """irr_set_user_map: bind a user map's launch function (an address,
+        e.g. the irr_compat_user_launch of a library built from
+        compat/irregular/irr_user_map.cu); value_kind 1 = float records."""
+        self._check(load().irr_set_user_map(self._h, C.c_void_p(launch_fn), C.c_void_p(ctx),
+                                            int(value_size), int(value_kind)), "irr_set_user_map")
+
+    def set_coordinates(self, coords: np.ndarray):
+        """irr_set_coordinates: (n, 2|3) float32 or float64 points that order the
+        nodes of a handle with a user map."""
+        a = np.ascontiguousarray(coords)
+        if a.dtype not in (np.float32, np.float64) or a.ndim != 2:
+            raise ValueError("coordinates: an (n, dims) float32 or float64 array")
+        self._check(load().irr_set_coordinates(self._h, _ptr(a), a.dtype.itemsize, a.shape[1],
+                                               a.shape[0]), "irr_set_coordinates")
 
     def set_params(self, blob: np.ndarray):
         blob = np.ascontiguousarray(blob)

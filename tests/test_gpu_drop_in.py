@@ -1,6 +1,7 @@
 """The compat IrregularRuntime class at run time (GPU): a C++ driver making
-moldyn's call sequence, built here against the compat headers, must reproduce
-the reference's own result (golden fixture) within the FP32 tolerance."""
+moldyn's call sequence, built here against the compat headers with the
+built-in moldyn law (IRR_COMPAT_MAP), must reproduce the reference's own
+result (golden fixture) within the FP32 tolerance."""
 import os
 import subprocess
 
@@ -16,7 +17,10 @@ pytestmark = pytest.mark.gpu
 def build_driver(tmp_path):
     exe = str(tmp_path / "moldyn_like")
     src = os.path.join(ROOT, "tests", "drop_in", "moldyn_like.cpp")
-    r = subprocess.run(["g++", "-std=c++17", "-O2", "-I", os.path.join(PKG, "compat"), "-I",
+    # the library's built-in moldyn law (the fast path); test_gpu_plugin.py
+    # runs the same driver with the map from an application table
+    r = subprocess.run(["g++", "-std=c++17", "-O2", "-DIRR_COMPAT_MAP=IRR_MAP_LJ_MOLDYN", "-I",
+                        os.path.join(PKG, "compat"), "-I",
                         os.path.join(ROOT, "include"), src, "-o", exe, "-L", PKG,
                         "-lirregular_gb300", f"-Wl,-rpath,{PKG}"], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
