@@ -32,8 +32,10 @@ Our arm prints one JSON line with
                same instances run one by one, and the served stream (p50 /
                p99 latency, throughput against serial execution, capacity).
 `--impl reference` times that CPU executor alone (rank 0; other ranks exit).
-With N > 1 (torchrun) every rank reduces its own replica of the workload
-(weak scaling, no collective on the data path); times are maxed over ranks.
+With N > 1 (torchrun) the workload is split into N shards of the node order,
+one per rank, with the halo positions exchanged over NCCL every step (strong
+scaling, `--mode sharded`, the default), or every rank reduces its own
+replica (`--mode replicas`, weak scaling); times are maxed over ranks.
 """
 from __future__ import annotations
 
@@ -484,6 +486,127 @@ def run_ours(args, rank, world, local):
     return 0
 
 
+def run_sharded(args, rank, world, local):
+    """Strong scaling: the one workload split into `world` shards of the
+    partition's execution order (sharding.plan: equal entry counts), one per
+    rank, each reduced by a shard handle (irr_set_shard) after a per-step halo
+    exchange of float4 positions over NCCL point-to-point (sharding.
+    HaloExchange) -- the reference's per-rank view and its halo exchange
+    (moldyn/irregular/partition_view.cpp:44-282, 285-435).  value = all edges
+    / the slowest rank's time for the step (exchange + reduction)."""
+    import torch
+
+    import irregular_gb300 as irr
+    import sharding
+
+    torch.cuda.set_device(local)
+    dev = local
+    stream = torch.cuda.Stream(device=dev)
+    pos, side = positions(args.nodes)
+    n = pos.shape[0]
+    edges = irr.neighbor_build(pos, float(side), CUTOFF * CUTOFF, device=dev,
+                               stream=stream.cuda_stream)
+    E = edges.count
+    params = irr.moldyn_params(float(side), CUTOFF)
+    # the whole problem's partition (every rank computes the same one)
+    hw = irr.Handle(irr.default_config(device=dev, map_idx=irr.IRR_MAP_LJ_MOLDYN,
+                                       exec=irr.IRR_EXEC_PARTITIONED))
+    hw.set_stream(stream.cuda_stream)
+    hw.set_params(params)
+    hw.set_edges(edges)
+    hw.set_nodes(pos, 12)
+    hw.init()
+    perm, row_off, col = hw.partition()
+    hw.close()
+    edges.close()
+    shards = sharding.plan(row_off, col, world)
+    lp = sharding.local_problem(shards[rank], row_off, col)
+    pos4 = np.zeros((n, 4), np.float32)
+    pos4[:, :3] = pos[perm]
+    del pos
+    n_local = lp.nodes.shape[0]
+    loc_np = np.ascontiguousarray(pos4[lp.nodes])
+    h = irr.Handle(irr.default_config(device=dev, map_idx=irr.IRR_MAP_LJ_MOLDYN,
+                                      exec=irr.IRR_EXEC_PARTITIONED, reorder=0,
+                                      layout=LAYOUTS[args.layout]))
+    h.set_stream(stream.cuda_stream)
+    h.set_params(params)
+    h.set_shard(lp.own_lo, lp.own_hi)
+    h.set_edges(lp.edges)
+    h.set_nodes(loc_np, 16)
+    h.init()
+    loc = torch.from_numpy(loc_np).to(f"cuda:{dev}")
+    hx = sharding.HaloExchange(lp, f"cuda:{dev}")
+    below = loc[:lp.own_lo]
+    above = loc[lp.own_hi:]
+
+    def one_step():
+        hx.run(loc)
+        if lp.own_lo > 0:
+            h.set_nodes_range(below, 0, 16)
+        if lp.own_hi < n_local:
+            h.set_nodes_range(above, lp.own_hi, 16)
+        h.step()
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            one_step()
+        h.sync()
+        barrier(world)
+        torch.cuda.synchronize()
+        clocks = ClockSampler(dev)
+        clocks.start()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            one_step()
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        clk = clocks.stop()
+        h.sync()
+    barrier(world)
+    ms = max_over_ranks(ms, world)
+    value = E * args.steps / (ms / 1e3)
+    # force error of this rank's owned rows on a seeded sample (FP64 checker)
+    err = None
+    if rank == 0:
+        f_own = h.get_result(elm_size=12)
+        own = np.arange(lp.lo, lp.hi)
+        smp = np.sort(np.random.Generator(np.random.PCG64(SEED + 3)).choice(
+            own, min(own.shape[0], FORCE_SAMPLE), replace=False))
+        rows = np.repeat(smp, (row_off[smp + 1] - row_off[smp]).astype(np.int64))
+        cols = np.concatenate([col[row_off[r]:row_off[r + 1]] for r in smp])
+        insmp = np.zeros(n, bool)
+        insmp[smp] = True
+        keep = ~insmp[cols] | (rows < cols)  # a pair of two sampled rows once
+        inc = np.stack([rows[keep], cols[keep]], axis=1)
+        g, sabs, sinf = fp64_forces(pos4[:, :3], inc, float(side), CUTOFF)
+        err = force_err(f_own[smp - lp.lo], g[smp], sabs[smp], sinf[smp])
+    halo = max_over_ranks(float(n_local - (lp.hi - lp.lo)), world)
+    h.close()
+    line = {
+        "metric": METRIC, "value": value, "unit": "edges/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded uniform-random positions; edge list built on the GPU)",
+        "config": {"workload": workload_name(n), "nodes": n, "edges": E,
+                   "exec": "sharded: equal-entry ranges of the Hilbert order, one shard handle "
+                           "per rank, halo positions exchanged every step (NCCL send/recv)",
+                   "max_halo_nodes_per_rank": int(halo),
+                   "l2": "inputs larger than L2 (1.07 GB entry stream read every step)",
+                   "parallelism": f"shards x{world}"},
+        "clocks": clk,
+        "gpu_launches": args.steps,
+    }
+    if err is not None:
+        line["force_err"] = err
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_batched(args):
     """Config 4: 512 instances, sizes log-uniform in [1,024, 262,144] atoms, each
     uniform-random in its own periodic box at density 0.8442, cutoff 2.5; one
@@ -729,6 +852,11 @@ def main():
                     help="entry layout of the timed partitioned handle (irr_config.layout)")
     ap.add_argument("--capacity", type=int, default=1,
                     help="1: the served leg also sweeps the arrival rate for its capacity")
+    ap.add_argument("--mode", choices=["auto", "replicas", "sharded"], default="auto",
+                    help="N > 1: 'sharded' (default) splits the one workload across the ranks "
+                         "with a halo exchange per step (strong scaling); 'replicas' runs one "
+                         "workload per rank (weak scaling).  N = 1: 'sharded' runs the shard "
+                         "path with one shard")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -741,7 +869,8 @@ def main():
         print(json.dumps(leg), flush=True)
         return 0
     rank, world, local = dist_init(args)
-    rc = run_ours(args, rank, world, local)
+    sharded = args.mode == "sharded" or (args.mode == "auto" and world > 1)
+    rc = (run_sharded if sharded else run_ours)(args, rank, world, local)
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()

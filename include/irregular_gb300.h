@@ -166,6 +166,8 @@ typedef struct irr_info {
     int32_t layout;          /* enum irr_layout in use (CSR or SLICED)              */
     int32_t order;           /* enum irr_order of the node order                    */
     int64_t num_slots;       /* entry slots stored: num_entries plus padding        */
+    int64_t own_lo;          /* rows reduced: caller ids [own_lo, own_hi)           */
+    int64_t own_hi;          /* (irr_set_shard; else [0, num_nodes))               */
 } irr_info;
 
 IRR_API void irr_config_default(irr_config *cfg);
@@ -321,6 +323,31 @@ enum irr_value_kind {
  * 2 * value_size-byte doubles).  launch == NULL unbinds (before irr_init). */
 IRR_API int irr_set_user_map(irr_handle *h, irr_user_launch_fn launch, void *ctx, int value_size,
                              int value_kind);
+/* ----------------------------------------------------------------- shards
+ * A handle reduces one shard of a larger problem: the reference's per-rank
+ * view (moldyn/irregular/partition_view.cpp:44-282), in which a rank owns a
+ * range of nodes, keeps every edge that touches one of them and receives the
+ * positions of the remote endpoints (its halo) before each step (:285-435).
+ * Here the shard's nodes are given to the handle as one node array -- owned
+ * and halo nodes, in any order -- with the edges that touch an owned node;
+ * irr_set_shard (before irr_init) names the owned nodes as the caller-id range
+ * [own_lo, own_hi).  Rows of other nodes get no entries, so the step reduces
+ * owned rows only, each over all of its edges; irr_get_result and
+ * irr_get_result_device return own_hi - own_lo records (ids own_lo ...).
+ * With reorder = 0 and the shard's nodes in the order of the whole problem's
+ * execution order, every owned row holds the same neighbours in the same
+ * order as in a handle over the whole problem, and with the CSR or sliced
+ * layout its result is the same bit for bit. */
+IRR_API int irr_set_shard(irr_handle *h, int64_t own_lo, int64_t own_hi);
+/* Replaces node records [first, first + count) (caller ids) -- a shard's
+ * halo before each step, or any range -- from host memory (page-locked memory
+ * on a 16-byte boundary is read in place, as irr_set_nodes reads it) or, with
+ * _device, from device memory; elm_size as irr_set_nodes gave. */
+IRR_API int irr_set_nodes_range(irr_handle *h, const void *node_data, int elm_size, int64_t first,
+                                int64_t count);
+IRR_API int irr_set_nodes_range_device(irr_handle *h, const void *d_node_data, int elm_size,
+                                       int64_t first, int64_t count);
+
 /* The constructor's node_coordinates (irregular_runtime.cu:17-48):
  * num_nodes points of num_dims (2 or 3) components of coord_size (4 = float,
  * 8 = double) bytes, host memory, caller's order; copied.  Used to order the

@@ -291,6 +291,28 @@ int set_edges_common(irr_handle* h, const int32_t* src, int64_t e, cudaMemcpyKin
     return IRR_OK;
 }
 
+// irr_set_shard: rows outside [own_lo, own_hi) (caller ids) lose their
+// entries; h->m = the entries left.
+int apply_shard(irr_handle* h)
+{
+    if (h->own_hi < 0) {
+        h->m = 2 * h->e;
+        return IRR_OK;
+    }
+    if (h->own_lo < 0 || h->own_lo > h->own_hi || h->own_hi > h->n)
+        return fail(h, IRR_ERR_STATE, "shard rows [%lld, %lld) outside the %lld nodes", (long long)h->own_lo,
+                    (long long)h->own_hi, (long long)h->n);
+    H_CUDA(h, keep_rows(&h->part, h->n, h->own_lo, h->own_hi, &h->m, h->stream), "shard rows");
+    return IRR_OK;
+}
+
+// Rows whose results a read returns: [lo, lo + count) of the caller's ids.
+void result_rows(const irr_handle* h, int64_t* lo, int64_t* count)
+{
+    *lo = h->own_hi >= 0 ? h->own_lo : 0;
+    *count = h->own_hi >= 0 ? h->own_hi - h->own_lo : h->n;
+}
+
 // User map: positions for the partitioner (coordinates, else position-like
 // records, else none: the caller's order is kept), then the partition, the
 // node records in execution order, and the view's other arrays.
@@ -318,6 +340,11 @@ int init_user(irr_handle* h)
         free_layout(h);
         return cuda_fail(h, pe, "build partition");
     }
+    int rc = apply_shard(h);
+    if (rc) {
+        free_layout(h);
+        return rc;
+    }
     dfree(h->d_pos);  // the user kernel reads the records
     H_CUDA(h, cudaMalloc(&h->d_rec, nb * h->raw_elm), "allocate node records");
     H_CUDA(h, launch_gather_records(h->d_raw, h->raw_elm, h->part.perm, n, h->d_rec, s), "gather node records");
@@ -331,7 +358,7 @@ int init_user(irr_handle* h)
         H_CUDA(h, cudaMemcpyAsync(h->d_param, h->param.data(), h->param.size(), cudaMemcpyHostToDevice, s),
                "copy parameters");
     h->dev_bytes = (int64_t)nb * (h->raw_elm + h->value_size + 3 * 4) + (int64_t)h->raw_cap + 4 * (n + 1) +
-                   8 * e + (int64_t)h->coord_cap;
+                   4 * h->m + (int64_t)h->coord_cap;
     h->inited = true;
     dfree(h->d_edges);
     h->edges_cap = 0;
@@ -375,10 +402,13 @@ int step_user(irr_handle* h)
 // addresses): value_size records, or widened doubles at 2 * value_size.
 int store_user(irr_handle* h, void* d_out, int elm_size)
 {
+    int64_t lo, count;
+    result_rows(h, &lo, &count);
     if (elm_size == h->value_size)
-        H_CUDA(h, launch_gather_records(h->d_vals, elm_size, h->part.inv, h->n, d_out, h->stream), "store results");
+        H_CUDA(h, launch_gather_records(h->d_vals, elm_size, h->part.inv + lo, count, d_out, h->stream),
+               "store results");
     else
-        H_CUDA(h, launch_widen_records(h->d_vals, h->value_size, h->part.inv, h->n, d_out, h->stream),
+        H_CUDA(h, launch_widen_records(h->d_vals, h->value_size, h->part.inv + lo, count, d_out, h->stream),
                "store results");
     return IRR_OK;
 }
@@ -419,7 +449,7 @@ int irr_ensure_layout(irr_handle* h, int lanes_per_row, int block_nodes, int sta
                                    : cuda_fail(h, se, "build staged layout");
                 }
             }
-            if (want == IRR_LAYOUT_AUTO && h->st.words && 2 * e < kStagedMinReuse * h->st.nids)
+            if (want == IRR_LAYOUT_AUTO && h->st.words && h->m < kStagedMinReuse * h->st.nids)
                 free_staged(&h->st);  // too little reuse to pay for staging
             staged = h->st.words != nullptr || (n == 0 && want == IRR_LAYOUT_STAGED);
         } else if (want == IRR_LAYOUT_STAGED) {
@@ -442,7 +472,7 @@ int irr_ensure_layout(irr_handle* h, int lanes_per_row, int block_nodes, int sta
                     return se == cudaErrorInvalidValue
                                ? fail(h, IRR_ERR_CAPACITY, "sliced layout above 2^32 words")
                                : cuda_fail(h, se, "build sliced layout");
-            } else if (want != IRR_LAYOUT_SLICED && !sliced_pays(h->sl, 2 * e)) {
+            } else if (want != IRR_LAYOUT_SLICED && !sliced_pays(h->sl, h->m)) {
                 free_sliced(&h->sl);
             }
         }
@@ -452,7 +482,7 @@ int irr_ensure_layout(irr_handle* h, int lanes_per_row, int block_nodes, int sta
     rc = upload_items(h);
     if (rc) return rc;
     h->dev_bytes = 2 * (int64_t)(n > 0 ? n : 1) * (int64_t)sizeof(float4) + (int64_t)h->raw_cap +
-                   (int64_t)(2 * n + n + 1) * 4 + 2 * e * 4 +
+                   (int64_t)(2 * n + n + 1) * 4 + h->m * 4 +
                    (h->sl.lanes ? 4 * (h->sl.words + h->sl.slices + 1) : 0) +
                    (h->shape.staged ? 4 * (h->st.nwords + h->st.nids + h->st.slices + 1) : 0);
     return IRR_OK;
@@ -679,6 +709,8 @@ int irr_init(irr_handle* h)
     if (!h->have_law) return fail(h, IRR_ERR_STATE, "irr_init before irr_set_params");
     if (h->user_launch && h->cfg.exec != IRR_EXEC_PARTITIONED)
         return fail(h, IRR_ERR_STATE, "a user map needs the partitioned executor");
+    if (h->own_hi >= 0 && h->cfg.exec != IRR_EXEC_PARTITIONED)
+        return fail(h, IRR_ERR_STATE, "a shard needs the partitioned executor");
     DeviceGuard dev_guard(h->device);
     cudaStream_t s = h->stream;
     const int64_t n = h->n, e = h->e;
@@ -707,6 +739,11 @@ int irr_init(irr_handle* h)
     if (pe != cudaSuccess) {
         free_layout(h);
         return cuda_fail(h, pe, "build partition");
+    }
+    rc = apply_shard(h);
+    if (rc) {
+        free_layout(h);
+        return rc;
     }
     H_CUDA(h, launch_load_nodes(h->d_raw, h->raw_elm, h->part.perm, n, h->d_pos, s), "gather node data");
     h->raw_pending = false;
@@ -773,7 +810,10 @@ int irr_get_result_device(irr_handle* h, void* d_out, int elm_size)
         return fail(h, IRR_ERR_ARG, "result buffer not aligned to %d bytes for %d-byte records",
                     (int)align, elm_size);
     DeviceGuard dev_guard(h->device);
-    H_CUDA(h, launch_store_result(h->d_force, h->part.inv, h->n, elm_size, d_out, h->stream), "store result");
+    int64_t lo, count;
+    result_rows(h, &lo, &count);
+    H_CUDA(h, launch_store_result(h->d_force, h->part.inv ? h->part.inv + lo : nullptr, count, elm_size, d_out,
+                                  h->stream), "store result");
     return IRR_OK;
 }
 
@@ -784,16 +824,19 @@ int irr_get_result(irr_handle* h, void* out, int elm_size)
         return fail(h, IRR_ERR_ARG, "result elm_size %d: not a record size of this handle", elm_size);
     if (!h->inited) return fail(h, IRR_ERR_STATE, "no result before irr_step");
     DeviceGuard dev_guard(h->device);
-    if (h->n > 0 && !h->user_launch) {
+    int64_t lo, count;
+    result_rows(h, &lo, &count);
+    if (count > 0 && !h->user_launch) {
         // into page-locked host memory directly: written in order over the
         // host link, gathered from execution order on the device
         if (void* mapped = host_device_view(out)) {
-            H_CUDA(h, launch_store_result(h->d_force, h->part.inv, h->n, elm_size, mapped, h->stream),
+            H_CUDA(h, launch_store_result(h->d_force, h->part.inv ? h->part.inv + lo : nullptr, count, elm_size,
+                                          mapped, h->stream),
                    "store result");
             return check_status(h);
         }
     }
-    const size_t bytes = (size_t)(h->n > 0 ? h->n : 1) * elm_size;
+    const size_t bytes = (size_t)(count > 0 ? count : 1) * elm_size;
     if (bytes > h->out_cap) {
         dfree(h->d_out);
         h->out_cap = 0;
@@ -802,8 +845,8 @@ int irr_get_result(irr_handle* h, void* out, int elm_size)
     }
     int rc = irr_get_result_device(h, h->d_out, elm_size);
     if (rc) return rc;
-    if (h->n > 0)
-        H_CUDA(h, cudaMemcpyAsync(out, h->d_out, (size_t)h->n * elm_size, cudaMemcpyDeviceToHost, h->stream), "copy result");
+    if (count > 0)
+        H_CUDA(h, cudaMemcpyAsync(out, h->d_out, (size_t)count * elm_size, cudaMemcpyDeviceToHost, h->stream), "copy result");
     return check_status(h);
 }
 
@@ -829,7 +872,10 @@ int irr_get_info(const irr_handle* h, irr_info* info)
     memset(info, 0, sizeof(*info));
     info->num_nodes = h->n;
     info->num_edges = h->e;
-    info->num_entries = h->cfg.exec == IRR_EXEC_PARTITIONED ? 2 * (h->e > 0 ? h->e : 0) : (h->e > 0 ? h->e : 0);
+    info->num_entries = h->cfg.exec == IRR_EXEC_PARTITIONED ? (h->inited ? h->m : 2 * (h->e > 0 ? h->e : 0))
+                                                            : (h->e > 0 ? h->e : 0);
+    info->own_lo = h->own_hi >= 0 ? h->own_lo : 0;
+    info->own_hi = h->own_hi >= 0 ? h->own_hi : h->n;
     info->num_blocks = h->num_items;
     info->device_bytes = h->dev_bytes;
     info->block_nodes = h->shape.block_nodes;
@@ -850,7 +896,7 @@ int irr_get_partition(irr_handle* h, int32_t* perm, int64_t* row_off, int32_t* c
     if (h->cfg.exec != IRR_EXEC_PARTITIONED) return fail(h, IRR_ERR_STATE, "handle is not partitioned");
     if (!h->inited) return fail(h, IRR_ERR_STATE, "no partition before irr_init");
     DeviceGuard dev_guard(h->device);
-    const int64_t n = h->n, m = 2 * h->e;
+    const int64_t n = h->n, m = h->m;
     if (perm && n > 0)
         H_CUDA(h, cudaMemcpyAsync(perm, h->part.perm, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, h->stream), "copy perm");
     std::vector<uint32_t> ro;
@@ -918,6 +964,75 @@ int irr_set_user_map(irr_handle* h, irr_user_launch_fn launch, void* ctx, int va
     }
     h->have_law = false;
     return h->param.empty() ? IRR_OK : make_law(h);
+}
+
+int irr_set_shard(irr_handle* h, int64_t own_lo, int64_t own_hi)
+{
+    if (!h) return IRR_ERR_ARG;
+    if (h->inited) return fail(h, IRR_ERR_STATE, "irr_set_shard after irr_init");
+    if (own_lo < 0 || own_hi < own_lo || own_hi > 0x7fffffffLL)
+        return fail(h, IRR_ERR_ARG, "shard rows [%lld, %lld)", (long long)own_lo, (long long)own_hi);
+    h->own_lo = own_lo;
+    h->own_hi = own_hi;
+    return IRR_OK;
+}
+
+namespace {
+
+int set_nodes_range_common(irr_handle* h, const void* src, int elm, int64_t first, int64_t count,
+                           cudaMemcpyKind kind)
+{
+    if (!h || (!src && count > 0) || first < 0 || count < 0) return fail(h, IRR_ERR_ARG, "bad node range arguments");
+    if (h->n < 0) return fail(h, IRR_ERR_STATE, "irr_set_nodes_range before irr_set_nodes");
+    if (first + count > h->n)
+        return fail(h, IRR_ERR_ARG, "node range [%lld, %lld) outside %lld nodes", (long long)first,
+                    (long long)(first + count), (long long)h->n);
+    if (count == 0) return IRR_OK;
+    if (!h->inited || h->raw_pending || h->user_launch) {
+        // the records wait in d_raw, in the caller's order: patch them there
+        if (elm != h->raw_elm)
+            return fail(h, IRR_ERR_STATE, "record size %d differs from the node data's %d", elm, h->raw_elm);
+        if (h->inited && !h->raw_pending) {
+            // user map after init: d_raw is stale, so bring it up to date first
+            H_CUDA(h, launch_gather_records(h->d_rec, h->raw_elm, h->part.inv, h->n, h->d_raw, h->stream),
+                   "save node records");
+        }
+        H_CUDA(h, cudaMemcpyAsync(static_cast<char*>(h->d_raw) + (size_t)first * elm, src, (size_t)count * elm,
+                                  kind, h->stream), "copy node range");
+        h->raw_pending = true;
+        return IRR_OK;
+    }
+    if (!valid_node_elm(h, elm)) return fail(h, IRR_ERR_ARG, "node elm_size %d: use 12, 16 or 24", elm);
+    const void* rec = src;
+    if (kind == cudaMemcpyHostToDevice) {
+        rec = host_device_view(src);
+        if (!rec) {
+            int rc = ensure_raw(h, (size_t)h->n * elm);
+            if (rc) return rc;
+            H_CUDA(h, cudaMemcpyAsync(h->d_raw, src, (size_t)count * elm, kind, h->stream), "copy node range");
+            rec = h->d_raw;
+        }
+    }
+    // records [first, first + count) in the caller's order -> execution order
+    H_CUDA(h, launch_load_nodes_scatter(rec, elm, h->part.inv + first, count, h->d_pos, h->stream),
+           "load node range");
+    return IRR_OK;
+}
+
+}  // namespace
+
+int irr_set_nodes_range(irr_handle* h, const void* node_data, int elm_size, int64_t first, int64_t count)
+{
+    if (!h) return IRR_ERR_ARG;
+    DeviceGuard dev_guard(h->device);
+    return set_nodes_range_common(h, node_data, elm_size, first, count, cudaMemcpyHostToDevice);
+}
+
+int irr_set_nodes_range_device(irr_handle* h, const void* d_node_data, int elm_size, int64_t first, int64_t count)
+{
+    if (!h) return IRR_ERR_ARG;
+    DeviceGuard dev_guard(h->device);
+    return set_nodes_range_common(h, d_node_data, elm_size, first, count, cudaMemcpyDeviceToDevice);
 }
 
 int irr_set_coordinates(irr_handle* h, const void* coords, int coord_size, int num_dims, int64_t num_nodes)

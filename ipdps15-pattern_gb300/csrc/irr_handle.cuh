@@ -28,6 +28,9 @@ struct irr_handle {
 
     int64_t n = -1;
     int64_t e = -1;
+    int64_t m = 0;               // directed entries held (2e, fewer for a shard)
+    int64_t own_lo = 0;          // irr_set_shard: rows reduced and results read,
+    int64_t own_hi = -1;         // caller ids [own_lo, own_hi); -1 = all
     void* d_raw = nullptr;       // node records as the caller passed them
     size_t raw_cap = 0;
     int raw_elm = 0;

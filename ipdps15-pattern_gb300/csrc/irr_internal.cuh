@@ -321,6 +321,9 @@ cudaError_t bbox_frame(const float4* pos, int64_t n, float lo[3], float scale[3]
 // curve: 0 = Hilbert (IRR_ORDER_HILBERT), 1 = Morton.
 cudaError_t build_partition(const float4* pos_user, int64_t n, const int2* edges, int64_t e,
                             int reorder, PartitionOut* out, cudaStream_t s, int curve = 0);
+// A shard's partition: rows whose caller id is outside [lo, hi) lose their
+// entries (row_off and col rebuilt, order kept); *m_out = entries left.
+cudaError_t keep_rows(PartitionOut* p, int64_t n, int64_t lo, int64_t hi, int64_t* m_out, cudaStream_t s);
 // Half neighbour list (irr_neighbor.cu); *d_edges is cudaMalloc'd, or, with
 // stream_ordered, cudaMallocAsync'd on s (free it with cudaFreeAsync).
 // sort_rows == false returns the same pairs (i < j) in no particular order,

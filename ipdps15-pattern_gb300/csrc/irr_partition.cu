@@ -868,6 +868,62 @@ cudaError_t build_partition(const float4* pos_user, int64_t n, const int2* edges
     return cudaSuccess;
 }
 
+namespace {
+
+// Row r keeps its entries when its caller id perm[r] is in [lo, hi).
+__global__ void kept_degree_kernel(const int32_t* perm, const uint32_t* row_off, int64_t n, int64_t lo,
+                                   int64_t hi, uint32_t* deg)
+{
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n;
+         r += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t id = perm[r];
+        deg[r] = (id >= lo && id < hi) ? row_off[r + 1] - row_off[r] : 0u;
+    }
+}
+
+// One warp per row: a kept row's entries, in order, to its new offset.
+__global__ void copy_kept_rows_kernel(const uint32_t* old_off, const int32_t* old_col,
+                                      const uint32_t* new_off, int64_t n, int32_t* new_col)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n; r += warps) {
+        const uint32_t len = new_off[r + 1] - new_off[r];
+        const uint32_t src = old_off[r], dst = new_off[r];
+        for (uint32_t k = lane; k < len; k += 32) new_col[dst + k] = old_col[src + k];
+    }
+}
+
+}  // namespace
+
+cudaError_t keep_rows(PartitionOut* p, int64_t n, int64_t lo, int64_t hi, int64_t* m_out, cudaStream_t s)
+{
+    uint32_t* new_off = nullptr;
+    int32_t* new_col = nullptr;
+    IRR_CUDA_TRY(alloc_async(&new_off, n + 1, s));
+    IRR_CUDA_TRY(cudaMemsetAsync(new_off, 0, sizeof(uint32_t) * (size_t)(n + 1), s));
+    if (n > 0) {
+        kept_degree_kernel<<<grid_for(n), 256, 0, s>>>(p->perm, p->row_off, n, lo, hi, new_off);
+        IRR_CUDA_TRY(cudaGetLastError());
+    }
+    IRR_CUDA_TRY(scan_exclusive_u32(new_off, new_off, n + 1, nullptr, s));
+    uint32_t m = 0;
+    IRR_CUDA_TRY(cudaMemcpyAsync(&m, new_off + n, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    IRR_CUDA_TRY(cudaStreamSynchronize(s));
+    IRR_CUDA_TRY(alloc_async(&new_col, (int64_t)m + kColPad, s));
+    IRR_CUDA_TRY(cudaMemsetAsync(new_col + m, 0, sizeof(int32_t) * kColPad, s));
+    if (n > 0) {
+        copy_kept_rows_kernel<<<grid_for(32 * n), 256, 0, s>>>(p->row_off, p->col, new_off, n, new_col);
+        IRR_CUDA_TRY(cudaGetLastError());
+    }
+    IRR_CUDA_TRY(cudaFreeAsync(p->row_off, s));
+    IRR_CUDA_TRY(cudaFreeAsync(p->col, s));
+    p->row_off = new_off;
+    p->col = new_col;
+    *m_out = (int64_t)m;
+    return cudaSuccess;
+}
+
 cudaError_t build_sliced(const uint32_t* row_off, const int32_t* col, int64_t n, int G,
                          Sliced* sl, cudaStream_t s)
 {

@@ -62,7 +62,8 @@ class Info(C.Structure):
                 ("num_blocks", C.c_int64), ("device_bytes", C.c_int64),
                 ("block_nodes", C.c_int32), ("lanes_per_row", C.c_int32),
                 ("stage_smem", C.c_int32), ("exec", C.c_int32), ("layout", C.c_int32),
-                ("order", C.c_int32), ("num_slots", C.c_int64)]
+                ("order", C.c_int32), ("num_slots", C.c_int64), ("own_lo", C.c_int64),
+                ("own_hi", C.c_int64)]
 
 
 class MDConfig(C.Structure):
@@ -142,6 +143,9 @@ _SIGS = {
     "irr_get_staged": (C.c_int, [P, P, P, P, P, P]),
     "irr_set_user_map": (C.c_int, [P, P, P, C.c_int, C.c_int]),
     "irr_set_coordinates": (C.c_int, [P, P, C.c_int, C.c_int, I64]),
+    "irr_set_shard": (C.c_int, [P, I64, I64]),
+    "irr_set_nodes_range": (C.c_int, [P, P, C.c_int, I64, I64]),
+    "irr_set_nodes_range_device": (C.c_int, [P, P, C.c_int, I64, I64]),
     "irr_neighbor_build": (C.c_int, [C.c_int, P, P, C.c_int, C.c_int, I64, C.c_float, C.c_float,
                                      C.POINTER(P), C.POINTER(I64)]),
     "irr_device_free": (C.c_int, [C.c_int, P]),
@@ -414,9 +418,26 @@ class Handle:
         self._check(load().irr_set_wait_limit(self._h, int(limit_us), int(withhold_once)),
                     "irr_set_wait_limit")
 
+    def set_shard(self, own_lo: int, own_hi: int):
+        """irr_set_shard: reduce (and return) only rows [own_lo, own_hi)."""
+        self._check(load().irr_set_shard(self._h, int(own_lo), int(own_hi)), "irr_set_shard")
+
+    def set_nodes_range(self, nodes, first: int, elm_size: Optional[int] = None):
+        """irr_set_nodes_range[_device]: replace node records [first, first + len)."""
+        if hasattr(nodes, "data_ptr"):
+            elm = elm_size or nodes.element_size() * nodes.shape[-1]
+            cnt = nodes.numel() * nodes.element_size() // elm
+            self._check(load().irr_set_nodes_range_device(self._h, _ptr(nodes), elm, int(first), cnt),
+                        "irr_set_nodes_range_device")
+            return
+        a = np.ascontiguousarray(nodes)
+        elm = elm_size or a.dtype.itemsize * (a.shape[-1] if a.ndim > 1 else 1)
+        self._check(load().irr_set_nodes_range(self._h, _ptr(a), elm, int(first), a.nbytes // elm),
+                    "irr_set_nodes_range")
+
     def get_result(self, out: Optional[np.ndarray] = None, elm_size: int = 12) -> np.ndarray:
         info = self.info()
-        n = info.num_nodes
+        n = info.own_hi - info.own_lo
         if out is None:
             dt = np.float64 if elm_size == 24 else np.float32
             out = np.empty((n, elm_size // np.dtype(dt).itemsize), dt)

@@ -1,9 +1,13 @@
 """The multi-GPU sharding plan, exercised by world_size-2 gloo ranks on CPU.
 
-Each rank owns a contiguous range of the partition's rows, receives its halo
-positions from the other rank (point-to-point, the all-to-all-v of the plan),
-and reduces its own rows with the FP64 law; rank 0 gathers the rows.  The
-union must equal the single-process reduction of the whole edge list.
+Each rank builds the local problem a shard handle reduces (sharding.
+local_problem: its nodes in the whole problem's execution order, its owned
+range, the pairs touching an owned node), receives its halo positions from
+the other rank by the plan's exchange lists (point-to-point, the
+all-to-all-v of the plan), and reduces its owned rows with the FP64 law;
+rank 0 gathers the rows.  The union must equal the single-process reduction
+of the whole edge list bit for bit.  tests/test_gpu_shard.py runs the same
+local problems through shard handles on the GPU.
 """
 import os
 import socket
@@ -44,29 +48,61 @@ def partition_of(case):
     return perm, row_off, col
 
 
+def lj_owned_rows(pos_local, lp, side, rc2):
+    """The owned rows of a local problem (sharding.local_rows), FP64."""
+    row_off, col = sharding_mod().local_rows(lp)
+    n_own = lp.own_hi - lp.own_lo
+    f = np.zeros((n_own, 3))
+    for i in range(n_own):
+        js = col[row_off[i]:row_off[i + 1]]
+        if js.size == 0:
+            continue
+        d = pos_local[lp.own_lo + i] - pos_local[js]
+        d = np.where(d < -0.5 * side, d + side, d)
+        d = np.where(d > 0.5 * side, d - side, d)
+        rd = (d * d).sum(axis=1)
+        ok = rd < rc2
+        r = 1.0 / rd[ok]
+        s = r ** 7 - 0.5 * r ** 4
+        f[i] = (d[ok] * s[:, None]).sum(axis=0)
+    return f
+
+
+def sharding_mod():
+    import sharding
+    return sharding
+
+
 def worker(rank, world, port, name, out_path):
+    """One rank: the local problem a shard handle would get (irr_set_shard),
+    its halo received from the peers by the exchange lists of the plan, its
+    owned rows reduced; rank 0 gathers the rows."""
     os.environ["MASTER_ADDR"] = "127.0.0.1"
     os.environ["MASTER_PORT"] = str(port)
     dist.init_process_group("gloo", rank=rank, world_size=world)
-    import sharding
+    sharding = sharding_mod()
     case = load_golden(name)
     perm, row_off, col = partition_of(case)
     pos = case["pos"][perm]                 # partition order
     side = float(case["side"])
     shards = sharding.plan(row_off, col, world)
-    me = shards[rank]
-    # halo exchange: send what peers need, receive ours
-    reqs, recv = [], {}
-    for q, ids in me.send_to.items():
-        reqs.append(dist.isend(torch.from_numpy(pos[ids].copy()), dst=q))
-    for q, ids in me.recv_from.items():
+    lps = [sharding.local_problem(sh, row_off, col) for sh in shards]
+    me = lps[rank]
+    # local positions: owned from this rank's own data, halo from the peers
+    local = np.full((me.nodes.shape[0], 3), np.nan)
+    local[me.own_lo:me.own_hi] = pos[me.lo:me.hi]
+    owned = pos[me.lo:me.hi]
+    reqs = []
+    for q, ids in me.send_local.items():
+        reqs.append(dist.isend(torch.from_numpy(owned[ids - me.own_lo].copy()), dst=q))
+    for q, ids in me.recv_local.items():
         buf = torch.empty((ids.shape[0], 3), dtype=torch.float64)
         dist.recv(buf, src=q)
-        recv[q] = buf.numpy()
+        local[ids] = buf.numpy()
     for r in reqs:
         r.wait()
-    local = sharding.local_positions(me, pos[me.lo:me.hi], recv)
-    f_own = lj_rows(local, me.row_off, me.col, side, float(case["cutoff"]) ** 2)
+    assert not np.isnan(local).any()
+    f_own = lj_owned_rows(local, me, side, float(case["cutoff"]) ** 2)
     # gather owned rows on rank 0
     sizes = [s.hi - s.lo for s in shards]
     if rank == 0:
@@ -89,6 +125,43 @@ def free_port():
     p = s.getsockname()[1]
     s.close()
     return p
+
+
+def exchange_worker(rank, world, port, name, out_path):
+    """sharding.HaloExchange (the bench's per-step exchange) on gloo: every
+    rank's local record tensor, owned part filled, halo part NaN, must come out
+    equal to the whole problem's records at the local nodes."""
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    sharding = sharding_mod()
+    case = load_golden(name)
+    perm, row_off, col = partition_of(case)
+    pos = np.zeros((perm.shape[0], 4), np.float32)
+    pos[:, :3] = case["pos"][perm]
+    lps = [sharding.local_problem(sh, row_off, col) for sh in sharding.plan(row_off, col, world)]
+    me = lps[rank]
+    local = torch.full((me.nodes.shape[0], 4), float("nan"))
+    local[me.own_lo:me.own_hi] = torch.from_numpy(pos[me.lo:me.hi])
+    hx = sharding.HaloExchange(me, "cpu")
+    for _ in range(2):  # the buffers are reused step after step
+        hx.run(local)
+    ok = bool(np.array_equal(local.numpy(), pos[me.nodes]))
+    flags = torch.tensor([1 if ok else 0], dtype=torch.int64)
+    dist.all_reduce(flags)
+    if rank == 0:
+        np.save(out_path, flags.numpy())
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+@pytest.mark.parametrize("world", [2, 3])
+def test_halo_exchange_fills_every_halo(tmp_path, world):
+    import torch.multiprocessing as mp
+    out = str(tmp_path / "ok.npy")
+    mp.start_processes(exchange_worker, args=(world, free_port(), "moldyn_random_2048", out),
+                       nprocs=world, join=True, start_method="spawn")
+    assert int(np.load(out)[0]) == world
 
 
 @pytest.mark.parametrize("name", ["moldyn_random_2048", "moldyn_fcc_864"])
