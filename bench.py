@@ -15,7 +15,10 @@ Our arm prints one JSON line with
                the launching stream over K steps);
   e2e          the same metric through the public C ABI with host buffers:
                every step copies float xyz positions from pinned host memory,
-               reduces, and reads the float xyz forces back;
+               reduces, and reads the float xyz forces back, steps pipelined
+               (irr_step_pipelined: copies overlap the neighbouring steps'
+               reductions); e2e_sequential makes the same calls one after
+               another (irr_set_nodes, irr_step, irr_get_result);
   roofline     algorithmic bytes per step 8*E + 24*N (int32 endpoint pair per
                edge; float xyz read and force write per node) over the
                measured step time, against the measured HBM copy bandwidth;
@@ -416,6 +419,18 @@ def run_ours(args, rank, world, local):
         h.step()
         h.get_result(out_np, 12)
     e2e_s = max_over_ranks(time.perf_counter() - t0, world)
+    e2e_seq = E * e2e_steps * world / e2e_s
+    # the same, pipelined (irr_step_pipelined): the upload of step k+1 and the
+    # read-back of step k-1 overlap the reduction of step k
+    for _ in range(3):
+        h.step_pipelined(pin_in.numpy(), out_np, 12, 12)
+    h.pipeline_sync()
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        h.step_pipelined(pin_in.numpy(), out_np, 12, 12)
+    h.pipeline_sync()
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world)
     e2e = E * e2e_steps * world / e2e_s
 
     # the same reduction in the caller's random node order, for comparison
@@ -435,8 +450,9 @@ def run_ours(args, rank, world, local):
     alg_bytes = 8.0 * E + 24.0 * n
     achieved = alg_bytes / step_s / 1e9
     peak, peak_kind = measured_hbm_peak()
-    traffic = ncu_traffic("tiled_kernel_moldyn_4M") if n == N_NODES else None
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+    kernel = "halo_kernel" if info.layout == LAYOUTS["staged"] else "tiled_kernel"
+    traffic = ncu_traffic(f"{kernel}_moldyn_4M") if n == N_NODES else None
+    roofline = {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic,
                 "peak_source": f"{peak_kind} (hbm_gbs, MEASURED_PEAKS.json)",
                 "algorithmic_bytes_per_step": alg_bytes}
@@ -458,13 +474,23 @@ def run_ours(args, rank, world, local):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded uniform-random positions; edge list built on the GPU)",
         "config": {"workload": workload_name(n), "nodes": n, "edges": E,
-                   "exec": "partitioned (Hilbert-ordered node blocks, sliced entries, owner-computes tiled kernel)",
+                   "exec": "partitioned: Hilbert-ordered nodes, " + {0: "plain", 1: "CSR", 2: "sliced",
+                                                                      3: "staged (halo)"}[info.layout]
+                           + " layout, owner-computes kernel",
                    "lanes_per_row": info.lanes_per_row, "stage_smem": info.stage_smem,
                    "l2": "inputs larger than L2 (1.07 GB entry stream read every step)",
                    "parallelism": f"replicas x{world}"},
         "roofline": roofline,
         "e2e": {"value": e2e, "unit": "edges/s", "h2d_bytes_per_step": 12 * n,
-                "d2h_bytes_per_step": 12 * n},
+                "d2h_bytes_per_step": 12 * n, "steps": e2e_steps,
+                "mode": "pipelined (irr_step_pipelined): every step uploads float xyz positions "
+                        "from pinned host memory, reduces and reads float xyz forces back; the "
+                        "upload of step k+1 and the read-back of step k-1 overlap the reduction "
+                        "of step k (independent inputs: a served stream, a sweep)"},
+        "e2e_sequential": {"value": e2e_seq, "unit": "edges/s", "h2d_bytes_per_step": 12 * n,
+                           "d2h_bytes_per_step": 12 * n, "steps": e2e_steps,
+                           "mode": "irr_set_nodes, irr_step, irr_get_result one after another "
+                                   "(a dependent loop such as MD: nothing to overlap)"},
         "clocks": clk,
         "gpu_launches": args.steps,
         "variants_edges_per_s": variants,

@@ -232,6 +232,26 @@ IRR_API int irr_get_result(irr_handle *h, void *out, int elm_size);
  * 24-byte records, else IRR_ERR_ARG); enqueued, does not synchronise. */
 IRR_API int irr_get_result_device(irr_handle *h, void *d_out, int elm_size);
 
+/* One step on new node data, pipelined with the steps before and after it:
+ * irr_set_nodes + irr_step + irr_get_result for a stream of independent
+ * inputs (a served stream, a parameter sweep), returning at once.  The
+ * records (num_nodes of node_elm bytes, caller's order, host memory) are
+ * copied to the device on a copy stream, reordered and reduced on the
+ * handle's stream, and the result (out_elm bytes per result row, as
+ * irr_get_result writes it) copied back to `out` on a second copy stream;
+ * two slots of device staging let the upload of step k+1 and the read-back
+ * of step k-1 run while step k reduces.  node_data is read and out written
+ * asynchronously (page-locked memory gives overlapped copies; pageable memory
+ * is copied synchronously): keep node_data unchanged and out unread until
+ * irr_pipeline_sync returns.  After irr_init; built-in maps only.  No
+ * counterpart in the reference, whose IrregularStart and
+ * get_reduction_result each wait (irregular_runtime.cu:311-411). */
+IRR_API int irr_step_pipelined(irr_handle *h, const void *node_data, int node_elm, void *out,
+                               int out_elm);
+/* Waits for every pipelined step issued so far (results in their `out`
+ * buffers) and reports any device-side fault. */
+IRR_API int irr_pipeline_sync(irr_handle *h);
+
 /* Waits for the handle's stream and reports any device-side fault. */
 IRR_API int irr_sync(irr_handle *h);
 /* The limit of the partitioned kernel's device-side waits (irr_config

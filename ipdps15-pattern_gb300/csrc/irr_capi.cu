@@ -313,6 +313,77 @@ void result_rows(const irr_handle* h, int64_t* lo, int64_t* count)
     *count = h->own_hi >= 0 ? h->own_hi - h->own_lo : h->n;
 }
 
+// The reduction of one step over the positions in d_pos, on h->stream.
+int launch_reduction(irr_handle* h)
+{
+    if (h->cfg.exec == IRR_EXEC_PLAIN) {
+        H_CUDA(h, cudaMemsetAsync(h->d_force, 0, (size_t)(h->n > 0 ? h->n : 1) * sizeof(float4), h->stream), "clear results");
+        H_CUDA(h, launch_plain(h->d_pos, h->d_edges, h->e, h->d_force, h->law, h->stream), "plain kernel");
+        return IRR_OK;
+    }
+    H_CUDA(h, cudaMemsetAsync(h->d_queue, 0, sizeof(int), h->stream), "clear work queue");
+    const WaitPolicy wp = h->wait;
+    h->wait.withhold = 0;  // one step only
+    H_CUDA(h, launch_tiled(h->shape, h->d_inst, h->d_items, h->num_items, h->d_queue,
+                           h->sms * kCtasPerSm, h->d_status, h->stream, &h->inst, 1, wp),
+           "tiled kernel");
+    return IRR_OK;
+}
+
+// Streams, events and staging of the pipelined path (grown as needed).
+int ensure_pipe(irr_handle* h, size_t in_bytes, size_t out_bytes)
+{
+    irr_handle::Pipe& P = h->pipe;
+    if (!P.s_in) {
+        H_CUDA(h, cudaStreamCreateWithFlags(&P.s_in, cudaStreamNonBlocking), "pipeline stream");
+        H_CUDA(h, cudaStreamCreateWithFlags(&P.s_out, cudaStreamNonBlocking), "pipeline stream");
+        for (int s = 0; s < 2; s++) {
+            H_CUDA(h, cudaEventCreateWithFlags(&P.in_done[s], cudaEventDisableTiming), "pipeline event");
+            H_CUDA(h, cudaEventCreateWithFlags(&P.in_free[s], cudaEventDisableTiming), "pipeline event");
+            H_CUDA(h, cudaEventCreateWithFlags(&P.out_ready[s], cudaEventDisableTiming), "pipeline event");
+            H_CUDA(h, cudaEventCreateWithFlags(&P.out_free[s], cudaEventDisableTiming), "pipeline event");
+        }
+    }
+    if (in_bytes > P.in_cap || out_bytes > P.out_cap) {
+        // no step in flight may use the old staging
+        H_CUDA(h, cudaStreamSynchronize(P.s_in), "pipeline");
+        H_CUDA(h, cudaStreamSynchronize(h->stream), "pipeline");
+        H_CUDA(h, cudaStreamSynchronize(P.s_out), "pipeline");
+        if (in_bytes > P.in_cap) {
+            for (int s = 0; s < 2; s++) dfree(P.in[s]);
+            P.in_cap = 0;
+            for (int s = 0; s < 2; s++) H_CUDA(h, cudaMalloc(&P.in[s], in_bytes), "pipeline staging");
+            P.in_cap = in_bytes;
+        }
+        if (out_bytes > P.out_cap) {
+            for (int s = 0; s < 2; s++) dfree(P.out[s]);
+            P.out_cap = 0;
+            for (int s = 0; s < 2; s++) H_CUDA(h, cudaMalloc(&P.out[s], out_bytes), "pipeline staging");
+            P.out_cap = out_bytes;
+        }
+    }
+    return IRR_OK;
+}
+
+void free_pipe(irr_handle* h)
+{
+    irr_handle::Pipe& P = h->pipe;
+    if (P.s_in) cudaStreamSynchronize(P.s_in);
+    if (P.s_out) cudaStreamSynchronize(P.s_out);
+    for (int s = 0; s < 2; s++) {
+        dfree(P.in[s]);
+        dfree(P.out[s]);
+        for (cudaEvent_t* e : {&P.in_done[s], &P.in_free[s], &P.out_ready[s], &P.out_free[s]})
+            if (*e) {
+                cudaEventDestroy(*e);
+                *e = nullptr;
+            }
+    }
+    if (P.s_in) cudaStreamDestroy(P.s_in);
+    if (P.s_out) cudaStreamDestroy(P.s_out);
+    P = irr_handle::Pipe{};
+}
+
 // User map: positions for the partitioner (coordinates, else position-like
 // records, else none: the caller's order is kept), then the partition, the
 // node records in execution order, and the view's other arrays.
@@ -592,6 +663,7 @@ int irr_destroy(irr_handle* h)
     dfree(h->d_queue);
     dfree(h->d_out);
     dfree(h->d_coord);
+    free_pipe(h);
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
     delete h;
     return IRR_OK;
@@ -777,18 +849,59 @@ int irr_step(irr_handle* h)
         H_CUDA(h, launch_load_nodes(h->d_raw, h->raw_elm, h->part.perm, h->n, h->d_pos, h->stream), "load node data");
         h->raw_pending = false;
     }
-    if (h->cfg.exec == IRR_EXEC_PLAIN) {
-        H_CUDA(h, cudaMemsetAsync(h->d_force, 0, (size_t)(h->n > 0 ? h->n : 1) * sizeof(float4), h->stream), "clear results");
-        H_CUDA(h, launch_plain(h->d_pos, h->d_edges, h->e, h->d_force, h->law, h->stream), "plain kernel");
-        return IRR_OK;
-    }
-    H_CUDA(h, cudaMemsetAsync(h->d_queue, 0, sizeof(int), h->stream), "clear work queue");
-    const WaitPolicy wp = h->wait;
-    h->wait.withhold = 0;  // one step only
-    H_CUDA(h, launch_tiled(h->shape, h->d_inst, h->d_items, h->num_items, h->d_queue,
-                           h->sms * kCtasPerSm, h->d_status, h->stream, &h->inst, 1, wp),
-           "tiled kernel");
+    return launch_reduction(h);
+}
+
+int irr_step_pipelined(irr_handle* h, const void* node_data, int node_elm, void* out, int out_elm)
+{
+    if (!h) return IRR_ERR_ARG;
+    if (!h->inited) return fail(h, IRR_ERR_STATE, "irr_step_pipelined before irr_init");
+    if (h->user_launch) return fail(h, IRR_ERR_STATE, "a handle with a user map steps with irr_step");
+    if (!valid_node_elm(h, node_elm)) return fail(h, IRR_ERR_ARG, "node elm_size %d: use 12, 16 or 24", node_elm);
+    if (out_elm != 12 && out_elm != 16 && out_elm != 24)
+        return fail(h, IRR_ERR_ARG, "result elm_size %d: use 12, 16 or 24", out_elm);
+    int64_t lo, count;
+    result_rows(h, &lo, &count);
+    if ((!node_data && h->n > 0) || (!out && count > 0)) return fail(h, IRR_ERR_ARG, "null buffer");
+    DeviceGuard dev_guard(h->device);
+    const int64_t n = h->n;
+    int rc = ensure_pipe(h, (size_t)(n > 0 ? n : 1) * node_elm, (size_t)(count > 0 ? count : 1) * out_elm);
+    if (rc) return rc;
+    irr_handle::Pipe& P = h->pipe;
+    const int s = (int)(P.issued & 1);
+    // upload, once the reduction two steps back has consumed this slot
+    H_CUDA(h, cudaStreamWaitEvent(P.s_in, P.in_free[s], 0), "pipeline order");
+    if (n > 0)
+        H_CUDA(h, cudaMemcpyAsync(P.in[s], node_data, (size_t)n * node_elm, cudaMemcpyHostToDevice, P.s_in),
+               "upload node data");
+    H_CUDA(h, cudaEventRecord(P.in_done[s], P.s_in), "pipeline order");
+    // reduce: records -> execution order, the reduction, results -> staging
+    H_CUDA(h, cudaStreamWaitEvent(h->stream, P.in_done[s], 0), "pipeline order");
+    H_CUDA(h, launch_load_nodes(P.in[s], node_elm, h->part.perm, n, h->d_pos, h->stream), "load node data");
+    H_CUDA(h, cudaEventRecord(P.in_free[s], h->stream), "pipeline order");
+    h->raw_pending = false;
+    rc = launch_reduction(h);
+    if (rc) return rc;
+    H_CUDA(h, cudaStreamWaitEvent(h->stream, P.out_free[s], 0), "pipeline order");
+    H_CUDA(h, launch_store_result(h->d_force, h->part.inv ? h->part.inv + lo : nullptr, count, out_elm, P.out[s],
+                                  h->stream), "store result");
+    H_CUDA(h, cudaEventRecord(P.out_ready[s], h->stream), "pipeline order");
+    // read back, while the next step reduces
+    H_CUDA(h, cudaStreamWaitEvent(P.s_out, P.out_ready[s], 0), "pipeline order");
+    if (count > 0)
+        H_CUDA(h, cudaMemcpyAsync(out, P.out[s], (size_t)count * out_elm, cudaMemcpyDeviceToHost, P.s_out),
+               "read back results");
+    H_CUDA(h, cudaEventRecord(P.out_free[s], P.s_out), "pipeline order");
+    P.issued++;
     return IRR_OK;
+}
+
+int irr_pipeline_sync(irr_handle* h)
+{
+    if (!h) return IRR_ERR_ARG;
+    DeviceGuard dev_guard(h->device);
+    if (h->pipe.s_out) H_CUDA(h, cudaStreamSynchronize(h->pipe.s_out), "pipeline");
+    return check_status(h);
 }
 
 int irr_get_result_device(irr_handle* h, void* d_out, int elm_size)

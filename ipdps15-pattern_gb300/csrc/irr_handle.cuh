@@ -57,6 +57,23 @@ struct irr_handle {
     size_t out_cap = 0;
     int64_t dev_bytes = 0;
 
+    // irr_step_pipelined: two slots of staging for the host copies, a
+    // copy-in and a copy-out stream, and the events that order slot reuse
+    // against the reduction on `stream`
+    struct Pipe {
+        cudaStream_t s_in = nullptr;
+        cudaStream_t s_out = nullptr;
+        void* in[2] = {nullptr, nullptr};
+        void* out[2] = {nullptr, nullptr};
+        size_t in_cap = 0;
+        size_t out_cap = 0;
+        cudaEvent_t in_done[2] = {nullptr, nullptr};    // upload of the slot finished
+        cudaEvent_t in_free[2] = {nullptr, nullptr};    // the slot's records consumed
+        cudaEvent_t out_ready[2] = {nullptr, nullptr};  // results staged in the slot
+        cudaEvent_t out_free[2] = {nullptr, nullptr};   // the slot's read-back finished
+        int64_t issued = 0;
+    } pipe;
+
     // user map (the irregular.h plugin): bound by irr_set_user_map
     irr_user_launch_fn user_launch = nullptr;
     void* user_ctx = nullptr;

@@ -674,7 +674,10 @@ __device__ __forceinline__ float4 lds128(uint32_t addr)
 // On the 4M-node workload (ms per step): static 0.396 vs dynamic 0.414 slice
 // claims; pair addresses 0.391 vs 0.396; 7 consumer warps 0.455 and 3 CTAs
 // per SM 0.415 vs 8 warps x 4 CTAs 0.396; rotated claims 0.3877 vs 0.3899;
-// the step loop unrolled by 2 (spills) 0.421; sleep-free waits 0.393; 3-stage
+// the step loop unrolled by 2 (spills) 0.421; the steps that every row of a
+// slice fills split off into a loop without the entry masks (spills) 0.410;
+// sleep-free waits 0.393, and polls that sleep up to 128 ns to 2 us between
+// tests all 0.3875-0.3878; 3-stage
 // rings (3 CTAs per SM, or smaller items at 4) 0.395-0.431; 4 or 6 consumer
 // warps with 6 or 7 CTAs per SM 0.413-0.418; each item's steps cut evenly
 // across the warps (slices split between warps, piece sums joined in shared
@@ -720,6 +723,22 @@ __device__ __forceinline__ bool mbar_wait_policy(uint64_t* bar, uint32_t parity,
     else return mbar_wait_backoff<MAX_NS>(bar, parity, limit_ns);
 }
 
+// The two neighbours of a lane's step: one word of two 16-bit table byte
+// offsets, then the two positions from the table.
+__device__ __forceinline__ void halo_operands(uint32_t addr, uint32_t tab_u32, uint32_t tab_pair, float4& b0,
+                                              float4& b1)
+{
+    if (IRR_HALO_PAIR_ADDR) {
+        const uint32_t wd = lds32(addr) + tab_pair;
+        b0 = lds128(wd & 0xffffu);
+        b1 = lds128(wd >> 16);
+    } else {
+        const uint32_t wd = lds32(addr);
+        b0 = lds128(tab_u32 + (wd & 0xffffu));
+        b1 = lds128(tab_u32 + (wd >> 16));
+    }
+}
+
 template <bool PERIODIC>
 __device__ __forceinline__ void consume_halo(int row0, int nrows, const uint32_t* soff, int* claim,
                                              const InstHot& I, const uint32_t* sw, int lane32,
@@ -753,15 +772,7 @@ __device__ __forceinline__ void consume_halo(int row0, int nrows, const uint32_t
         for (uint32_t t = 0; t < steps; t++) {
             addr += 128u;
             float4 b0, b1;
-            if (IRR_HALO_PAIR_ADDR) {
-                const uint32_t wd = lds32(addr) + tab_pair;
-                b0 = lds128(wd & 0xffffu);
-                b1 = lds128(wd >> 16);
-            } else {
-                const uint32_t wd = lds32(addr);
-                b0 = lds128(tab_u32 + (wd & 0xffffu));
-                b1 = lds128(tab_u32 + (wd >> 16));
-            }
+            halo_operands(addr, tab_u32, tab_pair, b0, b1);
             const uint32_t k0 = 8 * t + lane;
             lj_pair<PERIODIC>(a, b0, b1, k0 < len, k0 + 4 < len, H, cold, ax, ay, az);
         }

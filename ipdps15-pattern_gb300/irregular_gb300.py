@@ -144,6 +144,8 @@ _SIGS = {
     "irr_set_user_map": (C.c_int, [P, P, P, C.c_int, C.c_int]),
     "irr_set_coordinates": (C.c_int, [P, P, C.c_int, C.c_int, I64]),
     "irr_set_shard": (C.c_int, [P, I64, I64]),
+    "irr_step_pipelined": (C.c_int, [P, P, C.c_int, P, C.c_int]),
+    "irr_pipeline_sync": (C.c_int, [P]),
     "irr_set_nodes_range": (C.c_int, [P, P, C.c_int, I64, I64]),
     "irr_set_nodes_range_device": (C.c_int, [P, P, C.c_int, I64, I64]),
     "irr_neighbor_build": (C.c_int, [C.c_int, P, P, C.c_int, C.c_int, I64, C.c_float, C.c_float,
@@ -411,6 +413,18 @@ class Handle:
 
     def sync(self):
         self._check(load().irr_sync(self._h), "irr_sync")
+
+    def step_pipelined(self, nodes: np.ndarray, out: np.ndarray, node_elm: int = 12,
+                       out_elm: int = 12):
+        """irr_step_pipelined: upload nodes, reduce, read the result into out,
+        overlapped with the neighbouring steps; out is valid after
+        pipeline_sync().  Both arrays must stay alive (and nodes unchanged)
+        until then."""
+        self._check(load().irr_step_pipelined(self._h, _ptr(nodes), int(node_elm), _ptr(out),
+                                              int(out_elm)), "irr_step_pipelined")
+
+    def pipeline_sync(self):
+        self._check(load().irr_pipeline_sync(self._h), "irr_pipeline_sync")
 
     def set_wait_limit(self, limit_us: int, withhold_once: bool = False):
         """irr_set_wait_limit: the device-side wait limit, and (withhold_once)
