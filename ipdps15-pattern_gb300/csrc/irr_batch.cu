@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "irr_handle.cuh"
+#include "irr_trace.cuh"
 
 using namespace irr;
 
@@ -321,6 +322,7 @@ int irr_batch_add(irr_batch* b, irr_handle* h)
 
 int irr_batch_finalize(irr_batch* b, int autotune_shape)
 {
+    irr::TraceRange trace_("irr_batch_finalize");
     if (!b) return IRR_ERR_ARG;
     if (b->finalized) return IRR_OK;
     if (b->handles.empty()) return bfail(b, IRR_ERR_STATE, "empty batch");
@@ -351,6 +353,7 @@ int irr_batch_finalize(irr_batch* b, int autotune_shape)
 
 int irr_batch_step(irr_batch* b)
 {
+    irr::TraceRange trace_("irr_batch_step");
     if (!b) return IRR_ERR_ARG;
     if (!b->finalized) return bfail(b, IRR_ERR_STATE, "irr_batch_step before irr_batch_finalize");
     DeviceGuard dev_guard(b->device);
@@ -415,6 +418,7 @@ int irr_batch_get_info(const irr_batch* b, irr_batch_info* info)
 
 int irr_autotune(irr_handle* h)
 {
+    irr::TraceRange trace_("irr_autotune");
     if (!h) return IRR_ERR_ARG;
     if (h->cfg.exec != IRR_EXEC_PARTITIONED) return IRR_OK;  // nothing to tune
     if (!h->inited) {

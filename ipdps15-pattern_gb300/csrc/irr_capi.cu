@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "irr_handle.cuh"
+#include "irr_trace.cuh"
 
 using namespace irr;
 
@@ -493,6 +494,7 @@ bool user_result_ok(const irr_handle* h, int elm_size)
 
 int irr_ensure_layout(irr_handle* h, int lanes_per_row, int block_nodes, int staged_ok)
 {
+    TraceRange trace_("irr_layout");
     if (!h || !h->inited || h->cfg.exec != IRR_EXEC_PARTITIONED) return IRR_ERR_STATE;
     if (h->user_launch) return fail(h, IRR_ERR_STATE, "a handle with a user map runs its own kernel");
     DeviceGuard dev_guard(h->device);
@@ -760,6 +762,7 @@ int irr_set_edges_device(irr_handle* h, const int32_t* d_edges, int64_t num_edge
 
 int irr_set_nodes(irr_handle* h, const void* node_data, int elm_size, int64_t num_nodes)
 {
+    TraceRange trace_("irr_set_nodes");
     if (!h) return IRR_ERR_ARG;
     DeviceGuard dev_guard(h->device);
     return set_nodes_common(h, node_data, elm_size, num_nodes, cudaMemcpyHostToDevice);
@@ -774,6 +777,7 @@ int irr_set_nodes_device(irr_handle* h, const void* d_node_data, int elm_size, i
 
 int irr_init(irr_handle* h)
 {
+    TraceRange trace_("irr_init");
     if (!h) return IRR_ERR_ARG;
     if (h->inited) return IRR_OK;
     if (h->n < 0) return fail(h, IRR_ERR_STATE, "irr_init before irr_set_nodes");
@@ -838,6 +842,7 @@ int irr_init(irr_handle* h)
 
 int irr_step(irr_handle* h)
 {
+    TraceRange trace_("irr_step");
     if (!h) return IRR_ERR_ARG;
     if (!h->inited) {
         int rc = irr_init(h);
@@ -854,6 +859,7 @@ int irr_step(irr_handle* h)
 
 int irr_step_pipelined(irr_handle* h, const void* node_data, int node_elm, void* out, int out_elm)
 {
+    TraceRange trace_("irr_step_pipelined");
     if (!h) return IRR_ERR_ARG;
     if (!h->inited) return fail(h, IRR_ERR_STATE, "irr_step_pipelined before irr_init");
     if (h->user_launch) return fail(h, IRR_ERR_STATE, "a handle with a user map steps with irr_step");
@@ -932,6 +938,7 @@ int irr_get_result_device(irr_handle* h, void* d_out, int elm_size)
 
 int irr_get_result(irr_handle* h, void* out, int elm_size)
 {
+    TraceRange trace_("irr_get_result");
     if (!h || (!out && h->n > 0)) return fail(h, IRR_ERR_ARG, "null output");
     if (h->user_launch ? !user_result_ok(h, elm_size) : (elm_size != 12 && elm_size != 16 && elm_size != 24))
         return fail(h, IRR_ERR_ARG, "result elm_size %d: not a record size of this handle", elm_size);

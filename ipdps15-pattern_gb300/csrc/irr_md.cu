@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "irr_md.cuh"
+#include "irr_trace.cuh"
 
 using namespace irr;
 
@@ -473,6 +474,7 @@ void irr_md_config_default(irr_md_config* c)
 int irr_md_create(const irr_md_config* cfg, const double* pos, const double* vel, int64_t n,
                   irr_md** out)
 {
+    irr::TraceRange trace_("irr_md_create");
     if (!cfg || !out || n < 2 || !pos || !vel) return IRR_ERR_ARG;
     *out = nullptr;
     if (!(cfg->side > 0) || !(cfg->dt > 0) || !(cfg->cutforce > 0) || !(cfg->skin >= 0) ||
@@ -587,6 +589,7 @@ int irr_md_set_stream(irr_md* m, void* stream)
 
 int irr_md_run(irr_md* m, int steps)
 {
+    irr::TraceRange trace_("irr_md_run");
     if (!m || steps < 0) return IRR_ERR_ARG;
     DeviceGuard dev_guard(m->device);
     for (int t = 0; t < steps; t++) {

@@ -32,6 +32,7 @@
 #include <vector>
 
 #include "irr_internal.cuh"
+#include "irr_trace.cuh"
 #include "../../include/irregular_gb300.h"
 
 namespace irr {
@@ -795,6 +796,7 @@ int irr_neighbor_build(int device, void* stream, const void* pos, int pos_elm, i
                        int64_t n, float box, float list_cut2, int32_t** d_edges,
                        int64_t* num_edges)
 {
+    irr::TraceRange trace_("irr_neighbor_build");
     if (!d_edges || !num_edges || n < 0 || (n > 0 && !pos)) return IRR_ERR_ARG;
     if (pos_elm != 12 && pos_elm != 16 && pos_elm != 24) return IRR_ERR_ARG;
     if (!(box >= 0.0f) || !(list_cut2 >= 0.0f) || !std::isfinite(box) || !std::isfinite(list_cut2))

@@ -30,6 +30,7 @@
 #include <vector>
 
 #include "irr_md.cuh"
+#include "irr_trace.cuh"
 
 using namespace irr;
 
@@ -476,6 +477,7 @@ int irr_serve_job_state(const irr_serve_config* cfg, int job, int64_t* atoms, do
 
 int irr_serve_run(const irr_serve_config* cfg, irr_serve_stats* st, irr_serve_job* out)
 {
+    irr::TraceRange trace_("irr_serve_run");
     if (!cfg || !st) return IRR_ERR_ARG;
     if (cfg->num_jobs < 0 || cfg->steps_per_job < 1 || cfg->rebuild_every < 1 ||
         cfg->min_atoms < 32 || cfg->max_atoms < cfg->min_atoms || !(cfg->density > 0) ||
