@@ -683,7 +683,10 @@ __device__ __forceinline__ float4 lds128(uint32_t addr)
 // across the warps (slices split between warps, piece sums joined in shared
 // memory) 0.722: the extra state around the step loop doubled its
 // instructions.  The words prefetched into L2 one item ahead: 0.3907 vs
-// 0.3873.  What the warps still lose is the ring's coupling: a stage is
+// 0.3873.  A table ring one buffer deeper than the word ring, each item's
+// table gathered one item ahead (limits 3072 words / 576 ids to fit 4 CTAs
+// per SM): 0.403, vs 0.3888 for this kernel at those limits and 0.3874 at
+// 3584 / 640 -- the refill is not bounded by the table gather alone.  What the warps still lose is the ring's coupling: a stage is
 // refilled only when its slowest warp is done (~4.3K cycles after the first),
 // and the refill takes ~3.6K cycles, so the first warps wait ~1.2K of each
 // item's ~7.6K cycles.

@@ -298,3 +298,28 @@ def test_user_map_handles_run_alone(plugins):
     with pytest.raises(irr.IrregularError) as e:
         b.finalize()
     assert e.value.status == irr.IRR_ERR_STATE
+
+
+def test_user_map_on_shards(plugins):
+    """A user map on shard handles (irr_set_shard): the union of the shards'
+    owned rows equals one whole-problem handle bit for bit."""
+    import sharding
+    nodes, x, edges, para = spring_case(n=2500, seed=21)
+    hw = spring_handle(plugins["launch"]["spring"], nodes, x, edges, para)
+    hw.step()
+    perm, row_off, col = hw.partition()
+    whole = hw.get_result(elm_size=12)[perm]
+    rec = nodes.view(np.uint8).reshape(len(nodes), -1)[perm]
+    got = np.zeros_like(whole)
+    for sh in sharding.plan(row_off, col, 3):
+        lp = sharding.local_problem(sh, row_off, col)
+        h = irr.Handle(exec=irr.IRR_EXEC_PARTITIONED, reorder=0)
+        h.set_user_map(plugins["launch"]["spring"], 12, 1)
+        h.set_params(para)
+        h.set_shard(lp.own_lo, lp.own_hi)
+        h.set_edges(lp.edges)
+        h.set_nodes(np.ascontiguousarray(rec[lp.nodes]), elm_size=32)
+        h.init()
+        h.step()
+        got[lp.lo:lp.hi] = h.get_result(elm_size=12)
+    assert np.array_equal(got.view(np.uint32), whole.view(np.uint32))

@@ -163,3 +163,25 @@ def test_shard_arguments(built_lib):
     assert e.value.status == irr.IRR_ERR_STATE
     with pytest.raises(irr.IrregularError):
         h2.set_nodes_range(np.zeros((4, 4), np.float32), 2046, elm_size=16)  # past the end
+
+
+def test_pipelined_steps_on_shards(built_lib):
+    """irr_step_pipelined on shard handles returns the owned rows only, the
+    bits of the sequential calls."""
+    c = load_golden("moldyn_random_2048")
+    params = irr.moldyn_params(float(c["side"]), float(c["cutoff"]))
+    pos4 = as_f4(c["pos"].astype(np.float32))
+    hw = whole_handle(pos4, c["edges"], params, irr.IRR_LAYOUT_SLICED)
+    perm, row_off, col = hw.partition()
+    plans = [sharding.local_problem(sh, row_off, col) for sh in sharding.plan(row_off, col, 2)]
+    hs = shard_handles(plans, pos4[perm], params, irr.IRR_LAYOUT_SLICED)
+    hw.step()
+    whole = hw.get_result(elm_size=16)[perm]
+    for lp, h in zip(plans, hs):
+        recs = np.ascontiguousarray(pos4[perm][lp.nodes])
+        outs = [np.empty((lp.own_hi - lp.own_lo, 4), np.float32) for _ in range(3)]
+        for o in outs:
+            h.step_pipelined(recs, o, 16, 16)
+        h.pipeline_sync()
+        for o in outs:
+            assert np.array_equal(o.view(np.uint32), whole[lp.lo:lp.hi].view(np.uint32))
