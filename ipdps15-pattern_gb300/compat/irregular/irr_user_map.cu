@@ -42,6 +42,21 @@ struct TableCall {
     }
 };
 
+// IRR_PLUGIN_INLINE_MAP=<name>: call that map of the FGPU namespace directly
+// (inlined into the kernel) instead of through the table; map_idx is then
+// ignored.  With IRR_PLUGIN_COMPENSATED the reduce is not called either.
+#ifdef IRR_PLUGIN_INLINE_MAP
+struct InlineCall {
+    int reduce_idx;
+    __device__ void operator()(Sobject *object, void *point_data, int *part_index, void *edge_data,
+                               void *parameter, unsigned int task_id, unsigned int part_id) const
+    {
+        FGPU::IRR_PLUGIN_INLINE_MAP(object, point_data, part_index, edge_data, parameter, task_id, part_id,
+                                    FGPU::reduce_function_table[reduce_idx]);
+    }
+};
+#endif
+
 constexpr int kNumMaps = (int)(sizeof(FGPU::map_function_table) / sizeof(FGPU::map_function_table[0]));
 constexpr int kNumReduces =
     (int)(sizeof(FGPU::reduce_function_table) / sizeof(FGPU::reduce_function_table[0]));
@@ -54,7 +69,11 @@ extern "C" int irr_compat_user_launch(const irr_user_view *view, void *stream, v
     if (!view || view->map_idx < 0 || view->map_idx >= kNumMaps || view->reduce_idx < 0 ||
         view->reduce_idx >= kNumReduces)
         return IRR_ERR_ARG;
+#ifdef IRR_PLUGIN_INLINE_MAP
+    return irr_plugin::launch_rows<Sobject>(view, stream, InlineCall{view->reduce_idx});
+#else
     return irr_plugin::launch_rows<Sobject>(view, stream, TableCall{view->map_idx, view->reduce_idx});
+#endif
 }
 
 extern "C" int irr_compat_register_user_map(irr_handle *h)

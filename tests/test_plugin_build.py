@@ -31,6 +31,8 @@ def test_fixture_plugins_compile(tmp_path):
         "spring_comp": (os.path.join(FIXTURES, "spring"), str(tmp_path / "spring_comp.o"), False,
                         ("IRR_PLUGIN_COMPENSATED",), True),
         "lj": (os.path.join(FIXTURES, "lj"), str(tmp_path / "lj.o"), False, (), False),
+        "lj_inline": (os.path.join(FIXTURES, "lj"), str(tmp_path / "lj_inline.o"), False,
+                      ("IRR_PLUGIN_INLINE_MAP=lj_box", "IRR_PLUGIN_COMPENSATED"), True),
     }
     for name, obj in build_plugins(jobs).items():
         syms = defined_symbols(obj)
