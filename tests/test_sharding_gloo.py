@@ -200,3 +200,31 @@ def test_plan_properties():
         counts = [int(row_off[s.hi] - row_off[s.lo]) for s in shards]
         # each cut lands within one row of its target
         assert max(counts) - min(counts) <= 2 * int(np.diff(row_off).max())
+
+
+def test_local_problems_keep_every_owned_row(oracle_lib):
+    """sharding.local_problem: every owned row of every shard holds, in local
+    ids, exactly the whole problem's row -- with duplicated pairs and self
+    pairs (which fill their row twice) kept."""
+    import sharding
+    O = oracle_lib
+    rng = np.random.default_rng(3)
+    n = 400
+    pos = rng.random((n, 3)).astype(np.float32)
+    e = rng.integers(0, n, (3000, 2)).astype(np.int32)
+    e[:60, 1] = e[:60, 0]                        # self pairs
+    e = np.concatenate([e, e[:150], e[:30]])     # duplicates, self pairs among them
+    lo, scale = O.morton_frame(pos)
+    _, _, row_off, col = O.partition(pos, lo, scale, e)
+    for parts in (1, 2, 3, 5):
+        for sh in sharding.plan(row_off, col, parts):
+            lp = sharding.local_problem(sh, row_off, col)
+            assert np.all(np.diff(lp.nodes) > 0)
+            assert np.array_equal(lp.nodes[lp.own_lo:lp.own_hi], np.arange(sh.lo, sh.hi))
+            ro, cc = sharding.local_rows(lp)
+            assert np.array_equal(ro, row_off[sh.lo:sh.hi + 1] - row_off[sh.lo])
+            assert np.array_equal(lp.nodes[cc], col[row_off[sh.lo]:row_off[sh.hi]])
+            # the exchange lists cover the halo exactly once
+            got = np.sort(np.concatenate([v for v in lp.recv_local.values()])) if lp.recv_local else []
+            halo = np.r_[np.arange(0, lp.own_lo), np.arange(lp.own_hi, lp.nodes.shape[0])]
+            assert np.array_equal(got, halo)
