@@ -77,3 +77,16 @@ def test_pipelined_before_init_is_refused(built_lib):
     with pytest.raises(irr.IrregularError) as e:
         h.step_pipelined(np.zeros((4, 3), np.float32), np.zeros((4, 3), np.float32))
     assert e.value.status == irr.IRR_ERR_STATE
+
+
+def test_pipelined_step_of_an_empty_graph(built_lib):
+    pos = np.random.default_rng(1).random((100, 3)).astype(np.float32) * 10
+    h = irr.Handle(exec=irr.IRR_EXEC_PARTITIONED)
+    h.set_params(irr.moldyn_params(10.0, 2.5))
+    h.set_edges(np.zeros((0, 2), np.int32))
+    h.set_nodes(pos, 12)
+    h.init()
+    out = np.full((100, 3), 7.0, np.float32)
+    h.step_pipelined(pos, out, 12, 12)
+    h.pipeline_sync()
+    assert np.all(out == 0)

@@ -323,3 +323,11 @@ def test_user_map_on_shards(plugins):
         h.step()
         got[lp.lo:lp.hi] = h.get_result(elm_size=12)
     assert np.array_equal(got.view(np.uint32), whole.view(np.uint32))
+
+
+def test_user_map_without_edges(plugins):
+    """No edges: every row's object stays empty and stores zero bytes."""
+    nodes, x, _, para = spring_case(n=64, seed=2)
+    h = spring_handle(plugins["launch"]["spring"], nodes, x, np.zeros((0, 2), np.int32), para)
+    h.step()
+    assert np.all(h.get_result(elm_size=12) == 0)

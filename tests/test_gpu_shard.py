@@ -185,3 +185,29 @@ def test_pipelined_steps_on_shards(built_lib):
         h.pipeline_sync()
         for o in outs:
             assert np.array_equal(o.view(np.uint32), whole[lp.lo:lp.hi].view(np.uint32))
+
+
+@pytest.mark.parametrize("layout", [irr.IRR_LAYOUT_AUTO, irr.IRR_LAYOUT_SLICED, irr.IRR_LAYOUT_CSR])
+def test_degenerate_shards(built_lib, layout):
+    """A shard that owns no rows, and one that owns every node but sees no
+    edges: both run, and return no records / zero forces."""
+    c = load_golden("moldyn_random_2048")
+    params = irr.moldyn_params(float(c["side"]), float(c["cutoff"]))
+    pos4 = as_f4(c["pos"].astype(np.float32))
+    h = irr.Handle(exec=irr.IRR_EXEC_PARTITIONED, layout=layout, reorder=0)
+    h.set_params(params)
+    h.set_shard(5, 5)
+    h.set_edges(c["edges"])
+    h.set_nodes(pos4, elm_size=16)
+    h.init()
+    h.step()
+    assert h.info().num_entries == 0
+    assert h.get_result(elm_size=16).shape[0] == 0
+    h2 = irr.Handle(exec=irr.IRR_EXEC_PARTITIONED, layout=layout, reorder=0)
+    h2.set_params(params)
+    h2.set_shard(0, pos4.shape[0])
+    h2.set_edges(np.zeros((0, 2), np.int32))
+    h2.set_nodes(pos4, elm_size=16)
+    h2.init()
+    h2.step()
+    assert np.all(h2.get_result(elm_size=16) == 0)
