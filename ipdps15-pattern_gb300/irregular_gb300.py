@@ -733,20 +733,36 @@ class IrregularRuntime:
     """The reference's IrregularRuntime interface over the C ABI.
 
     Constructor arguments follow irregular_runtime.h:71-86; `num_procs`,
-    `num_iters` and the edge/coordinate extras are accepted for source
-    compatibility (one GPU, no MPI split).  `map_idx` picks the built-in user
-    function (IRR_MAP_*)."""
+    `num_iters` and the edge data are accepted for source compatibility (one
+    GPU, no MPI split).  `map_idx` picks a built-in user function (IRR_MAP_*);
+    `user_launch` (the address of an irr_user_launch_fn, e.g. the
+    irr_compat_user_launch of a library built from compat/irregular/
+    irr_user_map.cu with the application's irregular.h) binds the
+    application's own map and reduce tables instead, with `value_size`-byte
+    results, and then `node_coordinates` ((n, node_num_dims) floats or
+    doubles) order the nodes."""
 
     def __init__(self, num_edges, num_nodes, edges, edge_data, node_data, edge_data_elm_size,
                  node_data_elm_size, reduction_elm_size, node_num_dims=3,
                  node_coordinates=None, coordinate_size=8, parameter=None, parameter_size=None,
                  num_procs=1, num_iters=1, map_idx=IRR_MAP_LJ_MOLDYN,
-                 exec_mode=IRR_EXEC_PARTITIONED, **cfg_kw):
+                 exec_mode=IRR_EXEC_PARTITIONED, user_launch=None, value_size=12, value_kind=1,
+                 **cfg_kw):
         self.num_edges = int(num_edges)
         self.num_nodes = int(num_nodes)
         self.node_elm = int(node_data_elm_size)
         self.red_elm = int(reduction_elm_size)
-        self.h = Handle(default_config(map_idx=map_idx, exec=exec_mode, **cfg_kw))
+        self.user = user_launch is not None
+        if self.user:
+            self.h = Handle(default_config(exec=exec_mode, **cfg_kw))
+            self.h.set_user_map(user_launch, value_size, value_kind)
+            if map_idx:
+                self.h.set_map(map_idx)
+            if node_coordinates is not None:
+                dt = np.float64 if int(coordinate_size) == 8 else np.float32
+                self.h.set_coordinates(np.asarray(node_coordinates, dt).reshape(self.num_nodes, int(node_num_dims)))
+        else:
+            self.h = Handle(default_config(map_idx=map_idx, exec=exec_mode, **cfg_kw))
         self.h.set_params(np.ascontiguousarray(parameter))
         self.h.set_edges(np.asarray(edges, np.int32).reshape(-1, 2)[: self.num_edges])
         self.h.set_nodes(node_data, self.node_elm, self.num_nodes)
@@ -755,8 +771,7 @@ class IrregularRuntime:
         self.h.set_map(idx)
 
     def set_reduce_idx(self, idx: int):
-        if idx != IRR_REDUCE_SUM:
-            raise IrregularError(IRR_ERR_ARG, f"unknown reduce index {idx}")
+        self.h.set_reduce(idx)
 
     def IrregularInit(self):
         self.h.init()

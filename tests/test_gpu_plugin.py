@@ -331,3 +331,24 @@ def test_user_map_without_edges(plugins):
     h = spring_handle(plugins["launch"]["spring"], nodes, x, np.zeros((0, 2), np.int32), para)
     h.step()
     assert np.all(h.get_result(elm_size=12) == 0)
+
+
+@pytest.mark.parametrize("user", [False, True])
+def test_python_irregular_runtime(plugins, oracle_lib, user):
+    """The ctypes IrregularRuntime mirror with moldyn's call sequence, on a
+    built-in law and on the application's map (the LJ fixture)."""
+    O = oracle_lib
+    c = load_golden("moldyn_random_2048")
+    pos = np.ascontiguousarray(c["pos"], np.float64)
+    n, e = pos.shape[0], c["edges"].shape[0]
+    kw = dict(user_launch=plugins["launch"]["lj"], value_size=12) if user else {}
+    rt = irr.IrregularRuntime(e, n, c["edges"], None, pos, 0, 24, 12, 3, pos, 8,
+                              parameter=np.asarray(c["param"], np.float64), parameter_size=16, **kw)
+    rt.IrregularInit()
+    for _ in range(2):
+        rt.reset_node_data(pos)
+        rt.IrregularStart()
+        f = rt.get_reduction_result()
+        rt.IrregularBarrier()
+    _, sabs = O.lj_reduce_f64(pos, c["edges"], oracle_param(O, c))
+    assert scaled_error(f, c["f_ref"], sabs) <= TOL_VS_REFERENCE
