@@ -561,6 +561,50 @@ int irr_ensure_layout(irr_handle* h, int lanes_per_row, int block_nodes, int sta
     return IRR_OK;
 }
 
+namespace {
+
+int set_nodes_range_common(irr_handle* h, const void* src, int elm, int64_t first, int64_t count,
+                           cudaMemcpyKind kind)
+{
+    if (!h || (!src && count > 0) || first < 0 || count < 0) return fail(h, IRR_ERR_ARG, "bad node range arguments");
+    if (h->n < 0) return fail(h, IRR_ERR_STATE, "irr_set_nodes_range before irr_set_nodes");
+    if (first + count > h->n)
+        return fail(h, IRR_ERR_ARG, "node range [%lld, %lld) outside %lld nodes", (long long)first,
+                    (long long)(first + count), (long long)h->n);
+    if (count == 0) return IRR_OK;
+    if (!h->inited || h->raw_pending || h->user_launch) {
+        // the records wait in d_raw, in the caller's order: patch them there
+        if (elm != h->raw_elm)
+            return fail(h, IRR_ERR_STATE, "record size %d differs from the node data's %d", elm, h->raw_elm);
+        if (h->inited && !h->raw_pending) {
+            // user map after init: d_raw is stale, so bring it up to date first
+            H_CUDA(h, launch_gather_records(h->d_rec, h->raw_elm, h->part.inv, h->n, h->d_raw, h->stream),
+                   "save node records");
+        }
+        H_CUDA(h, cudaMemcpyAsync(static_cast<char*>(h->d_raw) + (size_t)first * elm, src, (size_t)count * elm,
+                                  kind, h->stream), "copy node range");
+        h->raw_pending = true;
+        return IRR_OK;
+    }
+    if (!valid_node_elm(h, elm)) return fail(h, IRR_ERR_ARG, "node elm_size %d: use 12, 16 or 24", elm);
+    const void* rec = src;
+    if (kind == cudaMemcpyHostToDevice) {
+        rec = host_device_view(src);
+        if (!rec) {
+            int rc = ensure_raw(h, (size_t)h->n * elm);
+            if (rc) return rc;
+            H_CUDA(h, cudaMemcpyAsync(h->d_raw, src, (size_t)count * elm, kind, h->stream), "copy node range");
+            rec = h->d_raw;
+        }
+    }
+    // records [first, first + count) in the caller's order -> execution order
+    H_CUDA(h, launch_load_nodes_scatter(rec, elm, h->part.inv + first, count, h->d_pos, h->stream),
+           "load node range");
+    return IRR_OK;
+}
+
+}  // namespace
+
 extern "C" {
 
 void irr_config_default(irr_config* cfg)
@@ -1096,50 +1140,6 @@ int irr_set_shard(irr_handle* h, int64_t own_lo, int64_t own_hi)
     h->own_hi = own_hi;
     return IRR_OK;
 }
-
-namespace {
-
-int set_nodes_range_common(irr_handle* h, const void* src, int elm, int64_t first, int64_t count,
-                           cudaMemcpyKind kind)
-{
-    if (!h || (!src && count > 0) || first < 0 || count < 0) return fail(h, IRR_ERR_ARG, "bad node range arguments");
-    if (h->n < 0) return fail(h, IRR_ERR_STATE, "irr_set_nodes_range before irr_set_nodes");
-    if (first + count > h->n)
-        return fail(h, IRR_ERR_ARG, "node range [%lld, %lld) outside %lld nodes", (long long)first,
-                    (long long)(first + count), (long long)h->n);
-    if (count == 0) return IRR_OK;
-    if (!h->inited || h->raw_pending || h->user_launch) {
-        // the records wait in d_raw, in the caller's order: patch them there
-        if (elm != h->raw_elm)
-            return fail(h, IRR_ERR_STATE, "record size %d differs from the node data's %d", elm, h->raw_elm);
-        if (h->inited && !h->raw_pending) {
-            // user map after init: d_raw is stale, so bring it up to date first
-            H_CUDA(h, launch_gather_records(h->d_rec, h->raw_elm, h->part.inv, h->n, h->d_raw, h->stream),
-                   "save node records");
-        }
-        H_CUDA(h, cudaMemcpyAsync(static_cast<char*>(h->d_raw) + (size_t)first * elm, src, (size_t)count * elm,
-                                  kind, h->stream), "copy node range");
-        h->raw_pending = true;
-        return IRR_OK;
-    }
-    if (!valid_node_elm(h, elm)) return fail(h, IRR_ERR_ARG, "node elm_size %d: use 12, 16 or 24", elm);
-    const void* rec = src;
-    if (kind == cudaMemcpyHostToDevice) {
-        rec = host_device_view(src);
-        if (!rec) {
-            int rc = ensure_raw(h, (size_t)h->n * elm);
-            if (rc) return rc;
-            H_CUDA(h, cudaMemcpyAsync(h->d_raw, src, (size_t)count * elm, kind, h->stream), "copy node range");
-            rec = h->d_raw;
-        }
-    }
-    // records [first, first + count) in the caller's order -> execution order
-    H_CUDA(h, launch_load_nodes_scatter(rec, elm, h->part.inv + first, count, h->d_pos, h->stream),
-           "load node range");
-    return IRR_OK;
-}
-
-}  // namespace
 
 int irr_set_nodes_range(irr_handle* h, const void* node_data, int elm_size, int64_t first, int64_t count)
 {
