@@ -563,6 +563,9 @@ def run_sharded(args, rank, world, local):
     h.init()
     loc = torch.from_numpy(loc_np).to(f"cuda:{dev}")
     hx = sharding.HaloExchange(lp, f"cuda:{dev}")
+    # a collective first, so that the exchange's batched point-to-point calls
+    # are not the group's first NCCL operation (which every rank must join)
+    barrier(world)
     below = loc[:lp.own_lo]
     above = loc[lp.own_hi:]
 
