@@ -33,7 +33,9 @@ Our arm prints one JSON line with
                run (N = 1): the 1,048,576-atom MD loop, 512 batched instances
                in one graph-captured persistent launch per step against the
                same instances run one by one, and the served stream (p50 /
-               p99 latency, throughput against serial execution, capacity).
+               p99 latency, throughput against serial execution, capacity);
+  plugin       the same workload through the irregular.h plugin: the LJ law
+               as an application's FP64 user map, compiled at run time.
 `--impl reference` times that CPU executor alone (rank 0; other ranks exit).
 With N > 1 (torchrun) the workload is split into N shards of the node order,
 one per rank, with the halo positions exchanged over NCCL every step (strong
@@ -505,6 +507,7 @@ def run_ours(args, rank, world, local):
         line["md"] = run_md(args)
         line["batched"] = run_batched(args)
         line["served"] = run_served(args)
+        line["plugin"] = run_plugin(args, pos, side)
     elif args.legs == "all":
         line["legs"] = "md / batched / served run at N = 1 only"
     if rank == 0:
@@ -634,6 +637,63 @@ def run_sharded(args, rank, world, local):
     if rank == 0:
         print(json.dumps(line), flush=True)
     return 0
+
+
+def run_plugin(args, pos, side):
+    """The irregular.h plugin path on the same workload: the LJ law written
+    as an application's FP64 user map (tests/plugin/lj/irregular.h, the
+    reference's irregular.h form), compiled through the compat shim
+    (compat/irregular/irr_user_map.cu, one map inlined, compensated float
+    sums) and run by a partitioned handle (irr_set_user_map).  Returns the
+    leg's JSON object, or its reason for being unavailable."""
+    import ctypes as C
+
+    import irregular_gb300 as irr
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from plugin_build import build_plugins
+
+    out = {"leg": "plugin", "map": "LJ as an FP64 user map (irregular.h form), IRR_PLUGIN_INLINE_MAP, "
+                                   "IRR_PLUGIN_COMPENSATED"}
+    lib_path = os.path.join(tempfile.mkdtemp(), "libplugin_lj.so")
+    try:
+        build_plugins({"lj": (os.path.join(ROOT, "tests", "plugin", "lj"), lib_path, True,
+                              ("IRR_PLUGIN_INLINE_MAP=lj_box", "IRR_PLUGIN_COMPENSATED"), True)})
+    except Exception as e:  # no nvcc on the host running the bench
+        out["unavailable"] = str(e).splitlines()[0][:200]
+        return out
+    lib = C.CDLL(lib_path)
+    fn = C.cast(lib.irr_compat_user_launch, C.c_void_p).value
+    n = pos.shape[0]
+    edges = irr.neighbor_build(pos, float(side), CUTOFF * CUTOFF)
+    E = edges.count
+    h = irr.Handle(irr.default_config(exec=irr.IRR_EXEC_PARTITIONED))
+    h.set_user_map(fn, 12, 1)
+    h.set_params(np.array([float(side), CUTOFF], np.float64))
+    h.set_edges(edges)
+    h.set_nodes(pos.astype(np.float64), 24)
+    h.init()
+    for _ in range(3):
+        h.step()
+    h.sync()
+    steps = 20
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        h.step()
+    h.sync()
+    dt = (time.perf_counter() - t0) / steps
+    f = h.get_result(elm_size=12)
+    host_edges = edges.to_host()
+    smp = np.sort(np.random.Generator(np.random.PCG64(SEED + 1)).choice(n, min(n, FORCE_SAMPLE),
+                                                                        replace=False))
+    g, sabs, sinf = fp64_forces(pos, incident(host_edges, n, smp), float(side), CUTOFF)
+    out.update({"ms_per_step": 1e3 * dt, "edges_per_s": E / dt, "steps": steps,
+                "timing": "host wall clock around synchronised steps",
+                "force_err": force_err(f[smp], g[smp], sabs[smp], sinf[smp]),
+                "note": "FP64-pipe bound: two FP64 law evaluations per edge; the built-in FP32 law "
+                        "is the fast path"})
+    h.close()
+    edges.close()
+    return out
 
 
 def run_batched(args):
