@@ -693,7 +693,9 @@ __device__ __forceinline__ float4 lds128(uint32_t addr)
 // slice fills split off into a loop without the entry masks (spills) 0.410;
 // sleep-free waits 0.393, and polls that sleep up to 128 ns to 2 us between
 // tests all 0.3875-0.3878; the entry masks as per-slice step-count bounds
-// (t < n0, t < n1 instead of 8t + lane < len) 0.4163; 3-stage
+// (t < n0, t < n1 instead of 8t + lane < len) 0.4163, but as bounds on the
+// step's word address, which the loop advances anyway (no step counter or
+// index add left), 0.3736 vs 0.3876 -- the loop below; 3-stage
 // rings (3 CTAs per SM, or smaller items at 4) 0.395-0.431; 4 or 6 consumer
 // warps with 6 or 7 CTAs per SM 0.413-0.418; each item's steps cut evenly
 // across the warps (slices split between warps, piece sums joined in shared
