@@ -335,15 +335,13 @@ int launch_reduction(irr_handle* h)
 int ensure_pipe(irr_handle* h, size_t in_bytes, size_t out_bytes)
 {
     irr_handle::Pipe& P = h->pipe;
-    if (!P.s_in) {
-        H_CUDA(h, cudaStreamCreateWithFlags(&P.s_in, cudaStreamNonBlocking), "pipeline stream");
-        H_CUDA(h, cudaStreamCreateWithFlags(&P.s_out, cudaStreamNonBlocking), "pipeline stream");
-        for (int s = 0; s < 2; s++) {
-            H_CUDA(h, cudaEventCreateWithFlags(&P.in_done[s], cudaEventDisableTiming), "pipeline event");
-            H_CUDA(h, cudaEventCreateWithFlags(&P.in_free[s], cudaEventDisableTiming), "pipeline event");
-            H_CUDA(h, cudaEventCreateWithFlags(&P.out_ready[s], cudaEventDisableTiming), "pipeline event");
-            H_CUDA(h, cudaEventCreateWithFlags(&P.out_free[s], cudaEventDisableTiming), "pipeline event");
-        }
+    // each object made once; after a failed call the next one makes what is missing
+    if (!P.s_in) H_CUDA(h, cudaStreamCreateWithFlags(&P.s_in, cudaStreamNonBlocking), "pipeline stream");
+    if (!P.s_out) H_CUDA(h, cudaStreamCreateWithFlags(&P.s_out, cudaStreamNonBlocking), "pipeline stream");
+    for (int s = 0; s < 2; s++) {
+        cudaEvent_t* evs[4] = {&P.in_done[s], &P.in_free[s], &P.out_ready[s], &P.out_free[s]};
+        for (cudaEvent_t* ev : evs)
+            if (!*ev) H_CUDA(h, cudaEventCreateWithFlags(ev, cudaEventDisableTiming), "pipeline event");
     }
     if (in_bytes > P.in_cap || out_bytes > P.out_cap) {
         // no step in flight may use the old staging
