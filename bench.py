@@ -26,7 +26,7 @@ Our arm prints one JSON line with
                cores over a bounded sample of the same edge list;
   clocks       nvidia-smi samples taken during the timed region;
   force_err    a seeded sample of 2,000 nodes recomputed in FP64 by this
-               file's own checker (fp64_forces): normwise, per node against
+               file's own FP64 recomputation (fp64_forces): normwise, per node against
                the terms' magnitudes, and per result (p50 / p99 / max);
   md, batched, served
                the other configurations of the metric, measured in the same
@@ -63,7 +63,7 @@ for _p in (ROOT, PKG):
 import numpy as np  # noqa: E402
 
 N_NODES = 4194304
-FORCE_SAMPLE = 2000   # nodes whose results the FP64 checker recomputes
+FORCE_SAMPLE = 2000   # nodes whose results the FP64 recomputation covers
 LAYOUTS = {"auto": 0, "csr": 1, "sliced": 2, "staged": 3}  # enum irr_layout
 CUTOFF = 2.5
 DENSITY = 64.0 / (4.0 / 3.0 * math.pi * CUTOFF ** 3)
@@ -110,7 +110,7 @@ def ncu_traffic(key: str):
 
 
 def fp64_forces(pos32, edges, side: float, cutoff: float, periodic: bool = True):
-    """FP64 checker for the force-error fields: the LJ law d (r^-14 - r^-8/2) of
+    """FP64 recomputation for the force-error fields: the LJ law d (r^-14 - r^-8/2) of
     the reference's `map` (moldyn/irregular.h:47-78) on the float positions
     widened to double, minimum image in a cube of side `side`, applied when
     r^2 < cutoff^2, +f to idx0 and -f to idx1.  Returns per node the forces,
@@ -153,7 +153,7 @@ def incident(edges, n: int, sample):
 
 
 def force_err(f, f64, sabs, sinf) -> dict:
-    """Errors of results f against the FP64 checker, on the nodes given:
+    """Errors of results f against the FP64 recomputation, on the nodes given:
     normwise max|df| / max|f64|; per node and component |df| / sabs (sabs: the
     terms' magnitudes); and per result |df|inf / max(|f64|inf, 2^-10 sinf) at
     the median, 99th percentile and worst node."""
@@ -321,7 +321,8 @@ def run_reference(args, rank, world):
                                    "1,000,000 would leave most threads idle on the sample",
                    "kind": "port",
                    "why_port": "the reference's CPU code, compiled from its own sources, needs "
-                               "the reference tree, which the GPU box does not hold, and its "
+                               "the reference tree at run time, which a deployment of this repository does not "
+                               "include, and its "
                                "1,048,577-bucket table overflows (its insert then spins) at "
                                "4,194,304 nodes",
                    "threads": threads,
@@ -393,7 +394,7 @@ def run_ours(args, rank, world, local):
                               "layout": args.layout, "ms_per_step": ms / args.steps}), flush=True)
         return 0
 
-    # force error of the timed configuration on a seeded node sample (FP64 checker)
+    # force error of the timed configuration on a seeded node sample (FP64 recomputation)
     err = None
     if rank == 0:
         f_gpu = h.get_result(elm_size=12)
@@ -601,7 +602,7 @@ def run_sharded(args, rank, world, local):
     barrier(world)
     ms = max_over_ranks(ms, world)
     value = E * args.steps / (ms / 1e3)
-    # force error of this rank's owned rows on a seeded sample (FP64 checker)
+    # force error of this rank's owned rows on a seeded sample (FP64 recomputation)
     err = None
     if rank == 0:
         f_own = h.get_result(elm_size=12)
@@ -830,7 +831,7 @@ def run_md(args):
     ke1, pe1, vir1 = md.energy()
     n = pos.shape[0]
     info = md.info()
-    # forces at the end against the FP64 checker (x48: the MD's force units)
+    # forces at the end against the FP64 recomputation (x48: the MD's force units)
     gp, _ = md.state()
     f_gpu = md.forces()
     p32 = gp.astype(np.float32)

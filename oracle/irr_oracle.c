@@ -1,8 +1,9 @@
 /*
  * irr_oracle.c -- CPU oracle for the irregular-reduction hot path.
  *
- * TEST INFRASTRUCTURE ONLY: the checker for tests/, __graft_entry__.smoke()
- * and the timed CPU baseline of bench.py.  The product library never links or
+ * TEST INFRASTRUCTURE ONLY: the reference results that tests/ and
+ * __graft_entry__.smoke() compare against, and the timed CPU baseline of
+ * bench.py.  The product library never links or
  * calls it.  Compile with -ffp-contract=off: every double and float operation
  * below is meant to round on its own, as the reference's CPU code does when
  * built without FMA contraction.

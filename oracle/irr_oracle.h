@@ -3,8 +3,8 @@
  *
  * TEST INFRASTRUCTURE ONLY.  Nothing in the product library links, loads or
  * calls this code; only tests/, __graft_entry__.smoke() and bench.py's
- * cpu_baseline / --impl reference legs use it, and only as the checker or as
- * the timed CPU baseline.
+ * cpu_baseline / --impl reference legs use it, and only as the reference
+ * results they compare against or as the timed CPU baseline.
  *
  * It restates, in plain C, the arithmetic of the reference's CPU path:
  *   - the per-edge user function `map` (moldyn/irregular.h:26-107) and

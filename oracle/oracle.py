@@ -1,8 +1,8 @@
 """ctypes front end of the CPU oracle (test infrastructure only).
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline legs import
-this module, and only as the checker or the timed CPU baseline; the product
-library never does.  It loads
+this module, and only for reference results to compare against or the timed
+CPU baseline; the product library never does.  It loads
 
   oracle/liboracle.so          the C restatement of the reference's CPU path
                                (irr_oracle.c; provenance in irr_oracle.h), and
