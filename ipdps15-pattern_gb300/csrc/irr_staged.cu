@@ -161,9 +161,13 @@ __global__ void __launch_bounds__(kBuildThreads) staged_fill_kernel(
     for (int k = threadIdx.x; k < kHashSlots; k += blockDim.x)
         if (set[k] != -1) tab[atomicAdd(&count, 1)] = set[k];
     __syncthreads();
-    for (int size = 2; size <= kSortCap; size <<= 1)
+    // the INT_MAX padding sorts last, so sorting the first power of two that
+    // holds the table gives the same first ntab ids as sorting all kSortCap
+    int sort_n = 2;
+    while (sort_n < ntab) sort_n <<= 1;
+    for (int size = 2; size <= sort_n; size <<= 1)
         for (int stride = size >> 1; stride > 0; stride >>= 1) {
-            for (int k = threadIdx.x; k < kSortCap / 2; k += blockDim.x) {
+            for (int k = threadIdx.x; k < sort_n / 2; k += blockDim.x) {
                 const int lo = 2 * k - (k & (stride - 1));
                 const int hi = lo + stride;
                 const bool up = (lo & size) == 0;
@@ -203,28 +207,43 @@ __global__ void __launch_bounds__(kBuildThreads) staged_fill_kernel(
     uint32_t* sw = words + slice_off[q];
     int len = 0, own = 0;
     uint32_t hdr = 1u << 31;  // a padding row
-    int cnt[8], beg[8], cur[8];
+    // per bank group: the next unused slot of its bucket in rs and the
+    // bucket's end (indexed by compile-time constants only: registers)
+    int nxt[8], end[8];
 #pragma unroll
-    for (int g = 0; g < 8; g++) cnt[g] = beg[g] = cur[g] = 0;
+    for (int g = 0; g < 8; g++) nxt[g] = end[g] = 0;
     if (tid < m) {
         const int lrow = order[tid];
         const int64_t r = (int64_t)w.row0 + lrow;
         const int base = (int)(row_off[r] - e0);
         len = (int)(row_off[r + 1] - row_off[r]);
         own = slot_of(tab, ntab, (int32_t)r);
-        for (int k = 0; k < len; k++) cnt[slots[base + k] & 7]++;
+        int cnt[8];
+#pragma unroll
+        for (int g = 0; g < 8; g++) cnt[g] = 0;
+        for (int k = 0; k < len; k++) {
+            const int g = slots[base + k] & 7;
+#pragma unroll
+            for (int x = 0; x < 8; x++) cnt[x] += (g == x) ? 1 : 0;
+        }
         int acc = base;
 #pragma unroll
         for (int g = 0; g < 8; g++) {
-            beg[g] = acc;
+            nxt[g] = acc;
             acc += cnt[g];
+            end[g] = acc;
         }
         int fill[8];
 #pragma unroll
-        for (int g = 0; g < 8; g++) fill[g] = beg[g];
+        for (int g = 0; g < 8; g++) fill[g] = nxt[g];
         for (int k = 0; k < len; k++) {
             const uint16_t sl = slots[base + k];
-            rs[fill[sl & 7]++] = sl;
+            const int g = sl & 7;
+            int at = 0;
+#pragma unroll
+            for (int x = 0; x < 8; x++)
+                if (g == x) at = fill[x]++;
+            rs[at] = sl;
         }
         hdr = (uint32_t)(own * 16) | ((uint32_t)len << 14) | ((uint32_t)lrow << 24);
     }
@@ -232,17 +251,35 @@ __global__ void __launch_bounds__(kBuildThreads) staged_fill_kernel(
     const int p = i & 1;
     for (int t = 0; t < T; t++) {
         uint32_t pk[2][4];
+#pragma unroll
         for (int h = 0; h < 2; h++)
+#pragma unroll
             for (int l = 0; l < 4; l++) {
-                int g = (2 * t + h + 4 * p + l) & 7;
-                if (cur[g] >= cnt[g]) {
-                    int best = -1;
+                // the window's group if its bucket has slots left, else the
+                // group with the most left (the first such on ties), else
+                // padding (the row's own slot)
+                const int g0 = (2 * t + h + 4 * p + l) & 7;
+                int take = -1;
+#pragma unroll
+                for (int x = 0; x < 8; x++)
+                    if (x == g0 && nxt[x] < end[x]) take = x;
+                if (take < 0) {
+                    int most = 0;
+#pragma unroll
                     for (int x = 0; x < 8; x++)
-                        if (cnt[x] - cur[x] > 0 && (best < 0 || cnt[x] - cur[x] > cnt[best] - cur[best])) best = x;
-                    g = best;
+                        if (end[x] - nxt[x] > most) {
+                            most = end[x] - nxt[x];
+                            take = x;
+                        }
                 }
                 int slot = own;
-                if (g >= 0) slot = rs[beg[g] + cur[g]++];
+                if (take >= 0) {
+                    int at = 0;
+#pragma unroll
+                    for (int x = 0; x < 8; x++)
+                        if (x == take) at = nxt[x]++;
+                    slot = rs[at];
+                }
                 pk[h][l] = (uint32_t)(slot * 16);
             }
         *reinterpret_cast<uint4*>(sw + 32 * (t + 1) + 4 * i) =
