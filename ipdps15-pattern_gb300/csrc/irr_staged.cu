@@ -288,6 +288,36 @@ __global__ void __launch_bounds__(kBuildThreads) staged_fill_kernel(
     }
 }
 
+// out[j] = the length at position 8 j of an item's m row lengths in descending
+// order (the longest row of slice j once the rows are ordered longest first),
+// j < ceil(m / 8).  The lengths of an item's rows span a narrow range, so a
+// histogram over [min, max] finds them without sorting; wide ranges sort.
+void slice_longest(const uint32_t* lens, int m, uint32_t* out)
+{
+    static_assert(8 * kHaloSlicesPerItem <= 64, "an item holds at most 64 rows");
+    const int ns = (m + 7) / 8;
+    uint32_t lo = lens[0], hi = lens[0];
+    for (int k = 1; k < m; k++) {
+        lo = std::min(lo, lens[k]);
+        hi = std::max(hi, lens[k]);
+    }
+    if (hi - lo < 256) {
+        uint16_t cnt[256];
+        std::fill(cnt, cnt + (hi - lo + 1), (uint16_t)0);
+        for (int k = 0; k < m; k++) cnt[lens[k] - lo]++;
+        int pos = 0, j = 0;
+        for (uint32_t v = hi + 1; v-- > lo && j < ns;) {
+            pos += cnt[v - lo];
+            while (j < ns && 8 * j < pos) out[j++] = v;
+        }
+    } else {
+        uint32_t sorted[64];
+        std::copy(lens, lens + m, sorted);
+        std::sort(sorted, sorted + m, [](uint32_t x, uint32_t y) { return x > y; });
+        for (int j = 0; j < ns; j++) out[j] = sorted[8 * j];
+    }
+}
+
 template <class T>
 cudaError_t alloc_n(T** p, int64_t count, cudaStream_t s)
 {
@@ -376,19 +406,17 @@ cudaError_t build_staged(const uint32_t* row_off, const int32_t* col, const uint
     // the slices' word offsets, rows ordered longest first within each item
     std::vector<uint32_t> fin((size_t)S + 1, 0);
     uint64_t acc = 0, tab = 0;
-    std::vector<uint32_t> lens;
+    uint32_t lens[64], longest_of[kHaloSlicesPerItem];
     for (WorkItem& w : items) {
         w.tab0 = (uint32_t)tab;
         tab += w.ntab;
         if (tab > 0x7fffffffull) return cudaErrorNotSupported;
-        lens.clear();
-        for (int k = 0; k < w.nrows; k++)
-            lens.push_back(host_row_off[w.row0 + k + 1] - host_row_off[w.row0 + k]);
-        std::stable_sort(lens.begin(), lens.end(), [](uint32_t x, uint32_t y) { return x > y; });
+        for (int k = 0; k < w.nrows; k++) lens[k] = host_row_off[w.row0 + k + 1] - host_row_off[w.row0 + k];
+        slice_longest(lens, w.nrows, longest_of);
         const int64_t q0 = w.row0 / 8, ns = (w.nrows + 7) / 8;
         w.ent0 = (uint32_t)acc;
         for (int64_t j = 0; j < ns; j++) {
-            const uint32_t longest = lens[(size_t)(8 * j)];  // the first of a slice is its longest
+            const uint32_t longest = longest_of[j];  // the first of a slice is its longest
             acc += 32ull * ((longest + 7) / 8 + 1);
             if (acc > 0xffffffffull) return cudaErrorNotSupported;
             fin[(size_t)(q0 + j) + 1] = (uint32_t)acc;
