@@ -228,3 +228,27 @@ def test_local_problems_keep_every_owned_row(oracle_lib):
             got = np.sort(np.concatenate([v for v in lp.recv_local.values()])) if lp.recv_local else []
             halo = np.r_[np.arange(0, lp.own_lo), np.arange(lp.own_hi, lp.nodes.shape[0])]
             assert np.array_equal(got, halo)
+
+
+def test_plan_edge_cases():
+    """More shards than rows (some shards own nothing), and a graph with no
+    entries: the shards still tile the rows in order, empty shards have no
+    halo and an empty local problem, and every owned row is kept."""
+    import sharding
+    row_off = np.array([0, 2, 3, 5, 6, 6], np.uint32)
+    col = np.array([1, 2, 0, 0, 4, 2], np.int32)
+    for parts in (1, 3, 5, 8):
+        shards = sharding.plan(row_off, col, parts)
+        assert len(shards) == parts
+        assert shards[0].lo == 0 and shards[-1].hi == 5
+        assert all(a.hi == b.lo for a, b in zip(shards, shards[1:]))
+        for sh in shards:
+            lp = sharding.local_problem(sh, row_off, col)
+            if sh.hi == sh.lo:
+                assert sh.halo.size == 0 and lp.nodes.size == 0
+                continue
+            ro, cc = sharding.local_rows(lp)
+            assert np.array_equal(lp.nodes[cc], col[row_off[sh.lo]:row_off[sh.hi]])
+    empty = sharding.plan(np.zeros(4, np.uint32), np.zeros(0, np.int32), 3)
+    assert [(s.lo, s.hi) for s in empty][-1][1] == 3
+    assert all(s.halo.size == 0 for s in empty)
